@@ -1,0 +1,86 @@
+"""ctypes binding of libaugur_gb300.so (the C ABI declared in include/augur_pm.h).
+
+The product path has no fallback: if the library is missing or a call fails, a
+RuntimeError says why. Build it with ``python -m augur_gb300.build`` (or
+``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libaugur_gb300.so"
+
+AUGUR_MODE_PERIODIC = 0
+AUGUR_MODE_ISOLATED_SOFTENED = 1
+
+_vp, _i64, _i32, _f32, _f64 = C.c_void_p, C.c_int64, C.c_int, C.c_float, C.c_double
+
+# name -> (restype, argtypes); every symbol include/*.h declares is listed here
+SIGNATURES = {
+    "augur_status_string": (C.c_char_p, [_i32]),
+    "augur_version": (_i32, []),
+    "augur_pm_plan_create": (_i32, [C.POINTER(_vp), _i32, _i32, _i64, _i32, _f64, _f64, _f64]),
+    "augur_pm_plan_destroy": (_i32, [_vp]),
+    "augur_pm_plan_workspace_bytes": (_i64, [_vp]),
+    "augur_pm_cell_index": (_i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "augur_pm_deposit": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp]),
+    "augur_pm_poisson": (_i32, [_vp, _vp, _vp, _vp]),
+    "augur_pm_gather": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    "augur_pm_force": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+    "augur_pm_step": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp]),
+    "augur_pm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp]),
+    "augur_pm_run_begin": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),
+    "augur_pm_run_steps": (_i32, [_vp, _i32, _vp]),
+    "augur_pm_run_end": (_i32, [_vp, _vp, _vp, _vp, _vp]),
+    "augur_pm_last_launches": (_i64, [_vp]),
+    "augur_pm_check": (_i32, [_vp, _vp]),
+    "augur_direct_sum_fp64": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp]),
+    "augur_energy_fp64": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the library once; raises RuntimeError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"augur_gb300 native library not built: {LIB_PATH} is missing "
+                           "(run python -m augur_gb300.build)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            if name in OPTIONAL:
+                continue
+            raise RuntimeError(f"{LIB_PATH.name} does not export {name}")
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+OPTIONAL: set[str] = set()
+
+
+def status_text(rc: int) -> str:
+    return load().augur_status_string(rc).decode()
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed: {status_text(rc)} (status {rc})")
+
+
+def register(name: str, restype, argtypes, optional: bool = False) -> None:
+    """Declare an additional exported symbol (used by sibling modules)."""
+    SIGNATURES[name] = (restype, argtypes)
+    if optional:
+        OPTIONAL.add(name)
+    if _lib is not None:
+        fn = getattr(_lib, name, None)
+        if fn is not None:
+            fn.restype, fn.argtypes = restype, argtypes

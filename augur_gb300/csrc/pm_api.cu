@@ -1,0 +1,694 @@
+// pm_api.cu — C ABI of the PM gravity step: plan, workspace and kernel orchestration.
+//
+// One plan = one grid geometry + the device workspace for up to max_bodies bodies.
+// Every call enqueues kernels on the caller's stream and returns without a host
+// synchronisation (augur_pm_check is the exception), so a step can be captured in a
+// CUDA graph by the caller.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "pm_kernels.cuh"
+
+using namespace augur;
+
+struct augur_pm_plan {
+  int dim, G, mode;
+  double extent, eps, gnewton;
+  int64_t max_n;
+  GridParams gp;
+  int nrow, ntiles;
+  int L, M, Lt;  // transform length (G periodic, 2G isolated), half length, twiddle table length
+  FftShape sh_M, sh_L;
+  int dep_RY, dep_RZ, green_TY, c2r_RB, rows_RB, r2c_RB;
+  size_t smem_dep, smem_green, smem_c2r, smem_rows, smem_r2c;
+  float2 *tw;
+  float4 *pos4[2], *vel4[2];
+  int cur;
+  uint32_t *key, *slot, *row_count, *row_start, *tile_sum, *tile_off;
+  unsigned *d_err, *d_mmax;
+  float2 *spec, *spec3, *khat;
+  float4 *F4;
+  float *real_tmp, *phi2d, *rho2d;
+  int64_t run_n;
+  float run_dt;
+  int run_active;
+  int64_t launches;
+  size_t bytes;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA; }
+
+#define AUGUR_LAUNCH_CHECK(plan)                      \
+  do {                                                \
+    (plan)->launches++;                               \
+    cudaError_t _e = cudaGetLastError();              \
+    if (_e != cudaSuccess) {                          \
+      fprintf(stderr, "augur: launch failed: %s (%s:%d)\n", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return AUGUR_ECUDA;                             \
+    }                                                 \
+  } while (0)
+
+bool factor(int L, FftShape &sh) {
+  sh.L = L;
+  sh.nstages = 0;
+  int r = L;
+  while (r % 3 == 0) {
+    sh.radix[sh.nstages++] = 3;
+    r /= 3;
+  }
+  int e = 0;
+  while (r % 2 == 0) {
+    r /= 2;
+    ++e;
+  }
+  if (r != 1) return false;
+  if (e == 1) {
+    sh.radix[sh.nstages++] = 2;
+  } else if (e > 1) {
+    int q = e / 3, rem = e % 3;
+    if (rem == 1) {
+      q -= 1;
+      sh.radix[sh.nstages++] = 4;
+      sh.radix[sh.nstages++] = 4;
+    } else if (rem == 2) {
+      sh.radix[sh.nstages++] = 4;
+    }
+    for (int i = 0; i < q; ++i) sh.radix[sh.nstages++] = 8;
+  }
+  return sh.nstages <= 12;
+}
+
+template <typename T>
+int dalloc(augur_pm_plan *p, T **ptr, size_t count) {
+  *ptr = nullptr;
+  if (count == 0) return AUGUR_OK;
+  size_t b = count * sizeof(T);
+  if (cudaMalloc((void **)ptr, b) != cudaSuccess) {
+    *ptr = nullptr;
+    cudaGetLastError();
+    return AUGUR_ENOMEM;
+  }
+  p->bytes += b;
+  return AUGUR_OK;
+}
+
+unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+// ---- pipeline pieces ----------------------------------------------------------------
+
+int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *acc, const float *mass,
+                  const float *mask, int64_t n, bool drift, float dt, cudaStream_t st) {
+  const GridParams &g = p->gp;
+  if (cudaMemsetAsync(p->row_count, 0, sizeof(uint32_t) * p->nrow, st) != cudaSuccess) return AUGUR_ECUDA;
+  if (cudaMemsetAsync(p->d_mmax, 0, sizeof(unsigned), st) != cudaSuccess) return AUGUR_ECUDA;
+  const unsigned nb = blocks_for(n, 256);
+  const float hdt2 = (float)(0.5 * (double)dt * (double)dt);
+  if (n > 0) {
+    if (p->dim == 3) {
+      if (drift)
+        keys_hist_aos_kernel<3, true><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key, p->slot,
+                                                         p->row_count, p->d_mmax, p->d_err);
+      else
+        keys_hist_aos_kernel<3, false><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key,
+                                                          p->slot, p->row_count, p->d_mmax, p->d_err);
+    } else {
+      if (drift)
+        keys_hist_aos_kernel<2, true><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key, p->slot,
+                                                         p->row_count, p->d_mmax, p->d_err);
+      else
+        keys_hist_aos_kernel<2, false><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key,
+                                                          p->slot, p->row_count, p->d_mmax, p->d_err);
+    }
+    AUGUR_LAUNCH_CHECK(p);
+  }
+  scan_local_kernel<<<p->ntiles, 1024, 0, st>>>(p->row_count, p->row_start, p->tile_sum, p->nrow);
+  AUGUR_LAUNCH_CHECK(p);
+  scan_tiles_kernel<<<1, 1024, 0, st>>>(p->tile_sum, p->tile_off, p->ntiles);
+  AUGUR_LAUNCH_CHECK(p);
+  if (n > 0) {
+    if (p->dim == 3)
+      scatter_aos_kernel<3><<<nb, 256, 0, st>>>(pos, vel, mass, mask, n, p->key, p->slot, p->row_start, p->tile_off,
+                                                p->pos4[p->cur], p->vel4[p->cur]);
+    else
+      scatter_aos_kernel<2><<<nb, 256, 0, st>>>(pos, vel, mass, mask, n, p->key, p->slot, p->row_start, p->tile_off,
+                                                p->pos4[p->cur], p->vel4[p->cur]);
+    AUGUR_LAUNCH_CHECK(p);
+  }
+  return AUGUR_OK;
+}
+
+// re-sort the run state after a gather that produced keys + histogram
+int resort(augur_pm_plan *p, cudaStream_t st) {
+  const int64_t n = p->run_n;
+  scan_local_kernel<<<p->ntiles, 1024, 0, st>>>(p->row_count, p->row_start, p->tile_sum, p->nrow);
+  AUGUR_LAUNCH_CHECK(p);
+  scan_tiles_kernel<<<1, 1024, 0, st>>>(p->tile_sum, p->tile_off, p->ntiles);
+  AUGUR_LAUNCH_CHECK(p);
+  if (n > 0) {
+    const int c = p->cur;
+    scatter_sorted_kernel<<<blocks_for(n, 256), 256, 0, st>>>(p->pos4[c], p->vel4[c], n, p->key, p->slot,
+                                                              p->row_start, p->tile_off, p->pos4[c ^ 1],
+                                                              p->vel4[c ^ 1]);
+    AUGUR_LAUNCH_CHECK(p);
+    p->cur ^= 1;
+  }
+  return AUGUR_OK;
+}
+
+DepositArgs dep_args(const augur_pm_plan *p) {
+  DepositArgs a;
+  a.g = p->gp;
+  a.RY = p->dep_RY;
+  a.RZ = p->dim == 3 ? p->dep_RZ : 1;
+  a.fsh = p->sh_M;
+  a.twmul = p->Lt / p->M;
+  a.Lt = p->Lt;
+  return a;
+}
+
+unsigned dep_blocks(const augur_pm_plan *p) {
+  const int G = p->G;
+  return p->dim == 3 ? (unsigned)((G / p->dep_RY) * (G / p->dep_RZ)) : (unsigned)(G / p->dep_RY);
+}
+
+int deposit_rho(augur_pm_plan *p, float *rho, cudaStream_t st) {
+  DepositArgs a = dep_args(p);
+  size_t sm = (size_t)a.RY * a.RZ * p->G * 12 + (size_t)a.RY * a.RZ * 8;
+  if (p->dim == 3)
+    deposit_kernel<3, 0><<<dep_blocks(p), 512, sm, st>>>(p->pos4[p->cur], p->row_start, p->tile_off, p->d_mmax, a,
+                                                          p->tw, rho, nullptr, p->d_err);
+  else
+    deposit_kernel<2, 0><<<dep_blocks(p), 512, sm, st>>>(p->pos4[p->cur], p->row_start, p->tile_off, p->d_mmax, a,
+                                                          p->tw, rho, nullptr, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int fft_rows(augur_pm_plan *p, float2 *data, int64_t nrows, bool inverse, cudaStream_t st) {
+  const int L = p->L;
+  const int RB = p->rows_RB;
+  fft_rows_kernel<<<blocks_for(nrows, RB), 256, p->smem_rows, st>>>(data, nrows, RB, L, p->sh_L, p->Lt / L, p->Lt,
+                                                                     p->tw, inverse ? 1 : 0);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+// periodic 3D: spec (after R2C along x) -> F4 force grid
+int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
+  const int G = p->G, M = p->M;
+  int rc = fft_rows(p, p->spec, (int64_t)(M + 1) * G, false, st);
+  if (rc) return rc;
+  GreenArgs ga;
+  ga.G = G;
+  ga.TY = p->green_TY;
+  ga.ncomp = ncomp;
+  ga.Lt = p->Lt;
+  ga.fsh = p->sh_L;
+  ga.kfund = (float)(2.0 * M_PI / p->extent);
+  ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
+  fft_z_green_kernel<<<(unsigned)((M + 1) * (G / p->green_TY)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
+                                                                                           p->spec3);
+  AUGUR_LAUNCH_CHECK(p);
+  rc = fft_rows(p, p->spec3, (int64_t)ncomp * (M + 1) * G, true, st);
+  if (rc) return rc;
+  C2RArgs ca;
+  ca.L = G;
+  ca.nrows = G * G;
+  ca.RB = p->c2r_RB;
+  ca.ncomp = ncomp;
+  ca.Lt = p->Lt;
+  ca.nkeep = G * G;
+  ca.Lkeep = G;
+  ca.scale = 1.f;
+  ca.fsh = p->sh_M;
+  ca.twmul = p->Lt / M;
+  c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec3, ca, p->tw,
+                                                                                 reinterpret_cast<float *>(F4));
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int r2c_rows(augur_pm_plan *p, const float *in, int Lin, int nin, int nout, float2 *out, cudaStream_t st) {
+  RowsArgs ra;
+  ra.L = p->L;
+  ra.Lin = Lin;
+  ra.nin = nin;
+  ra.nout = nout;
+  ra.RB = p->r2c_RB;
+  ra.Lt = p->Lt;
+  ra.fsh = p->sh_M;
+  ra.twmul = p->Lt / p->M;
+  r2c_rows_kernel<<<blocks_for(nout, ra.RB), 256, p->smem_r2c, st>>>(in, ra, p->tw, out);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+// isolated 2D: rho (G x G) -> F4 (G x G)
+int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream_t st) {
+  const int G = p->G, L = p->L;
+  int rc = r2c_rows(p, rho, G, G, L, p->spec, st);
+  if (rc) return rc;
+  rc = fft_rows(p, p->spec, (int64_t)(p->M + 1), false, st);
+  if (rc) return rc;
+  const int64_t ns = (int64_t)(p->M + 1) * L;
+  kmul_kernel<<<blocks_for(ns, 256), 256, 0, st>>>(p->spec, p->khat, ns);
+  AUGUR_LAUNCH_CHECK(p);
+  rc = fft_rows(p, p->spec, (int64_t)(p->M + 1), true, st);
+  if (rc) return rc;
+  C2RArgs ca;
+  ca.L = L;
+  ca.nrows = L;
+  ca.RB = p->c2r_RB;
+  ca.ncomp = 1;
+  ca.Lt = p->Lt;
+  ca.nkeep = G;
+  ca.Lkeep = G;
+  const double h = p->extent / G;
+  ca.scale = (float)(h * h / ((double)L * L));
+  ca.fsh = p->sh_M;
+  ca.twmul = p->Lt / p->M;
+  c2r_rows_kernel<false><<<(unsigned)((G + p->c2r_RB - 1) / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec, ca, p->tw,
+                                                                                               p->phi2d);
+  AUGUR_LAUNCH_CHECK(p);
+  fd_grad2d_kernel<<<blocks_for((int64_t)G * G, 256), 256, 0, st>>>(p->phi2d, G, (float)(2.0 * h), F4);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+// sorted bodies -> F4 (the grid force of the plan's mode)
+int grid_force(augur_pm_plan *p, int ncomp, cudaStream_t st) {
+  if (p->mode == AUGUR_MODE_PERIODIC) {
+    DepositArgs a = dep_args(p);
+    deposit_kernel<3, 1><<<dep_blocks(p), 512, p->smem_dep, st>>>(p->pos4[p->cur], p->row_start, p->tile_off,
+                                                                   p->d_mmax, a, p->tw, nullptr, p->spec, p->d_err);
+    AUGUR_LAUNCH_CHECK(p);
+    return periodic_tail(p, ncomp, p->F4, st);
+  }
+  int rc = deposit_rho(p, p->rho2d, st);
+  if (rc) return rc;
+  return isolated_from_rho(p, p->rho2d, p->F4, st);
+}
+
+GatherArgs gather_args(const augur_pm_plan *p, float kick, float dt, int drift) {
+  GatherArgs a;
+  a.g = p->gp;
+  a.kick = kick;
+  a.dt = dt;
+  a.drift = drift;
+  return a;
+}
+
+int gather_force(augur_pm_plan *p, const float4 *F4, int64_t n, float *acc, float *phi, cudaStream_t st) {
+  if (n == 0) return AUGUR_OK;
+  GatherArgs a = gather_args(p, 0.f, 0.f, 0);
+  if (p->dim == 3)
+    gather_kernel<3, MODE_FORCE><<<blocks_for(n, 256), 256, 0, st>>>(
+        F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc, phi, nullptr, nullptr, nullptr, nullptr, p->d_err);
+  else
+    gather_kernel<2, MODE_FORCE><<<blocks_for(n, 256), 256, 0, st>>>(
+        F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc, phi, nullptr, nullptr, nullptr, nullptr, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int check_plan(const augur_pm_plan *p, int64_t n) {
+  if (!p) return AUGUR_EINVAL;
+  if (n < 0 || n > p->max_n) return AUGUR_EINVAL;
+  return AUGUR_OK;
+}
+
+}  // namespace
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+extern "C" {
+
+const char *augur_status_string(int status) {
+  switch (status) {
+    case AUGUR_OK: return "ok";
+    case AUGUR_EINVAL: return "invalid argument (shape, size, mode or pointer)";
+    case AUGUR_ENOMEM: return "device allocation failed";
+    case AUGUR_ETIMEDOUT: return "a device wait ran out of its budget";
+    case AUGUR_ERANGE: return "count or index outside the supported range";
+    case AUGUR_EIO: return "non-finite body state seen on the device";
+    case AUGUR_ECUDA: return "CUDA runtime error";
+    default: return "unknown status";
+  }
+}
+
+int augur_version(void) { return 0x000100; }
+
+int augur_pm_plan_destroy(augur_pm_plan *p) {
+  if (!p) return AUGUR_OK;
+  void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
+                  p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
+                  p->F4, p->real_tmp, p->phi2d, p->rho2d};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  delete p;
+  return AUGUR_OK;
+}
+
+int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bodies, int mode, double extent,
+                         double eps, double g_newton) {
+  if (!out) return AUGUR_EINVAL;
+  *out = nullptr;
+  if (!(dim == 3 && mode == AUGUR_MODE_PERIODIC) && !(dim == 2 && mode == AUGUR_MODE_ISOLATED_SOFTENED))
+    return AUGUR_EINVAL;
+  if (grid < 16 || grid > 1024 || (grid % 16) != 0) return AUGUR_EINVAL;
+  if (max_bodies < 1 || max_bodies > 0x7fffffffLL) return AUGUR_EINVAL;
+  if (!(extent > 0.0) || !std::isfinite(extent)) return AUGUR_EINVAL;
+  augur_pm_plan *p = new (std::nothrow) augur_pm_plan();
+  if (!p) return AUGUR_ENOMEM;
+  memset(p, 0, sizeof(*p));
+  p->dim = dim;
+  p->G = grid;
+  p->mode = mode;
+  p->extent = extent;
+  p->eps = eps;
+  p->gnewton = g_newton;
+  p->max_n = max_bodies;
+  const int G = grid;
+  const double h = extent / G;
+  GridParams &g = p->gp;
+  g.G = G;
+  g.D = dim;
+  g.periodic = mode == AUGUR_MODE_PERIODIC;
+  g.h = (float)h;
+  g.half_ext = (float)(extent / 2.0);
+  g.ext = (float)extent;
+  g.inv_hD = (float)(1.0 / (dim == 3 ? h * h * h : h * h));
+  p->nrow = (dim == 3) ? G * G : G + 2;
+  g.nrow = p->nrow;
+  p->ntiles = (p->nrow + SCAN_TILE - 1) / SCAN_TILE;
+  p->L = g.periodic ? G : 2 * G;
+  p->M = p->L / 2;
+  p->Lt = p->L;
+  if (!factor(p->M, p->sh_M) || !factor(p->L, p->sh_L)) {
+    delete p;
+    return AUGUR_EINVAL;
+  }
+  // tile shapes (the autotuner overrides these through augur_pm_plan_set_tiles)
+  p->dep_RY = 16;
+  if (dim == 3) {
+    int rr = 100000 / (12 * G);
+    int rz = rr / 16;
+    if (rz < 1) {
+      rz = 1;
+      p->dep_RY = 8;
+    }
+    while (rz > 1 && (G % rz) != 0) --rz;
+    if (rz > G) rz = G;
+    p->dep_RZ = rz;
+  } else {
+    p->dep_RZ = 1;
+  }
+  p->green_TY = (3 * G * 16 * 8 <= 200000) ? 16 : 8;
+  p->c2r_RB = (p->L <= 512) ? 16 : 8;
+  p->rows_RB = p->L >= 4096 ? 1 : 4096 / p->L;
+  p->r2c_RB = 16;
+  const int M = p->M, L = p->L, Lt = p->Lt;
+  p->smem_dep = (size_t)p->dep_RY * p->dep_RZ * G * 12 + (size_t)p->dep_RY * p->dep_RZ * 8 + (size_t)Lt * 8;
+  p->smem_green = (size_t)3 * G * p->green_TY * 8 + (size_t)Lt * 8;
+  p->smem_c2r = (size_t)2 * p->c2r_RB * (M + 1) * 8 + (size_t)(g.periodic ? 4 : 1) * p->c2r_RB * L * 4 + (size_t)Lt * 8;
+  p->smem_rows = (size_t)2 * p->rows_RB * (L + 1) * 8 + (size_t)Lt * 8;
+  p->smem_r2c = (size_t)2 * p->r2c_RB * (M + 1) * 8 + (size_t)Lt * 8;
+
+  int rc = AUGUR_OK;
+  const int64_t N = max_bodies;
+  const size_t ncell = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
+  const size_t nspec = (size_t)(M + 1) * (dim == 3 ? (size_t)G * G : (size_t)L);
+  rc |= dalloc(p, &p->tw, (size_t)Lt);
+  for (int b = 0; b < 2; ++b) {
+    rc |= dalloc(p, &p->pos4[b], (size_t)N);
+    rc |= dalloc(p, &p->vel4[b], (size_t)N);
+  }
+  rc |= dalloc(p, &p->key, (size_t)N);
+  rc |= dalloc(p, &p->slot, (size_t)N);
+  rc |= dalloc(p, &p->row_count, (size_t)p->nrow);
+  rc |= dalloc(p, &p->row_start, (size_t)(p->ntiles + 1) * SCAN_TILE);
+  rc |= dalloc(p, &p->tile_sum, (size_t)p->ntiles + 1);
+  rc |= dalloc(p, &p->tile_off, (size_t)p->ntiles + 1);
+  rc |= dalloc(p, &p->d_err, 1);
+  rc |= dalloc(p, &p->d_mmax, 1);
+  rc |= dalloc(p, &p->spec, nspec);
+  rc |= dalloc(p, &p->F4, ncell);
+  if (dim == 3) {
+    rc |= dalloc(p, &p->spec3, 4 * nspec);
+  } else {
+    rc |= dalloc(p, &p->khat, nspec);
+    rc |= dalloc(p, &p->real_tmp, (size_t)L * L);
+    rc |= dalloc(p, &p->phi2d, ncell);
+    rc |= dalloc(p, &p->rho2d, ncell);
+  }
+  if (rc != AUGUR_OK) {
+    augur_pm_plan_destroy(p);
+    return AUGUR_ENOMEM;
+  }
+  cudaMemset(p->row_count, 0, sizeof(uint32_t) * p->nrow);
+  cudaMemset(p->row_start, 0, sizeof(uint32_t) * (size_t)(p->ntiles + 1) * SCAN_TILE);
+  cudaMemset(p->d_err, 0, sizeof(unsigned));
+  cudaMemset(p->d_mmax, 0, sizeof(unsigned));
+  // twiddles exp(-2 pi i t / Lt) in double, rounded once to float
+  std::vector<float2> tw(Lt);
+  for (int t = 0; t < Lt; ++t) {
+    double ang = 2.0 * M_PI * (double)t / (double)Lt;
+    tw[t] = make_float2((float)std::cos(ang), (float)-std::sin(ang));
+  }
+  if (cudaMemcpy(p->tw, tw.data(), sizeof(float2) * Lt, cudaMemcpyHostToDevice) != cudaSuccess) {
+    augur_pm_plan_destroy(p);
+    return AUGUR_ECUDA;
+  }
+  // dynamic shared memory opt-in
+  cudaFuncSetAttribute(deposit_kernel<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
+  cudaFuncSetAttribute(deposit_kernel<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
+  cudaFuncSetAttribute(deposit_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
+  cudaFuncSetAttribute(fft_z_green_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
+  cudaFuncSetAttribute(c2r_rows_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
+  cudaFuncSetAttribute(c2r_rows_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
+  cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_rows);
+  cudaFuncSetAttribute(r2c_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_r2c);
+  if (cudaGetLastError() != cudaSuccess) {
+    augur_pm_plan_destroy(p);
+    return AUGUR_ECUDA;
+  }
+  if (mode == AUGUR_MODE_ISOLATED_SOFTENED) {
+    // kernel spectrum rfft2(K) of the 2G min-image lattice, once per plan
+    kernel_lattice_kernel<<<blocks_for((int64_t)L * L, 256), 256>>>(p->real_tmp, L, (float)h,
+                                                                    (float)(eps * eps));
+    rc = r2c_rows(p, p->real_tmp, L, L, L, p->khat, 0);
+    if (!rc) rc = fft_rows(p, p->khat, (int64_t)(M + 1), false, 0);
+    if (!rc) rc = cuda_status(cudaDeviceSynchronize());
+    if (rc) {
+      augur_pm_plan_destroy(p);
+      return rc;
+    }
+  }
+  *out = p;
+  return AUGUR_OK;
+}
+
+int64_t augur_pm_plan_workspace_bytes(const augur_pm_plan *p) { return p ? (int64_t)p->bytes : 0; }
+
+int64_t augur_pm_last_launches(const augur_pm_plan *p) { return p ? p->launches : 0; }
+
+int augur_pm_cell_index(augur_pm_plan *p, const float *pos, int64_t n, int32_t *i0, float *w, void *stream) {
+  if (!p || n < 0 || (n > 0 && (!pos || !i0 || !w))) return AUGUR_EINVAL;
+  p->launches = 0;
+  if (n == 0) return AUGUR_OK;
+  if (p->dim == 3)
+    cell_index_kernel<3><<<blocks_for(n, 256), 256, 0, S(stream)>>>(pos, n, p->gp, i0, w, p->d_err);
+  else
+    cell_index_kernel<2><<<blocks_for(n, 256), 256, 0, S(stream)>>>(pos, n, p->gp, i0, w, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int augur_pm_deposit(augur_pm_plan *p, const float *pos, const float *mass, const float *mask, int64_t n, float *rho,
+                     void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (!rho || (n > 0 && (!pos || !mass || !mask))) return AUGUR_EINVAL;
+  p->launches = 0;
+  p->run_active = 0;
+  cudaStream_t st = S(stream);
+  rc = sort_from_aos(p, const_cast<float *>(pos), nullptr, nullptr, mass, mask, n, false, 0.f, st);
+  if (rc) return rc;
+  return deposit_rho(p, rho, st);
+}
+
+int augur_pm_poisson(augur_pm_plan *p, const float *rho, float *force, void *stream) {
+  if (!p || !rho || !force) return AUGUR_EINVAL;
+  p->launches = 0;
+  cudaStream_t st = S(stream);
+  float4 *F4 = reinterpret_cast<float4 *>(force);
+  if (p->mode == AUGUR_MODE_PERIODIC) {
+    const int G = p->G;
+    int rc = r2c_rows(p, rho, G, G * G, G * G, p->spec, st);
+    if (rc) return rc;
+    return periodic_tail(p, 4, F4, st);
+  }
+  return isolated_from_rho(p, rho, F4, st);
+}
+
+int augur_pm_gather(augur_pm_plan *p, const float *force, const float *pos, const float *mask, int64_t n, float *acc,
+                    float *phi, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (!force || (n > 0 && (!pos || !mask || !acc))) return AUGUR_EINVAL;
+  p->launches = 0;
+  p->run_active = 0;
+  cudaStream_t st = S(stream);
+  // the gather reads the sorted body state; masses do not matter here (mask used as mass)
+  rc = sort_from_aos(p, const_cast<float *>(pos), nullptr, nullptr, mask, mask, n, false, 0.f, st);
+  if (rc) return rc;
+  return gather_force(p, reinterpret_cast<const float4 *>(force), n, acc, phi, st);
+}
+
+int augur_pm_force(augur_pm_plan *p, const float *pos, const float *mass, const float *mask, int64_t n, float *acc,
+                   float *phi, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (n > 0 && (!pos || !mass || !mask || !acc)) return AUGUR_EINVAL;
+  p->launches = 0;
+  p->run_active = 0;
+  cudaStream_t st = S(stream);
+  rc = sort_from_aos(p, const_cast<float *>(pos), nullptr, nullptr, mass, mask, n, false, 0.f, st);
+  if (rc) return rc;
+  rc = grid_force(p, phi ? 4 : 3, st);
+  if (rc) return rc;
+  return gather_force(p, p->F4, n, acc, phi, st);
+}
+
+int augur_pm_step(augur_pm_plan *p, float *pos, float *vel, float *acc, const float *mass, const float *mask,
+                  int64_t n, float dt, int have_acc, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (n > 0 && (!pos || !vel || !acc || !mass || !mask)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  int64_t launches = 0;
+  if (!have_acc) {
+    rc = augur_pm_force(p, pos, mass, mask, n, acc, nullptr, stream);
+    if (rc) return rc;
+    launches = p->launches;
+  }
+  p->launches = launches;
+  p->run_active = 0;
+  rc = sort_from_aos(p, pos, vel, acc, mass, mask, n, true, dt, st);
+  if (rc) return rc;
+  rc = grid_force(p, 3, st);
+  if (rc) return rc;
+  if (n == 0) return AUGUR_OK;
+  GatherArgs a = gather_args(p, (float)(0.5 * (double)dt), dt, 0);
+  if (p->dim == 3)
+    gather_kernel<3, MODE_VV><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc,
+                                                                  nullptr, vel, nullptr, nullptr, nullptr, p->d_err);
+  else
+    gather_kernel<2, MODE_VV><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc,
+                                                                  nullptr, vel, nullptr, nullptr, nullptr, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+static int run_gather(augur_pm_plan *p, float kick, int drift, float *acc_out, cudaStream_t st) {
+  const int64_t n = p->run_n;
+  if (n == 0) return AUGUR_OK;
+  GatherArgs a = gather_args(p, kick, p->run_dt, drift);
+  gather_kernel<3, MODE_KD><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a,
+                                                                acc_out, nullptr, nullptr, p->key, p->slot,
+                                                                p->row_count, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int augur_pm_run_begin(augur_pm_plan *p, const float *pos, const float *vel, const float *mass, const float *mask,
+                       int64_t n, float dt, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
+  if (n > 0 && (!pos || !vel || !mass || !mask)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  p->run_n = n;
+  p->run_dt = dt;
+  rc = sort_from_aos(p, const_cast<float *>(pos), vel, nullptr, mass, mask, n, false, 0.f, st);
+  if (rc) return rc;
+  rc = grid_force(p, 3, st);
+  if (rc) return rc;
+  rc = run_gather(p, (float)(0.5 * (double)dt), 1, nullptr, st);
+  if (rc) return rc;
+  p->run_active = 1;
+  return AUGUR_OK;
+}
+
+int augur_pm_run_steps(augur_pm_plan *p, int k, void *stream) {
+  if (!p || !p->run_active || k < 0) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  for (int s = 0; s < k; ++s) {
+    int rc = resort(p, st);
+    if (rc) return rc;
+    rc = grid_force(p, 3, st);
+    if (rc) return rc;
+    rc = run_gather(p, p->run_dt, 1, nullptr, st);
+    if (rc) return rc;
+  }
+  return AUGUR_OK;
+}
+
+int augur_pm_run_end(augur_pm_plan *p, float *pos, float *vel, float *acc_out, void *stream) {
+  if (!p || !p->run_active) return AUGUR_EINVAL;
+  if (p->run_n > 0 && (!pos || !vel)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  int rc = resort(p, st);
+  if (rc) return rc;
+  rc = grid_force(p, 3, st);
+  if (rc) return rc;
+  rc = run_gather(p, (float)(0.5 * (double)p->run_dt), 0, acc_out, st);
+  if (rc) return rc;
+  const int64_t n = p->run_n;
+  if (n > 0) {
+    unsort_kernel<3><<<blocks_for(n, 256), 256, 0, st>>>(p->pos4[p->cur], p->vel4[p->cur], n, pos, vel);
+    AUGUR_LAUNCH_CHECK(p);
+  }
+  p->run_active = 0;
+  return AUGUR_OK;
+}
+
+int augur_pm_run(augur_pm_plan *p, float *pos, float *vel, const float *mass, const float *mask, int64_t n, float dt,
+                 int nsteps, float *acc_out, void *stream) {
+  if (nsteps < 1) return AUGUR_EINVAL;
+  int rc = augur_pm_run_begin(p, pos, vel, mass, mask, n, dt, stream);
+  if (rc) return rc;
+  int64_t total = p->launches;
+  rc = augur_pm_run_steps(p, nsteps - 1, stream);
+  if (rc) return rc;
+  total += p->launches;
+  rc = augur_pm_run_end(p, pos, vel, acc_out, stream);
+  total += p->launches;
+  p->launches = total;
+  return rc;
+}
+
+int augur_pm_check(augur_pm_plan *p, void *stream) {
+  if (!p) return AUGUR_EINVAL;
+  if (cudaStreamSynchronize(S(stream)) != cudaSuccess) return AUGUR_ECUDA;
+  unsigned e = 0;
+  if (cudaMemcpy(&e, p->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return AUGUR_ECUDA;
+  if (cudaMemset(p->d_err, 0, sizeof(unsigned)) != cudaSuccess) return AUGUR_ECUDA;
+  if (e & AUGUR_ERRBIT_NONFINITE) return AUGUR_EIO;
+  if (e & AUGUR_ERRBIT_RANGE) return AUGUR_ERANGE;
+  return AUGUR_OK;
+}
+
+}  // extern "C"

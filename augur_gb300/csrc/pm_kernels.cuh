@@ -1,0 +1,904 @@
+// pm_kernels.cuh — device kernels of the PM gravity step (sm_103a).
+//
+// Data layout in HBM (x fastest everywhere):
+//   sorted body state  pos4[i] = (x, y, z, m*mask), vel4[i] = (vx, vy, vz, bits(id | maskbit))
+//   row histogram      one counter per grid row (3D periodic: row = z*G + y of the CIC base
+//                      cell; 2D isolated: row = y0+1, plus one discard bucket)
+//   half spectrum      spec[kx][row]  (kx = 0..L/2), complex64 — rows contiguous, so the
+//                      y transform reads contiguous lines and the z transform reads
+//                      128-byte column strips
+//   force grid         F4[cell] = (a_x, a_y, a_z, phi) float4, so the gather is one 128-bit
+//                      load per CIC corner
+#pragma once
+
+#include "augur_common.cuh"
+
+namespace augur {
+
+constexpr int SCAN_TILE = 4096;  // rows per local scan tile (1024 threads x 4)
+constexpr int MAXSEG = 64;
+
+struct GridParams {
+  int G;          // cells per side
+  int D;          // 2 or 3
+  int periodic;   // 1 periodic, 0 isolated (out-of-grid corners dropped)
+  int nrow;       // histogram buckets
+  float h;        // fp32(extent / G)
+  float half_ext; // fp32(extent / 2)
+  float ext;      // fp32(extent)
+  float inv_hD;   // fp32(1 / h^D) (density scale of ScatterField.scatter, in_scale = 1)
+};
+
+// fixed-point scale of the deposit, derived on the device from max(m*mask)
+struct QScale {
+  float qs1, qs2;   // contribution * qs1 * qs2 = contribution * 2^S (both exact)
+  float outscale;   // 2^-S / h^D
+};
+
+__device__ __forceinline__ QScale qscale_from_mmax(const unsigned *mmax_bits, float inv_hD) {
+  float mmax = __uint_as_float(*mmax_bits);
+  int e = 0;
+  if (mmax > 0.f) frexpf(mmax, &e);  // mmax = f * 2^e, f in [0.5, 1)
+  // every contribution c <= mmax < 2^e, so c * 2^(32-e) < 2^32
+  int S = 32 - e;
+  int S1 = S / 2, S2 = S - S1;
+  QScale q;
+  q.qs1 = ldexpf(1.f, S1);
+  q.qs2 = ldexpf(1.f, S2);
+  q.outscale = ldexpf(inv_hD, -S);
+  return q;
+}
+
+__device__ __forceinline__ uint32_t row_begin(const uint32_t *start, const uint32_t *tile_off, uint32_t r) {
+  return tile_off[r / SCAN_TILE] + start[r];
+}
+
+// Base-cell row key. 3D periodic: wrap(iz)*G + wrap(iy). 2D isolated: iy+1 in [0, G]
+// when some corner lands on the grid, else the discard bucket G+1.
+__device__ __forceinline__ uint32_t row_key(const GridParams &g, int ix, int iy, int iz) {
+  if (g.D == 3) {
+    return (uint32_t)(wrap_idx(iz, g.G) * g.G + wrap_idx(iy, g.G));
+  }
+  if (g.periodic) return (uint32_t)wrap_idx(iy, g.G);
+  bool on = (ix >= -1) && (ix < g.G) && (iy >= -1) && (iy < g.G);
+  return on ? (uint32_t)(iy + 1) : (uint32_t)(g.G + 1);
+}
+
+// Warp-aggregated slot within a row: one atomicAdd per distinct key per warp.
+// All 32 lanes must call this together.
+__device__ __forceinline__ uint32_t warp_slot(uint32_t *row_count, uint32_t key, bool valid) {
+  const int lane = threadIdx.x & 31;
+  unsigned peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu);
+  uint32_t base = 0;
+  if (valid) {
+    int leader = __ffs(peers) - 1;
+    if (lane == leader) base = atomicAdd(&row_count[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    base += __popc(peers & ((1u << lane) - 1u));
+  }
+  return base;
+}
+
+// ---------------------------------------------------------------------------------
+// K1: keys + histogram from caller (AoS) arrays. Optional velocity-Verlet drift
+// pos += dt*vel + (dt^2/2)*acc in the reference's fp32 order (scripts/scatter_field.py:685),
+// written back in place (periodic mode wraps into the box).
+// Also reduces max(m*mask) for the deposit's fixed-point scale.
+// ---------------------------------------------------------------------------------
+template <int D, bool DRIFT>
+__global__ void __launch_bounds__(256) keys_hist_aos_kernel(float *__restrict__ pos, const float *__restrict__ vel,
+                                                            const float *__restrict__ acc, const float *__restrict__ mass,
+                                                            const float *__restrict__ mask, int64_t n, GridParams g,
+                                                            float dt, float hdt2, uint32_t *__restrict__ key,
+                                                            uint32_t *__restrict__ slot, uint32_t *__restrict__ row_count,
+                                                            unsigned *__restrict__ mmax_bits, unsigned *__restrict__ err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  uint32_t k = 0;
+  float mm = 0.f;
+  if (valid) {
+    float x[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) x[d] = pos[i * D + d];
+    if (DRIFT) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        float t = __fadd_rn(x[d], __fmul_rn(dt, vel[i * D + d]));
+        t = __fadd_rn(t, __fmul_rn(hdt2, acc[i * D + d]));
+        if (g.periodic) {
+          if (t >= g.half_ext) t = __fsub_rn(t, g.ext);
+          else if (t < -g.half_ext) t = __fadd_rn(t, g.ext);
+        }
+        x[d] = t;
+        pos[i * D + d] = t;
+      }
+    }
+    int i0[3] = {0, 0, 0};
+    float w;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) ok &= cic_axis(x[d], g.half_ext, g.h, i0[d], w);
+    if (!ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
+    k = row_key(g, i0[0], i0[1], i0[2]);
+    mm = __fmul_rn(mass[i], mask[i]);
+  }
+  uint32_t s = warp_slot(row_count, k, valid);
+  if (valid) {
+    key[i] = k;
+    slot[i] = s;
+  }
+  // block max of m*mask (non-negative floats order like their bit patterns)
+  unsigned b = valid ? __float_as_uint(fmaxf(mm, 0.f)) : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(mmax_bits, b);
+}
+
+// ---------------------------------------------------------------------------------
+// Scan of the row histogram: local exclusive scan per 4096-row tile (and the
+// counters are cleared for the next histogram), then one block scans the tile totals.
+// row_begin(r) = tile_off[r / 4096] + start[r] for any r <= nrow.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) scan_local_kernel(uint32_t *__restrict__ count, uint32_t *__restrict__ start,
+                                                          uint32_t *__restrict__ tile_sum, int nrow) {
+  __shared__ uint32_t wsum[32];
+  const int tile = blockIdx.x;
+  const int base = tile * SCAN_TILE + threadIdx.x * 4;
+  uint32_t v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int r = base + q;
+    v[q] = (r < nrow) ? count[r] : 0u;
+    if (r < nrow) count[r] = 0u;
+  }
+  uint32_t local = v[0] + v[1] + v[2] + v[3];
+  // warp inclusive scan
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = wsum[lane];
+    uint32_t si = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += t;
+    }
+    wsum[lane] = si - s;  // exclusive
+    if (lane == 31) tile_sum[tile] = si;
+  }
+  __syncthreads();
+  uint32_t run = wsum[warp] + inc - local;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    start[base + q] = run;  // start is sized (ntiles + 1) * 4096, zero beyond nrow
+    run += v[q];
+  }
+}
+
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t *__restrict__ tile_sum,
+                                                          uint32_t *__restrict__ tile_off, int ntiles) {
+  __shared__ uint32_t wsum[32];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b0 = 0; b0 < ntiles; b0 += 1024) {
+    int t = b0 + threadIdx.x;
+    uint32_t v = t < ntiles ? tile_sum[t] : 0u;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t s = wsum[lane], si = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, si, o);
+        if (lane >= o) si += u;
+      }
+      wsum[lane] = si - s;
+    }
+    __syncthreads();
+    uint32_t c = carry;
+    if (t < ntiles) tile_off[t] = c + wsum[warp] + inc - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = c + wsum[warp] + inc;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tile_off[ntiles] = carry;
+}
+
+// ---------------------------------------------------------------------------------
+// Scatter bodies to their sorted slot. From caller AoS arrays (FROM_AOS) or from the
+// previous sorted state (run loop).
+// ---------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) scatter_aos_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
+                                                          const float *__restrict__ mass, const float *__restrict__ mask,
+                                                          int64_t n, const uint32_t *__restrict__ key,
+                                                          const uint32_t *__restrict__ slot,
+                                                          const uint32_t *__restrict__ start,
+                                                          const uint32_t *__restrict__ tile_off, float4 *__restrict__ pos4,
+                                                          float4 *__restrict__ vel4) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t dst = row_begin(start, tile_off, key[i]) + slot[i];
+  float mk = mask[i];
+  float4 p = make_float4(pos[i * D], pos[i * D + 1], D == 3 ? pos[i * D + 2] : 0.f, __fmul_rn(mass[i], mk));
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (vel) {
+    v.x = vel[i * D];
+    v.y = vel[i * D + 1];
+    if (D == 3) v.z = vel[i * D + 2];
+  }
+  uint32_t id = (uint32_t)i | (mk == 0.f ? 0x80000000u : 0u);
+  v.w = __uint_as_float(id);
+  pos4[dst] = p;
+  vel4[dst] = v;
+}
+
+__global__ void __launch_bounds__(256) scatter_sorted_kernel(const float4 *__restrict__ pos_in,
+                                                             const float4 *__restrict__ vel_in, int64_t n,
+                                                             const uint32_t *__restrict__ key,
+                                                             const uint32_t *__restrict__ slot,
+                                                             const uint32_t *__restrict__ start,
+                                                             const uint32_t *__restrict__ tile_off,
+                                                             float4 *__restrict__ pos_out, float4 *__restrict__ vel_out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t dst = row_begin(start, tile_off, key[i]) + slot[i];
+  pos_out[dst] = pos_in[i];
+  vel_out[dst] = vel_in[i];
+}
+
+// ---------------------------------------------------------------------------------
+// K2 (+K3a): deterministic CIC deposit of one block of grid rows, accumulated in
+// 64-bit fixed point in shared memory with warp-aggregated atomics (integer sums are
+// associative, so the result is independent of body order and scheduling), then
+// either written as float32 density rows (MODE 0) or transformed along x in shared
+// memory (R2C, MODE 1) and written to the half spectrum spec[kx][row].
+//
+// Block = RY consecutive y rows x RZ consecutive z planes (2D: RZ = 1). Bodies that
+// touch the block are those whose base row lies in [y0-1, y0+RY-1] x [z0-1, z0+RZ-1];
+// with the state sorted by base row they form at most 2*(RZ+1) contiguous segments.
+// ---------------------------------------------------------------------------------
+struct DepositArgs {
+  GridParams g;
+  int RY, RZ;
+  FftShape fsh;   // complex length M = G/2 (MODE 1)
+  int twmul;      // table stride for the length-M transform
+  int Lt;         // twiddle table length
+};
+
+template <int D, int MODE>
+__global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__ pos4,
+                                                      const uint32_t *__restrict__ start,
+                                                      const uint32_t *__restrict__ tile_off,
+                                                      const unsigned *__restrict__ mmax_bits, DepositArgs a,
+                                                      const float2 *__restrict__ twg, float *__restrict__ rho_out,
+                                                      float2 *__restrict__ spec_out, unsigned *__restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ long long s_beg[MAXSEG];
+  __shared__ long long s_pre[MAXSEG + 1];
+  __shared__ int s_nseg;
+
+  const GridParams &g = a.g;
+  const int G = g.G, RY = a.RY, RZ = a.RZ, RR = RY * RZ;
+  const int nyb = G / RY;
+  const int y0 = (blockIdx.x % nyb) * RY;
+  const int z0 = (D == 3) ? (blockIdx.x / nyb) * RZ : 0;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int RS = G + 2;  // fp32 row stride (keeps complex rows 8-byte aligned and padded)
+
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem);
+  float *rows = reinterpret_cast<float *>(smem + (size_t)RR * G * 8);
+  float2 *tw = reinterpret_cast<float2 *>(smem + (size_t)RR * G * 8 + (size_t)RR * RS * 4);
+
+  for (int e = tid; e < RR * G; e += nt) acc[e] = 0ull;
+  if (MODE == 1)
+    for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
+
+  if (tid == 0) {
+    int ns = 0;
+    auto add = [&](uint32_t r0, uint32_t r1) {  // rows [r0, r1)
+      uint32_t b = row_begin(start, tile_off, r0), e = row_begin(start, tile_off, r1);
+      if (e > b && ns < MAXSEG) {
+        s_beg[ns] = b;
+        s_pre[ns + 1] = (long long)(e - b);
+        ++ns;
+      }
+    };
+    if (D == 3) {
+      const int nz = (RZ < G) ? RZ + 1 : G;
+      const int zs = (RZ < G) ? z0 - 1 : 0;
+      for (int t = 0; t < nz; ++t) {
+        int iz = wrap_idx(zs + t, G);
+        uint32_t rb = (uint32_t)iz * G;
+        if (RY < G) {
+          int yh = wrap_idx(y0 - 1, G);
+          add(rb + yh, rb + yh + 1);
+          add(rb + y0, rb + y0 + RY);
+        } else {
+          add(rb, rb + G);
+        }
+      }
+    } else if (g.periodic) {
+      if (RY < G) {
+        int yh = wrap_idx(y0 - 1, G);
+        add(yh, yh + 1);
+        add(y0, y0 + RY);
+      } else {
+        add(0, G);
+      }
+    } else {
+      // isolated 2D: base rows y0-1 .. y0+RY-1  <->  keys y0 .. y0+RY
+      add(y0, y0 + RY + 1);
+    }
+    s_pre[0] = 0;
+    for (int s = 0; s < ns; ++s) s_pre[s + 1] += s_pre[s];
+    s_nseg = ns;
+  }
+  __syncthreads();
+
+  const QScale qs = qscale_from_mmax(mmax_bits, g.inv_hD);
+  const int nseg = s_nseg;
+  const long long total = s_pre[nseg];
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+
+  for (long long f0 = (long long)warp * 32; f0 < total; f0 += (long long)nwarp * 32) {
+    const long long f = f0 + lane;
+    const bool valid = f < total;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+      int lo = 0, hi = nseg - 1;  // find s with s_pre[s] <= f < s_pre[s+1]
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_pre[mid] <= f) lo = mid;
+        else hi = mid - 1;
+      }
+      p = pos4[s_beg[lo] + (f - s_pre[lo])];
+    }
+    int ix = 0, iy = 0, iz = 0;
+    float wx = 0.f, wy = 0.f, wz = 0.f;
+    bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx) & cic_axis(p.y, g.half_ext, g.h, iy, wy);
+    if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz);
+    if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
+    const bool live = valid && ok && p.w > 0.f;
+#pragma unroll
+    for (int ox = 0; ox < 2; ++ox) {
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy) {
+#pragma unroll
+        for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
+          unsigned target = 0xffffffffu;
+          uint32_t q = 0;
+          if (live) {
+            int cx = ix + ox, cy = iy + oy, cz = iz + oz;
+            bool in;
+            if (g.periodic) {
+              cx = wrap_idx(cx, G);
+              cy = wrap_idx(cy, G);
+              int ly = cy - y0;
+              if (ly < 0) ly += G;
+              int lz = 0;
+              if (D == 3) {
+                cz = wrap_idx(cz, G);
+                lz = cz - z0;
+                if (lz < 0) lz += G;
+              }
+              in = (ly < RY) && (lz < RZ);
+              if (in) target = (unsigned)((lz * RY + ly) * G + cx);
+            } else {
+              int ly = cy - y0;
+              in = (cx >= 0) && (cx < G) && (ly >= 0) && (ly < RY);
+              if (in) target = (unsigned)(ly * G + cx);
+            }
+            if (in) {
+              float wt = __fmul_rn(axis_w(wx, ox), axis_w(wy, oy));
+              if (D == 3) wt = __fmul_rn(wt, axis_w(wz, oz));
+              float c = __fmul_rn(wt, p.w);
+              q = __float2uint_rz(__fmul_rn(__fmul_rn(c, qs.qs1), qs.qs2));
+            }
+          }
+          // warp aggregation only when neighbouring lanes share a target
+          unsigned prev = __shfl_up_sync(0xffffffffu, target, 1);
+          bool dup = (lane > 0) && (target != 0xffffffffu) && (prev == target);
+          if (__any_sync(0xffffffffu, dup)) {
+            unsigned peers = __match_any_sync(0xffffffffu, target);
+            if (target != 0xffffffffu) {
+              uint32_t slo = __reduce_add_sync(peers, q & 0xffffu);
+              uint32_t shi = __reduce_add_sync(peers, q >> 16);
+              if (lane == __ffs(peers) - 1)
+                atomicAdd(&acc[target], ((unsigned long long)shi << 16) + (unsigned long long)slo);
+            }
+          } else if (target != 0xffffffffu && q) {
+            atomicAdd(&acc[target], (unsigned long long)q);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // fixed point -> float32 density rows
+  for (int e = tid; e < RR * G; e += nt) {
+    int rr = e / G, x = e - rr * G;
+    float v = __fmul_rn(__ull2float_rn(acc[e]), qs.outscale);
+    if (MODE == 0) {
+      int zz = rr / RY, yy = rr - zz * RY;
+      size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
+      rho_out[row * G + x] = v;
+    } else {
+      rows[rr * RS + x] = v;
+    }
+  }
+  if (MODE == 0) return;
+  __syncthreads();
+
+  // R2C along x: rows viewed as M = G/2 complex values, stride RS/2 = M+1
+  const int M = G / 2, MS = M + 1;
+  float2 *A = reinterpret_cast<float2 *>(rows);
+  float2 *B = reinterpret_cast<float2 *>(smem);  // acc area is free now
+  float2 *Z = fft_smem(a.fsh, A, B, RR, 1, MS, tw, a.twmul, false);
+  // post-process X_k = (Z_k + conj Z_{M-k})/2 - i/2 W^k (Z_k - conj Z_{M-k}), k = 0..M
+  const int tstep = a.Lt / G;
+  const size_t plane = (size_t)(D == 3 ? G : 1) * G;  // rows per kx plane
+  for (int e = tid; e < (M + 1) * RR; e += nt) {
+    int kx = e / RR, rr = e - kx * RR;
+    float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
+    float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
+    float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+    float2 od = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y - zc.y));
+    float2 w = tw[kx * tstep];
+    float2 t = cmul(w, od);
+    float2 X = make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
+    int zz = rr / RY, yy = rr - zz * RY;
+    size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
+    spec_out[(size_t)kx * plane + row] = X;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Generic R2C of real rows (zero padded from Lin to L, rows >= nin are zero):
+// out[kx * nout + r], kx = 0..L/2. Used for the Poisson solve from a given density
+// grid and for the 2D isolated (2G zero-padded) transform.
+// ---------------------------------------------------------------------------------
+struct RowsArgs {
+  int L, Lin, nin, nout, RB, Lt;
+  FftShape fsh;  // complex length L/2
+  int twmul;     // for the length L/2 transform
+};
+
+__global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__ in, RowsArgs a,
+                                                       const float2 *__restrict__ twg, float2 *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB;
+  float2 *A = reinterpret_cast<float2 *>(smem);
+  float2 *B = A + (size_t)RB * MS;
+  float2 *tw = B + (size_t)RB * MS;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int r0 = blockIdx.x * RB;
+  for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
+  float *Af = reinterpret_cast<float *>(A);
+  for (int e = tid; e < RB * L; e += nt) {
+    int rr = e / L, x = e - rr * L;
+    int r = r0 + rr;
+    float v = 0.f;
+    if (r < a.nin && x < a.Lin) v = in[(size_t)r * a.Lin + x];
+    Af[rr * 2 * MS + x] = v;
+  }
+  __syncthreads();
+  float2 *Z = fft_smem(a.fsh, A, B, RB, 1, MS, tw, a.twmul, false);
+  const int tstep = a.Lt / L;
+  for (int e = tid; e < (M + 1) * RB; e += nt) {
+    int kx = e / RB, rr = e - kx * RB;
+    int r = r0 + rr;
+    if (r >= a.nout) continue;
+    float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
+    float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
+    float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+    float2 od = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y - zc.y));
+    float2 t = cmul(tw[kx * tstep], od);
+    out[(size_t)kx * a.nout + r] = make_float2(ev.x + t.y, ev.y - t.x);
+  }
+}
+
+// In-place FFT of contiguous complex rows of length L (rows = lines along y).
+__global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data, int64_t nrows, int RB, int L,
+                                                       FftShape fsh, int twmul, int Lt,
+                                                       const float2 *__restrict__ twg, int inverse) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int LS = L + 1;
+  float2 *A = reinterpret_cast<float2 *>(smem);
+  float2 *B = A + (size_t)RB * LS;
+  float2 *tw = B + (size_t)RB * LS;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * RB;
+  const int nr = (int)min((int64_t)RB, nrows - r0);
+  for (int e = tid; e < Lt; e += nt) tw[e] = twg[e];
+  for (int e = tid; e < nr * L; e += nt) {
+    int rr = e / L, x = e - rr * L;
+    A[rr * LS + x] = data[(r0 + rr) * L + x];
+  }
+  __syncthreads();
+  float2 *R = fft_smem(fsh, A, B, nr, 1, LS, tw, twmul, inverse != 0);
+  for (int e = tid; e < nr * L; e += nt) {
+    int rr = e / L, x = e - rr * L;
+    data[(r0 + rr) * L + x] = R[rr * LS + x];
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// K3b: z transform + Green's function + spectral gradient + inverse z transform, for
+// one kx plane and a strip of TY ky columns, all z. spec is [kx][z][ky] (after the
+// forward y transform). Writes ncomp outputs out[c][kx][z][ky]: the three components of
+// a_k = -i k phi_k (Nyquist of the differentiated axis -> 0) and, if ncomp == 4, phi_k.
+// phi_k = -4 pi G rho_k / k^2 (k = 0 -> 0) with the 1/G^3 of the inverse transform folded in.
+// ---------------------------------------------------------------------------------
+struct GreenArgs {
+  int G, TY, ncomp, Lt;
+  FftShape fsh;    // length G
+  float kfund;     // 2 pi / box
+  float gfac;      // -4 pi G_newton / G^3
+};
+
+__global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
+                                                          const float2 *__restrict__ twg,
+                                                          float2 *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int G = a.G, TY = a.TY, M = G / 2;
+  const int nyt = G / TY;
+  const int kx = blockIdx.x / nyt;
+  const int y0 = (blockIdx.x % nyt) * TY;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const size_t plane = (size_t)G * G;
+  const size_t cstride = (size_t)(M + 1) * plane;
+  float2 *P = reinterpret_cast<float2 *>(smem);
+  float2 *B = P + (size_t)G * TY;
+  float2 *C = B + (size_t)G * TY;
+  float2 *tw = C + (size_t)G * TY;
+  for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
+  const float2 *src = spec + (size_t)kx * plane;
+  for (int e = tid; e < G * TY; e += nt) {
+    int z = e / TY, t = e - z * TY;
+    B[e] = src[(size_t)z * G + y0 + t];
+  }
+  __syncthreads();
+  float2 *R = fft_smem(a.fsh, B, C, TY, TY, 1, tw, 1, false);
+  // Green's function
+  const float mx = (float)kx;
+  for (int e = tid; e < G * TY; e += nt) {
+    int z = e / TY, t = e - z * TY;
+    int ky = y0 + t;
+    float my = (float)(ky < M ? ky : ky - G);
+    float mz = (float)(z < M ? z : z - G);
+    float m2 = mx * mx + my * my + mz * mz;
+    float2 v = R[e];
+    float f = (m2 > 0.f) ? a.gfac / (a.kfund * a.kfund * m2) : 0.f;
+    P[e] = make_float2(v.x * f, v.y * f);
+  }
+  __syncthreads();
+  for (int c = 0; c < a.ncomp; ++c) {
+    for (int e = tid; e < G * TY; e += nt) {
+      int z = e / TY, t = e - z * TY;
+      float2 ph = P[e];
+      float2 o;
+      if (c == 3) {
+        o = ph;
+      } else {
+        int idx = (c == 0) ? kx : (c == 1 ? y0 + t : z);
+        float m;
+        if (c == 0) m = (idx == M) ? 0.f : (float)idx;
+        else m = (idx == M) ? 0.f : (float)(idx < M ? idx : idx - G);
+        float k = a.kfund * m;
+        o = make_float2(k * ph.y, -k * ph.x);  // -i k phi
+      }
+      B[e] = o;
+    }
+    __syncthreads();
+    float2 *Q = fft_smem(a.fsh, B, C, TY, TY, 1, tw, 1, true);
+    float2 *dst = out + c * cstride + (size_t)kx * plane;
+    for (int e = tid; e < G * TY; e += nt) {
+      int z = e / TY, t = e - z * TY;
+      dst[(size_t)z * G + y0 + t] = Q[e];
+    }
+    __syncthreads();
+  }
+}
+
+// 2D isolated: pointwise product with the kernel spectrum (complex), spec[kx][ky].
+__global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict__ khat, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) spec[i] = cmul(spec[i], khat[i]);
+}
+
+// ---------------------------------------------------------------------------------
+// K3c: C2R along x. in[c][kx][r] (kx = 0..L/2, r < nrows). Each block transforms RB rows
+// of every component. OUT4: writes F4[r][x] = (c0, c1, c2, c3 or 0) for x < L.
+// Otherwise writes component 0 as real rows out[r][x] for r < nkeep, x < Lkeep (times scale).
+// ---------------------------------------------------------------------------------
+struct C2RArgs {
+  int L, nrows, RB, ncomp, Lt;
+  int nkeep, Lkeep;
+  float scale;
+  FftShape fsh;  // complex length L/2
+  int twmul;
+};
+
+template <bool OUT4>
+__global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
+                                                       const float2 *__restrict__ twg, float *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int r0 = blockIdx.x * RB;
+  float2 *X = reinterpret_cast<float2 *>(smem);
+  float2 *Y = X + (size_t)RB * MS;
+  float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [ncomp][RB][L]
+  float2 *tw = reinterpret_cast<float2 *>(res + (size_t)(OUT4 ? 4 : 1) * RB * L);
+  for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
+  const size_t cstride = (size_t)(M + 1) * a.nrows;
+  const int tstep = a.Lt / L;
+  const int nc = OUT4 ? a.ncomp : 1;
+  for (int c = 0; c < nc; ++c) {
+    const float2 *src = in + c * cstride;
+    for (int e = tid; e < (M + 1) * RB; e += nt) {
+      int kx = e / RB, rr = e - kx * RB;
+      int r = r0 + rr;
+      float2 v = (r < a.nrows) ? src[(size_t)kx * a.nrows + r] : make_float2(0.f, 0.f);
+      if (kx == 0 || kx == M) v.y = 0.f;  // imaginary part of DC and Nyquist is ignored
+      X[rr * MS + kx] = v;
+    }
+    __syncthreads();
+    // pre-process: E_k = X_k + conj X_{M-k} ; O_k = (X_k - conj X_{M-k}) W^{-k} ; Z_k = E_k + i O_k
+    for (int e = tid; e < M * RB; e += nt) {
+      int rr = e / M, k = e - rr * M;
+      float2 xk = X[rr * MS + k];
+      float2 xc = cconj(X[rr * MS + (M - k)]);
+      float2 E = cadd(xk, xc);
+      float2 w = tw[k * tstep];
+      float2 O = cmul(csub(xk, xc), cconj(w));
+      Y[rr * MS + k] = make_float2(E.x - O.y, E.y + O.x);
+    }
+    __syncthreads();
+    float2 *R = fft_smem(a.fsh, Y, X, RB, 1, MS, tw, a.twmul, true);
+    float *dst = res + (size_t)c * RB * L;
+    for (int e = tid; e < RB * M; e += nt) {
+      int rr = e / M, k = e - rr * M;
+      float2 v = R[rr * MS + k];
+      dst[rr * L + 2 * k] = v.x * a.scale;
+      dst[rr * L + 2 * k + 1] = v.y * a.scale;
+    }
+    __syncthreads();
+  }
+  if (OUT4) {
+    float4 *o4 = reinterpret_cast<float4 *>(out);
+    for (int e = tid; e < RB * L; e += nt) {
+      int rr = e / L, x = e - rr * L;
+      int r = r0 + rr;
+      if (r >= a.nrows) continue;
+      float4 v;
+      v.x = res[(size_t)0 * RB * L + rr * L + x];
+      v.y = res[(size_t)1 * RB * L + rr * L + x];
+      v.z = (a.ncomp > 2) ? res[(size_t)2 * RB * L + rr * L + x] : 0.f;
+      v.w = (a.ncomp > 3) ? res[(size_t)3 * RB * L + rr * L + x] : 0.f;
+      o4[(size_t)r * L + x] = v;
+    }
+  } else {
+    for (int e = tid; e < RB * L; e += nt) {
+      int rr = e / L, x = e - rr * L;
+      int r = r0 + rr;
+      if (r >= a.nkeep || x >= a.Lkeep) continue;
+      out[(size_t)r * a.Lkeep + x] = res[rr * L + x];
+    }
+  }
+}
+
+// 2D isolated: F4 grid from the potential by the reference's zero-padded central
+// difference (scripts/scatter_field.py:551-555): a_x = -((phi[y][x+1] - phi[y][x-1]) / (2h)).
+__global__ void fd_grad2d_kernel(const float *__restrict__ phi, int G, float two_h, float4 *__restrict__ F4) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= G * G) return;
+  int y = e / G, x = e - y * G;
+  float xp = (x + 1 < G) ? phi[e + 1] : 0.f, xm = (x > 0) ? phi[e - 1] : 0.f;
+  float yp = (y + 1 < G) ? phi[e + G] : 0.f, ym = (y > 0) ? phi[e - G] : 0.f;
+  float gx = __fdiv_rn(__fsub_rn(xp, xm), two_h);
+  float gy = __fdiv_rn(__fsub_rn(yp, ym), two_h);
+  F4[e] = make_float4(-gx, -gy, 0.f, phi[e]);
+}
+
+// 2D isolated: kernel lattice K = -1/sqrt(d_y^2 + d_x^2 + eps^2) on the 2G min-image
+// lattice (scripts/pm_baseline_force_error.py:70-73), fp32.
+__global__ void kernel_lattice_kernel(float *__restrict__ K, int G2, float h, float eps2) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= G2 * G2) return;
+  int y = e / G2, x = e - y * G2;
+  float dy = __fmul_rn((float)min(y, G2 - y), h), dx = __fmul_rn((float)min(x, G2 - x), h);
+  float s = __fadd_rn(__fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dx, dx)), eps2);
+  K[e] = __fdiv_rn(-1.0f, __fsqrt_rn(s));
+}
+
+// ---------------------------------------------------------------------------------
+// K4: CIC gather of F4 at the sorted bodies, fused with the integrator.
+//   MODE_FORCE : acc[id] = a * mask, phi[id]
+//   MODE_KD    : v += kick * a ; if drift: x += dt * v, wrap, new row key + slot (run loop)
+//   MODE_VV    : velocity-Verlet kick on caller arrays: vel[id] += (dt/2)*(acc[id] + a);
+//                acc[id] = a (scripts/scatter_field.py:686-688)
+// Corner order and fp32 operation order follow ScatterField.gather (:252-261).
+// ---------------------------------------------------------------------------------
+enum { MODE_FORCE = 0, MODE_KD = 1, MODE_VV = 2 };
+
+struct GatherArgs {
+  GridParams g;
+  float kick, dt;
+  int drift;
+};
+
+template <int D, int MODE>
+__global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
+                                                     float4 *__restrict__ vel4, int64_t n, GatherArgs a,
+                                                     float *__restrict__ acc_out, float *__restrict__ phi_out,
+                                                     float *__restrict__ vel_out, uint32_t *__restrict__ key,
+                                                     uint32_t *__restrict__ slot, uint32_t *__restrict__ row_count,
+                                                     unsigned *__restrict__ err) {
+  const GridParams &g = a.g;
+  const int G = g.G;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f), v = p;
+  if (valid) {
+    p = pos4[i];
+    v = vel4[i];
+  }
+  int ix = 0, iy = 0, iz = 0;
+  float wx = 0.f, wy = 0.f, wz = 0.f;
+  bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx) & cic_axis(p.y, g.half_ext, g.h, iy, wy);
+  if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz);
+  if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
+  float ax = 0.f, ay = 0.f, az = 0.f, ph = 0.f;
+  if (valid && ok) {
+#pragma unroll
+    for (int ox = 0; ox < 2; ++ox) {
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy) {
+#pragma unroll
+        for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
+          int cx = ix + ox, cy = iy + oy, cz = iz + oz;
+          float wt = __fmul_rn(axis_w(wx, ox), axis_w(wy, oy));
+          if (D == 3) wt = __fmul_rn(wt, axis_w(wz, oz));
+          bool in = true;
+          if (g.periodic) {
+            cx = wrap_idx(cx, G);
+            cy = wrap_idx(cy, G);
+            if (D == 3) cz = wrap_idx(cz, G);
+          } else {
+            in = (cx >= 0) && (cx < G) && (cy >= 0) && (cy < G);
+            cx = min(max(cx, 0), G - 1);
+            cy = min(max(cy, 0), G - 1);
+            if (!in) wt = 0.f;
+          }
+          size_t cell = (D == 3) ? ((size_t)cz * G + cy) * G + cx : (size_t)cy * G + cx;
+          float4 f = __ldg(&F4[cell]);
+          ax = __fadd_rn(ax, __fmul_rn(f.x, wt));
+          ay = __fadd_rn(ay, __fmul_rn(f.y, wt));
+          if (D == 3) az = __fadd_rn(az, __fmul_rn(f.z, wt));
+          ph = __fadd_rn(ph, __fmul_rn(f.w, wt));
+        }
+      }
+    }
+  }
+  const uint32_t idw = __float_as_uint(v.w);
+  const uint32_t id = idw & 0x7fffffffu;
+  const float mk = (idw & 0x80000000u) ? 0.f : 1.f;
+  if (MODE == MODE_FORCE) {
+    if (valid) {
+      acc_out[(size_t)id * D] = __fmul_rn(ax, mk);
+      acc_out[(size_t)id * D + 1] = __fmul_rn(ay, mk);
+      if (D == 3) acc_out[(size_t)id * D + 2] = __fmul_rn(az, mk);
+      if (phi_out) phi_out[id] = __fmul_rn(ph, mk);
+    }
+  } else if (MODE == MODE_VV) {
+    if (valid) {
+      float an[3] = {__fmul_rn(ax, mk), __fmul_rn(ay, mk), __fmul_rn(az, mk)};
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        float ao = acc_out[(size_t)id * D + d];
+        float dv = __fmul_rn(a.kick, __fadd_rn(ao, an[d]));
+        vel_out[(size_t)id * D + d] = __fadd_rn(vel_out[(size_t)id * D + d], dv);
+        acc_out[(size_t)id * D + d] = an[d];
+      }
+      if (phi_out) phi_out[id] = __fmul_rn(ph, mk);
+    }
+  } else {  // MODE_KD on the sorted state
+    uint32_t k = 0;
+    if (valid) {
+      ax = __fmul_rn(ax, mk);
+      ay = __fmul_rn(ay, mk);
+      az = __fmul_rn(az, mk);
+      v.x = __fadd_rn(v.x, __fmul_rn(a.kick, ax));
+      v.y = __fadd_rn(v.y, __fmul_rn(a.kick, ay));
+      if (D == 3) v.z = __fadd_rn(v.z, __fmul_rn(a.kick, az));
+      if (a.drift) {
+        float xs[3] = {p.x, p.y, p.z};
+        const float vs[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          float t = __fadd_rn(xs[d], __fmul_rn(a.dt, vs[d]));
+          if (t >= g.half_ext) t = __fsub_rn(t, g.ext);
+          else if (t < -g.half_ext) t = __fadd_rn(t, g.ext);
+          xs[d] = t;
+        }
+        p.x = xs[0];
+        p.y = xs[1];
+        p.z = xs[2];
+        int jx = 0, jy = 0, jz = 0;
+        float u;
+        bool ok2 = cic_axis(p.x, g.half_ext, g.h, jx, u) & cic_axis(p.y, g.half_ext, g.h, jy, u);
+        if (D == 3) ok2 &= cic_axis(p.z, g.half_ext, g.h, jz, u);
+        if (!ok2) set_err(err, AUGUR_ERRBIT_NONFINITE);
+        k = row_key(g, jx, jy, jz);
+      }
+      pos4[i] = p;
+      vel4[i] = v;
+      if (acc_out) {
+        acc_out[(size_t)id * D] = ax;
+        acc_out[(size_t)id * D + 1] = ay;
+        if (D == 3) acc_out[(size_t)id * D + 2] = az;
+      }
+    }
+    if (a.drift) {
+      uint32_t s = warp_slot(row_count, k, valid);
+      if (valid) {
+        key[i] = k;
+        slot[i] = s;
+      }
+    }
+  }
+}
+
+// Write the sorted state back to the caller's order (end of a run).
+template <int D>
+__global__ void unsort_kernel(const float4 *__restrict__ pos4, const float4 *__restrict__ vel4, int64_t n,
+                              float *__restrict__ pos, float *__restrict__ vel) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pos4[i], v = vel4[i];
+  uint32_t id = __float_as_uint(v.w) & 0x7fffffffu;
+  pos[(size_t)id * D] = p.x;
+  pos[(size_t)id * D + 1] = p.y;
+  vel[(size_t)id * D] = v.x;
+  vel[(size_t)id * D + 1] = v.y;
+  if (D == 3) {
+    pos[(size_t)id * D + 2] = p.z;
+    vel[(size_t)id * D + 2] = v.z;
+  }
+}
+
+// Cell index output (bit-exact with ScatterField._corners).
+template <int D>
+__global__ void cell_index_kernel(const float *__restrict__ pos, int64_t n, GridParams g, int32_t *__restrict__ i0,
+                                  float *__restrict__ w, unsigned *__restrict__ err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    int c;
+    float f;
+    if (!cic_axis(pos[i * D + d], g.half_ext, g.h, c, f)) set_err(err, AUGUR_ERRBIT_NONFINITE);
+    i0[i * D + d] = c;
+    w[i * D + d] = f;
+  }
+}
+
+}  // namespace augur

@@ -1,0 +1,240 @@
+"""Host-side API of the GB300 PM gravity step.
+
+`PMPlan` wraps one C-ABI plan (include/augur_pm.h): a grid geometry plus its device
+workspace. Every method takes CUDA float32 tensors in the reference's layouts
+((N, D) positions/velocities, (N,) masses and masks), enqueues the native kernels on
+the current torch stream and returns without synchronising. There is no CPU path:
+CPU tensors, wrong dtypes or a missing library raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import AUGUR_MODE_ISOLATED_SOFTENED, AUGUR_MODE_PERIODIC
+
+MODES = {"periodic": AUGUR_MODE_PERIODIC, "isolated": AUGUR_MODE_ISOLATED_SOFTENED,
+         "isolated_softened": AUGUR_MODE_ISOLATED_SOFTENED}
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _need(t: torch.Tensor, name: str, dtype=torch.float32, shape=None, device=None) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (the PM path has no CPU implementation)")
+    if t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+    if device is not None and t.device != device:
+        raise ValueError(f"{name} is on {t.device}, the plan is on {device}")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} must have shape {tuple(shape)}, got {tuple(t.shape)}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    return t
+
+
+class PMPlan:
+    """One grid geometry + workspace for up to ``max_bodies`` bodies.
+
+    dim=3, mode="periodic": unit-cell periodic box of side ``extent`` (phi_k = -4 pi G rho_k/k^2).
+    dim=2, mode="isolated": the reference's plain PM (scripts/pm_baseline_force_error.py:68-76).
+    """
+
+    def __init__(self, dim: int, grid: int, max_bodies: int, mode: str = "periodic", extent: float = 1.0,
+                 eps: float = 0.5, g_newton: float = 1.0, device=None):
+        self.lib = _lib.load()
+        self.dim, self.grid, self.max_bodies = int(dim), int(grid), int(max_bodies)
+        self.mode, self.extent, self.eps, self.g_newton = mode, float(extent), float(eps), float(g_newton)
+        self.h = self.extent / self.grid
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("PMPlan needs a CUDA device")
+        self._p = C.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.lib.augur_pm_plan_create(C.byref(self._p), self.dim, self.grid, self.max_bodies,
+                                               MODES[mode], self.extent, self.eps, self.g_newton)
+        _lib.check(rc, "augur_pm_plan_create")
+
+    # ---- lifetime --------------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_p", None) and self._p.value:
+            with torch.cuda.device(self.device):
+                torch.cuda.synchronize(self.device)
+                self.lib.augur_pm_plan_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self.lib.augur_pm_plan_workspace_bytes(self._p))
+
+    @property
+    def last_launches(self) -> int:
+        """Kernel launches issued by the last plan call."""
+        return int(self.lib.augur_pm_last_launches(self._p))
+
+    @property
+    def grid_shape(self) -> tuple[int, ...]:
+        return (self.grid,) * self.dim
+
+    def _n(self, pos: torch.Tensor) -> int:
+        _need(pos, "pos", device=self.device)
+        if pos.dim() != 2 or pos.shape[1] != self.dim:
+            raise ValueError(f"pos must be (N, {self.dim}), got {tuple(pos.shape)}")
+        n = pos.shape[0]
+        if n > self.max_bodies:
+            raise ValueError(f"{n} bodies exceed the plan's max_bodies={self.max_bodies}")
+        return n
+
+    def _mm(self, n, mass, mask):
+        if mass is None:
+            mass = torch.ones(n, device=self.device)
+        if mask is None:
+            mask = torch.ones(n, device=self.device)
+        return _need(mass, "mass", shape=(n,), device=self.device), _need(mask, "mask", shape=(n,), device=self.device)
+
+    def _call(self, name: str, *args) -> None:
+        with torch.cuda.device(self.device):
+            rc = getattr(self.lib, name)(self._p, *args, _stream(self.device))
+        _lib.check(rc, name)
+
+    # ---- sub-ops (ScatterField building blocks) ------------------------------------------
+    def cell_index(self, pos: torch.Tensor):
+        """Bit-exact CIC base cell and fraction (ScatterField._corners, scripts/scatter_field.py:179-182)."""
+        n = self._n(pos)
+        i0 = torch.empty((n, self.dim), dtype=torch.int32, device=self.device)
+        w = torch.empty((n, self.dim), dtype=torch.float32, device=self.device)
+        self._call("augur_pm_cell_index", pos.data_ptr(), n, i0.data_ptr(), w.data_ptr())
+        return i0, w
+
+    def deposit(self, pos, mass=None, mask=None) -> torch.Tensor:
+        """CIC mass density (mass channel of ScatterField.scatter, scripts/scatter_field.py:237-250)."""
+        n = self._n(pos)
+        mass, mask = self._mm(n, mass, mask)
+        rho = torch.empty(self.grid_shape, dtype=torch.float32, device=self.device)
+        self._call("augur_pm_deposit", pos.data_ptr(), mass.data_ptr(), mask.data_ptr(), n, rho.data_ptr())
+        return rho
+
+    def poisson(self, rho: torch.Tensor) -> torch.Tensor:
+        """Force grid (..., 4) = (a_x, a_y, a_z, phi) from a density grid."""
+        _need(rho, "rho", shape=self.grid_shape, device=self.device)
+        out = torch.empty(self.grid_shape + (4,), dtype=torch.float32, device=self.device)
+        self._call("augur_pm_poisson", rho.data_ptr(), out.data_ptr())
+        return out
+
+    def gather(self, force4: torch.Tensor, pos: torch.Tensor, mask=None):
+        """CIC gather of a (..., 4) force grid (ScatterField.gather, scripts/scatter_field.py:252-261)."""
+        n = self._n(pos)
+        _need(force4, "force", shape=self.grid_shape + (4,), device=self.device)
+        _, mask = self._mm(n, None, mask)
+        acc = torch.empty((n, self.dim), dtype=torch.float32, device=self.device)
+        phi = torch.empty((n,), dtype=torch.float32, device=self.device)
+        self._call("augur_pm_gather", force4.data_ptr(), pos.data_ptr(), mask.data_ptr(), n, acc.data_ptr(),
+                   phi.data_ptr())
+        return acc, phi
+
+    # ---- force / integrators --------------------------------------------------------------
+    def force(self, pos, mass=None, mask=None, with_phi: bool = False):
+        """Plain PM acceleration at the bodies (pm_acc, scripts/pm_baseline_force_error.py:68-76)."""
+        n = self._n(pos)
+        mass, mask = self._mm(n, mass, mask)
+        acc = torch.empty((n, self.dim), dtype=torch.float32, device=self.device)
+        phi = torch.empty((n,), dtype=torch.float32, device=self.device) if with_phi else None
+        self._call("augur_pm_force", pos.data_ptr(), mass.data_ptr(), mask.data_ptr(), n, acc.data_ptr(), _ptr(phi))
+        return (acc, phi) if with_phi else acc
+
+    def step(self, pos, vel, acc, mass=None, mask=None, dt: float = 1e-3, have_acc: bool = True) -> None:
+        """One velocity-Verlet step in place (ScatterField._step, scripts/scatter_field.py:677-688)."""
+        n = self._n(pos)
+        _need(vel, "vel", shape=pos.shape, device=self.device)
+        _need(acc, "acc", shape=pos.shape, device=self.device)
+        mass, mask = self._mm(n, mass, mask)
+        self._call("augur_pm_step", pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), mass.data_ptr(),
+                   mask.data_ptr(), n, float(dt), int(bool(have_acc)))
+
+    def run(self, pos, vel, mass=None, mask=None, dt: float = 1e-3, nsteps: int = 1, want_acc: bool = False):
+        """nsteps merged kick-drift-kick steps in place on the sorted device state."""
+        n = self._n(pos)
+        _need(vel, "vel", shape=pos.shape, device=self.device)
+        mass, mask = self._mm(n, mass, mask)
+        acc = torch.empty_like(pos) if want_acc else None
+        self._call("augur_pm_run", pos.data_ptr(), vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), n, float(dt),
+                   int(nsteps), _ptr(acc))
+        return acc
+
+    def run_begin(self, pos, vel, mass=None, mask=None, dt: float = 1e-3) -> None:
+        n = self._n(pos)
+        _need(vel, "vel", shape=pos.shape, device=self.device)
+        mass, mask = self._mm(n, mass, mask)
+        self._keep = (mass, mask)
+        self._call("augur_pm_run_begin", pos.data_ptr(), vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), n,
+                   float(dt))
+
+    def run_steps(self, k: int) -> None:
+        self._call("augur_pm_run_steps", int(k))
+
+    def run_end(self, pos, vel, want_acc: bool = False):
+        acc = torch.empty_like(pos) if want_acc else None
+        self._call("augur_pm_run_end", pos.data_ptr(), vel.data_ptr(), _ptr(acc))
+        return acc
+
+    def check(self) -> None:
+        """Synchronise and raise if a kernel flagged non-finite state."""
+        self._call("augur_pm_check")
+
+
+def direct_sum_fp64(targets: torch.Tensor, sources: torch.Tensor, mass: torch.Tensor | None = None,
+                    eps: float = 0.5, box: float = 0.0, target_index: torch.Tensor | None = None) -> torch.Tensor:
+    """FP64 softened direct sum on the GPU (exact_acc, scripts/scatter_scaling_ops.py:57-72).
+
+    box > 0 makes the sum periodic (minimum image + tabulated Ewald correction)."""
+    lib = _lib.load()
+    dev = targets.device
+    _need(targets, "targets", torch.float64)
+    _need(sources, "sources", torch.float64, device=dev)
+    d = targets.shape[1]
+    if mass is not None:
+        _need(mass, "mass", torch.float64, shape=(sources.shape[0],), device=dev)
+    if target_index is not None:
+        _need(target_index, "target_index", torch.int64, shape=(targets.shape[0],), device=dev)
+    out = torch.empty_like(targets)
+    with torch.cuda.device(dev):
+        rc = lib.augur_direct_sum_fp64(targets.data_ptr(), _ptr(target_index), targets.shape[0], sources.data_ptr(),
+                                       _ptr(mass), sources.shape[0], d, float(eps), float(box), out.data_ptr(),
+                                       _stream(dev))
+    _lib.check(rc, "augur_direct_sum_fp64")
+    return out
+
+
+def energy_fp64(vel: torch.Tensor, mass: torch.Tensor, mask: torch.Tensor, phi: torch.Tensor | None = None) -> dict:
+    """Compensated reductions: kinetic energy, momentum, mass and PM potential energy."""
+    lib = _lib.load()
+    dev = vel.device
+    _need(vel, "vel")
+    n, d = vel.shape
+    _need(mass, "mass", shape=(n,), device=dev)
+    _need(mask, "mask", shape=(n,), device=dev)
+    if phi is not None:
+        _need(phi, "phi", shape=(n,), device=dev)
+    out = torch.zeros(d + 3, dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        rc = lib.augur_energy_fp64(vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), _ptr(phi), n, d, out.data_ptr(),
+                                   _stream(dev))
+    _lib.check(rc, "augur_energy_fp64")
+    o = out.tolist()
+    return {"ke": o[0], "momentum": o[1:1 + d], "mass": o[d + 1], "pe": o[d + 2]}

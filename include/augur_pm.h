@@ -1,0 +1,187 @@
+/*
+ * augur_pm.h — C ABI of the GB300 (sm_103a) particle-mesh gravity step.
+ *
+ * Every entry point takes plain device pointers, element counts and a CUDA stream
+ * (passed as void*; NULL means the legacy default stream). Nothing here uses torch
+ * types. Functions return 0 on success or a negative status (AUGUR_E*); the text of
+ * a status comes from augur_status_string(). No entry point synchronises the device
+ * unless its comment says so, and none traps on the device: device-side problems
+ * (non-finite positions, grids too large for a launch) set a per-plan error word
+ * that augur_pm_check() reads.
+ *
+ * Layouts follow the reference's ScatterField tensors (scripts/scatter_field.py):
+ *   pos, vel  : (N, D) float32, contiguous (D = 2 or 3)
+ *   mass, mask: (N,)   float32; mask in {0,1}; masked bodies deposit nothing and get
+ *               zero force (scripts/scatter_field.py:238-241, :615)
+ *   grids     : row-major [z][y][x] (3D) or [y][x] (2D) float32, x fastest
+ * The grid covers [-extent/2, extent/2)^D (scripts/scatter_field.py:82-83, :179-182).
+ *
+ * Modes:
+ *   AUGUR_MODE_PERIODIC          D=3 periodic box: phi_k = -4 pi G rho_k / k^2 (k=0 -> 0),
+ *                                spectral gradient a_k = -i k phi_k (Nyquist -> 0).
+ *   AUGUR_MODE_ISOLATED_SOFTENED D=2 isolated box, the reference's plain PM
+ *                                (scripts/pm_baseline_force_error.py:68-76): 2G x 2G
+ *                                zero-padded convolution with K = -1/sqrt(d^2+eps^2),
+ *                                central-difference gradient (scripts/scatter_field.py:551-555).
+ */
+#ifndef AUGUR_PM_H
+#define AUGUR_PM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AUGUR_OK          0
+#define AUGUR_EINVAL    (-22)  /* bad shape, size, mode or pointer            */
+#define AUGUR_ENOMEM    (-12)  /* device allocation failed                    */
+#define AUGUR_ETIMEDOUT (-110) /* a device wait ran out of its budget         */
+#define AUGUR_ERANGE    (-34)  /* a count or grid index outside what is supported */
+#define AUGUR_EIO       (-5)   /* non-finite body state seen on the device    */
+#define AUGUR_ECUDA     (-1000)/* CUDA runtime error (launch or copy)         */
+
+#define AUGUR_MODE_PERIODIC          0
+#define AUGUR_MODE_ISOLATED_SOFTENED 1
+
+typedef struct augur_pm_plan augur_pm_plan;
+
+/* Human-readable text of a status code (static storage). */
+const char *augur_status_string(int status);
+
+/* Library version, 0xMMmmpp. */
+int augur_version(void);
+
+/*
+ * Plan: the grid geometry and all device workspace for up to max_bodies bodies.
+ * Replaces the geometry held by ScatterField.__init__ (scripts/scatter_field.py:76-140)
+ * and the workspace PyTorch allocated per call. extent is the box side; eps is the
+ * softening of the isolated kernel (ignored by the periodic mode); g_newton scales
+ * the periodic Green's function. The plan allocates its workspace with cudaMalloc on
+ * the current device and owns it until augur_pm_plan_destroy().
+ */
+int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bodies,
+                         int mode, double extent, double eps, double g_newton);
+int augur_pm_plan_destroy(augur_pm_plan *plan);
+/* Bytes of device memory the plan holds. */
+int64_t augur_pm_plan_workspace_bytes(const augur_pm_plan *plan);
+
+/*
+ * CIC base cell and fraction, bit-exact with ScatterField._corners
+ * (scripts/scatter_field.py:179-182): u = (x + extent/2) / h - 0.5 in IEEE float32
+ * (round-to-nearest, true division by float32(h)), i0 = floor(u), w = u - i0.
+ * i0_out: (N, D) int32 (not wrapped), w_out: (N, D) float32.
+ */
+int augur_pm_cell_index(augur_pm_plan *plan, const float *pos, int64_t n,
+                        int32_t *i0_out, float *w_out, void *stream);
+
+/*
+ * CIC mass deposit rho = sum m*mask*w / h^D, the mass channel of ScatterField.scatter
+ * (scripts/scatter_field.py:237-250). Deterministic: contributions are accumulated in
+ * 64-bit fixed point in shared memory after a counting sort by grid row, so the
+ * result does not depend on body order or on scheduling. Periodic mode wraps corner
+ * indices mod G; isolated mode drops out-of-grid corners (:208). rho_out: G^D floats.
+ */
+int augur_pm_deposit(augur_pm_plan *plan, const float *pos, const float *mass,
+                     const float *mask, int64_t n, float *rho_out, void *stream);
+
+/*
+ * Grid force from a density grid: the FFT Poisson solve and gradient of
+ * pm_acc (scripts/pm_baseline_force_error.py:69-75) for the isolated mode, the
+ * periodic Green's function + spectral gradient for the periodic mode.
+ * force_out: G^D cells x 4 floats (a_x, a_y, a_z, phi); in 2D the a_z lane is 0.
+ */
+int augur_pm_poisson(augur_pm_plan *plan, const float *rho, float *force_out, void *stream);
+
+/*
+ * CIC gather of a 4-lane force grid at body positions, ScatterField.gather
+ * (scripts/scatter_field.py:252-261): acc_out (N, D) = sum_corners w * F[corner].
+ * phi_out (N,) may be NULL.
+ */
+int augur_pm_gather(augur_pm_plan *plan, const float *force, const float *pos,
+                    const float *mask, int64_t n, float *acc_out, float *phi_out,
+                    void *stream);
+
+/*
+ * Plain PM force at the bodies: pm_acc (scripts/pm_baseline_force_error.py:68-76)
+ * for the isolated mode, the periodic PM force otherwise. acc_out (N, D) is
+ * multiplied by mask. phi_out (N,) (potential at the bodies) may be NULL.
+ */
+int augur_pm_force(augur_pm_plan *plan, const float *pos, const float *mass,
+                   const float *mask, int64_t n, float *acc_out, float *phi_out,
+                   void *stream);
+
+/*
+ * One velocity-Verlet step, ScatterField._step with verlet=True
+ * (scripts/scatter_field.py:677-688):
+ *   pos += dt*vel + dt^2/2 * acc ; a_new = F(pos) ; vel += dt/2 * (acc + a_new) ; acc = a_new
+ * pos, vel, acc are updated in place. If have_acc is 0, acc is first set to F(pos)
+ * (the reference's a_prev is None branch). Periodic mode wraps positions into the box.
+ */
+int augur_pm_step(augur_pm_plan *plan, float *pos, float *vel, float *acc,
+                  const float *mass, const float *mask, int64_t n, float dt,
+                  int have_acc, void *stream);
+
+/*
+ * nsteps leapfrog steps (kick-drift-kick, merged between steps as in Sim.tick,
+ * scripts/scatter_bh_1b.py:123-146) with the body state kept sorted by grid row on the
+ * device between steps; one force evaluation per step plus one at the start. The
+ * positions and velocities are written back to pos/vel in the caller's order.
+ * acc_out (N, D) receives the force at the final positions and may be NULL.
+ * Periodic mode only.
+ */
+int augur_pm_run(augur_pm_plan *plan, float *pos, float *vel, const float *mass,
+                 const float *mask, int64_t n, float dt, int nsteps, float *acc_out,
+                 void *stream);
+
+/*
+ * Split form of augur_pm_run, for callers that time or graph-capture single steps:
+ * run_begin loads and sorts the bodies and applies the opening half kick; run_steps
+ * advances k merged kick-drift steps (no host synchronisation, capture-safe);
+ * run_end applies the closing half kick and writes pos/vel (and acc_out if not NULL)
+ * back in the caller's order.
+ */
+int augur_pm_run_begin(augur_pm_plan *plan, const float *pos, const float *vel,
+                       const float *mass, const float *mask, int64_t n, float dt,
+                       void *stream);
+int augur_pm_run_steps(augur_pm_plan *plan, int k, void *stream);
+int augur_pm_run_end(augur_pm_plan *plan, float *pos, float *vel, float *acc_out,
+                     void *stream);
+
+/* Kernel launches issued by the last plan call (for launch accounting). */
+int64_t augur_pm_last_launches(const augur_pm_plan *plan);
+
+/*
+ * Synchronise the stream, read and clear the plan's device error word. Returns
+ * AUGUR_OK, AUGUR_EIO (non-finite body state) or AUGUR_ERANGE.
+ */
+int augur_pm_check(augur_pm_plan *plan, void *stream);
+
+/*
+ * FP64 softened direct sum, exact_acc (scripts/scatter_scaling_ops.py:57-72)
+ * generalised to D=2,3: acc[t] = sum_j m_j (x_j - x_t) / (|x_j - x_t|^2 + eps^2)^1.5
+ * with the self pair excluded (target index t_idx[t] is a source index, or -1 if the
+ * target is not a source). targets (T, D) f64, sources (N, D) f64, mass (N,) f64 or
+ * NULL for unit masses. acc_out (T, D) f64.
+ * If box > 0 the sum is periodic (Ewald; box side = box, minimum image plus a tabulated
+ * Ewald correction), else isolated.
+ */
+int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t t,
+                          const double *sources, const double *mass, int64_t n,
+                          int dim, double eps, double box, double *acc_out, void *stream);
+
+/*
+ * Compensated FP64 reductions over bodies (scripts/scatter_field.py:759-769):
+ * out[0] = kinetic energy sum m v^2 / 2, out[1..D] = momentum sum m v,
+ * out[D+1] = mass sum, out[D+2] = PM potential energy sum m phi / 2 (phi may be NULL -> 0).
+ * out must hold D+3 doubles (device memory).
+ */
+int augur_energy_fp64(const float *vel, const float *mass, const float *mask,
+                      const float *phi, int64_t n, int dim, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AUGUR_PM_H */

@@ -1,0 +1,415 @@
+"""CPU oracle for the PM gravity path — TEST INFRASTRUCTURE ONLY.
+
+This module restates, in numpy, the arithmetic of the reference's particle-mesh path
+(Faraday-dot-py/Augur, scripts/scatter_field.py and scripts/pm_baseline_force_error.py)
+and its 3D periodic generalisation. Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg may import it; the product (augur_gb300) never does.
+
+Parity pins: the 2D functions are checked against outputs of the reference itself
+(tests/golden/, generated by tests/golden/make_golden.py from the reference's own
+code: ScatterField._corners, ScatterField.scatter/gather, pm_acc, exact_acc, and the
+published plain-PM medians of results/pm_baseline_force_error.json).
+
+Conventions (all from the reference):
+  * grid covers [-E/2, E/2)^D, h = E/G, cell-centred CIC:
+    u = (x + E/2)/h - 0.5 ; i0 = floor(u) ; w = u - i0          (scatter_field.py:179-182)
+  * corner weights w or 1-w per axis, multiplied x then y (then z)  (scatter_field.py:203-209)
+  * density channel m*mask*w/h^D                                  (scatter_field.py:238-241)
+  * isolated PM: 2G zero-padded FFT convolution with -1/sqrt(d^2+eps^2), times h^2,
+    crop, zero-padded central difference                          (pm_baseline_force_error.py:68-76,
+                                                                   scatter_field.py:551-555)
+  * periodic 3D (no reference implementation; the build's own spec):
+    phi_k = -4 pi G rho_k / |k|^2, k = 2 pi m / E, k=0 -> 0; a_k = -i k phi_k with the
+    Nyquist term of the differentiated axis set to 0; numpy rfftn/irfftn normalisation.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+F32 = np.float32
+
+
+# ----------------------------------------------------------------------------------
+# cell index (scripts/scatter_field.py:179-182), bit-exact fp32
+# ----------------------------------------------------------------------------------
+def cell_index(pos, G: int, E: float):
+    """u = (x + E/2)/h - 0.5 in IEEE fp32 with true division, i0 = floor(u), w = u - i0."""
+    p = np.asarray(pos, dtype=F32)
+    t = (p + F32(E / 2)).astype(F32)
+    u = ((t / F32(E / G)).astype(F32) - F32(0.5)).astype(F32)
+    f = np.floor(u).astype(F32)
+    return f.astype(np.int64), (u - f).astype(F32)
+
+
+def _axis_w(w, o):
+    return w if o else (F32(1.0) - w).astype(F32)
+
+
+def corners(D: int):
+    """Corner order of ScatterField._corner_iter (ox outer, then oy, then oz)."""
+    if D == 2:
+        return [(ox, oy, 0) for ox in (0, 1) for oy in (0, 1)]
+    return [(ox, oy, oz) for ox in (0, 1) for oy in (0, 1) for oz in (0, 1)]
+
+
+def corner_weight(w, o, D):
+    wt = (_axis_w(w[:, 0], o[0]) * _axis_w(w[:, 1], o[1])).astype(F32)
+    if D == 3:
+        wt = (wt * _axis_w(w[:, 2], o[2])).astype(F32)
+    return wt
+
+
+# ----------------------------------------------------------------------------------
+# deposit
+# ----------------------------------------------------------------------------------
+def qscale(mm):
+    """Fixed-point scale of the deterministic deposit: contributions c <= max(m) < 2^e
+    are quantised as trunc(c * 2^(32-e)) into uint32 and summed exactly in uint64."""
+    mmax = float(np.max(mm)) if mm.size else 0.0
+    e = math.frexp(mmax)[1] if mmax > 0 else 0
+    S = 32 - e
+    S1 = int(S / 2)
+    return F32(math.ldexp(1.0, S1)), F32(math.ldexp(1.0, S - S1)), S
+
+
+def deposit_fixed(pos, mass, mask, G: int, E: float, periodic: bool):
+    """The GPU deposit's arithmetic, bit for bit: fp32 weights, uint32 quanta, exact
+    uint64 sums, one fp32 rounding of the sum and one of the scale."""
+    pos = np.asarray(pos, F32)
+    D = pos.shape[1]
+    mm = (np.asarray(mass, F32) * np.asarray(mask, F32)).astype(F32)
+    q1, q2, S = qscale(np.maximum(mm, 0))
+    h = E / G
+    inv_hD = F32(1.0 / (h * h * h if D == 3 else h * h))
+    outscale = F32(np.ldexp(inv_hD, -S))
+    i0, w = cell_index(pos, G, E)
+    acc = np.zeros(G ** D, dtype=np.uint64)
+    live = mm > 0
+    for o in corners(D):
+        wt = corner_weight(w, o, D)
+        c = (wt * mm).astype(F32)
+        q = ((c * q1).astype(F32) * q2).astype(F32)
+        q = np.trunc(q).astype(np.uint64)
+        idx = [i0[:, d] + o[d] for d in range(D)]
+        if periodic:
+            idx = [np.mod(ix, G) for ix in idx]
+            ok = live
+        else:
+            ok = live.copy()
+            for ix in idx:
+                ok &= (ix >= 0) & (ix < G)
+            idx = [np.clip(ix, 0, G - 1) for ix in idx]
+        flat = idx[0] + G * idx[1] + (G * G * idx[2] if D == 3 else 0)
+        np.add.at(acc, flat[ok], q[ok])
+    rho = (acc.astype(F32) * outscale).astype(F32)
+    return rho.reshape((G,) * D)
+
+
+def deposit_ref(pos, mass, mask, G: int, E: float, periodic: bool, dtype=np.float64):
+    """ScatterField.scatter mass channel in the reference's idiom (index_add over corners):
+    fp32 cell index, weights and values as the reference, accumulation in `dtype`."""
+    pos = np.asarray(pos, F32)
+    D = pos.shape[1]
+    h = E / G
+    i0, w = cell_index(pos, G, E)  # fp32, bit-exact with the reference
+    val = ((np.asarray(mass, F32) * np.asarray(mask, F32)).astype(F32) * F32(1.0 / h ** D)).astype(F32)
+    out = np.zeros(G ** D, dtype=dtype)
+    for o in corners(D):
+        wt = corner_weight(w, o, D).astype(dtype)
+        idx = [i0[:, d] + o[d] for d in range(D)]
+        if periodic:
+            idx = [np.mod(ix, G) for ix in idx]
+            ok = np.ones(len(pos), bool)
+        else:
+            ok = np.ones(len(pos), bool)
+            for ix in idx:
+                ok &= (ix >= 0) & (ix < G)
+            idx = [np.clip(ix, 0, G - 1) for ix in idx]
+        flat = idx[0] + G * idx[1] + (G * G * idx[2] if D == 3 else 0)
+        np.add.at(out, flat[ok], (val * wt)[ok])
+    return out.reshape((G,) * D)
+
+
+# ----------------------------------------------------------------------------------
+# Poisson solves
+# ----------------------------------------------------------------------------------
+def poisson_periodic(rho, E: float, g_newton: float = 1.0):
+    """3D periodic: returns F (G,G,G,4) float64 = (a_x, a_y, a_z, phi), grid [z][y][x]."""
+    rho = np.asarray(rho, np.float64)
+    G = rho.shape[0]
+    rk = np.fft.rfftn(rho)  # axes (z, y, x), x halved
+    m_full = np.fft.fftfreq(G, 1.0 / G)  # 0..G/2-1, -G/2..-1
+    mz = m_full[:, None, None]
+    my = m_full[None, :, None]
+    mx = np.arange(G // 2 + 1, dtype=np.float64)[None, None, :]
+    kf = 2 * np.pi / E
+    k2 = kf * kf * (mx ** 2 + my ** 2 + mz ** 2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        green = np.where(k2 > 0, -4 * np.pi * g_newton / k2, 0.0)
+    phik = rk * green
+    out = np.empty((G, G, G, 4), np.float64)
+    for c, m in enumerate((mx, my, mz)):
+        mm = np.where(np.abs(m) == G // 2, 0.0, m)  # Nyquist of the differentiated axis -> 0
+        out[..., c] = np.fft.irfftn(-1j * kf * mm * phik, s=(G, G, G), axes=(0, 1, 2))
+    out[..., 3] = np.fft.irfftn(phik, s=(G, G, G), axes=(0, 1, 2))
+    return out
+
+
+def kernel_lattice_2d(G: int, h: float, eps: float):
+    """-1/sqrt(d^2 + eps^2) on the 2G min-image lattice (pm_baseline_force_error.py:70-73), fp32."""
+    idx = np.arange(2 * G, dtype=F32)
+    d = (np.minimum(idx, F32(2 * G) - idx) * F32(h)).astype(F32)
+    s = ((d[:, None] ** 2).astype(F32) + (d[None, :] ** 2).astype(F32)).astype(F32) + F32(eps * eps)
+    return (F32(-1.0) / np.sqrt(s.astype(F32))).astype(F32)
+
+
+def isolated_phi_2d(rho, E: float, eps: float, dtype=np.float64):
+    """h^2 * irfft2(rfft2(rho, 2G) * rfft2(K))[:G, :G] (pm_baseline_force_error.py:74)."""
+    G = rho.shape[0]
+    h = E / G
+    K = kernel_lattice_2d(G, h, eps).astype(dtype)
+    full = np.fft.irfft2(np.fft.rfft2(np.asarray(rho, dtype), s=(2 * G, 2 * G)) * np.fft.rfft2(K), s=(2 * G, 2 * G))
+    return (full * h ** 2)[:G, :G]
+
+
+def neg_grad_2d(phi, h: float):
+    """Zero-padded central difference (scatter_field.py:551-555) -> (G, G, 4) (a_x, a_y, 0, phi)."""
+    p = np.pad(np.asarray(phi), 1)
+    gx = (p[1:-1, 2:] - p[1:-1, :-2]) / (2 * h)
+    gy = (p[2:, 1:-1] - p[:-2, 1:-1]) / (2 * h)
+    out = np.zeros(phi.shape + (4,), dtype=phi.dtype)
+    out[..., 0], out[..., 1], out[..., 3] = -gx, -gy, phi
+    return out
+
+
+# ----------------------------------------------------------------------------------
+# gather (scripts/scatter_field.py:252-261)
+# ----------------------------------------------------------------------------------
+def gather_f32(F4, pos, G: int, E: float, periodic: bool):
+    """fp32 gather in the GPU's (and the reference's) corner and operation order.
+    F4: (G,)*D + (4,) float32. Returns (acc (N, D), phi (N,))."""
+    pos = np.asarray(pos, F32)
+    D = pos.shape[1]
+    F = np.asarray(F4, F32).reshape(-1, 4)
+    i0, w = cell_index(pos, G, E)
+    a = np.zeros((len(pos), D), F32)
+    ph = np.zeros(len(pos), F32)
+    for o in corners(D):
+        wt = corner_weight(w, o, D)
+        idx = [i0[:, d] + o[d] for d in range(D)]
+        if periodic:
+            idx = [np.mod(ix, G) for ix in idx]
+        else:
+            ok = np.ones(len(pos), bool)
+            for ix in idx:
+                ok &= (ix >= 0) & (ix < G)
+            wt = np.where(ok, wt, F32(0)).astype(F32)
+            idx = [np.clip(ix, 0, G - 1) for ix in idx]
+        flat = idx[0] + G * idx[1] + (G * G * idx[2] if D == 3 else 0)
+        f = F[flat]
+        for d in range(D):
+            a[:, d] = (a[:, d] + (f[:, d] * wt).astype(F32)).astype(F32)
+        ph = (ph + (f[:, 3] * wt).astype(F32)).astype(F32)
+    return a, ph
+
+
+def gather_ref(F, pos, G: int, E: float, periodic: bool, dtype=np.float64):
+    """Gather with the reference's fp32 weights, accumulated in `dtype` (float64 for tolerance checks)."""
+    pos = np.asarray(pos, F32)
+    D = pos.shape[1]
+    i0, w = cell_index(pos, G, E)  # fp32 cell index and weights as the reference
+    Ff = np.asarray(F, dtype).reshape(-1, F.shape[-1])
+    out = np.zeros((len(pos), F.shape[-1]), dtype)
+    for o in corners(D):
+        wt = corner_weight(w, o, D).astype(dtype)
+        idx = [i0[:, d] + o[d] for d in range(D)]
+        if periodic:
+            idx = [np.mod(ix, G) for ix in idx]
+        else:
+            ok = np.ones(len(pos), bool)
+            for ix in idx:
+                ok &= (ix >= 0) & (ix < G)
+            wt = np.where(ok, wt, 0.0)
+            idx = [np.clip(ix, 0, G - 1) for ix in idx]
+        flat = idx[0] + G * idx[1] + (G * G * idx[2] if D == 3 else 0)
+        out += Ff[flat] * wt[:, None]
+    return out
+
+
+# ----------------------------------------------------------------------------------
+# full force evaluations
+# ----------------------------------------------------------------------------------
+def pm_force_periodic(pos, mass, mask, G: int, E: float = 1.0, g_newton: float = 1.0, fixed_deposit=True):
+    """3D periodic plain PM force at the bodies, float64 FFT. Returns (acc (N,3), phi (N,))."""
+    if fixed_deposit:
+        rho = deposit_fixed(pos, mass, mask, G, E, True).astype(np.float64)
+    else:
+        rho = deposit_ref(pos, mass, mask, G, E, True)
+    F = poisson_periodic(rho, E, g_newton)
+    out = gather_ref(F, pos, G, E, True)
+    m = np.asarray(mask, np.float64)[:, None]
+    return out[:, :3] * m, out[:, 3] * m[:, 0]
+
+
+def pm_acc_isolated_2d(pos, mass, mask, G: int, E: float, eps: float, fixed_deposit=False, f32=False):
+    """pm_acc (scripts/pm_baseline_force_error.py:68-76) for one scene.
+
+    f32=False: float64 throughout (after the fp32 cell index and weights).
+    f32=True: rounds where the reference's float32 pipeline rounds — density and
+    potential grids to fp32, then the central difference and gather in fp32. The
+    potential is O(N/r) while the force is its difference across two cells, so that
+    rounding of phi sets the reference's own force noise (~1e-5 relative)."""
+    h = E / G
+    if fixed_deposit:
+        rho = deposit_fixed(pos, mass, mask, G, E, False).astype(np.float64)
+    else:
+        rho = deposit_ref(pos, mass, mask, G, E, False)
+    if f32:
+        rho = rho.astype(F32).astype(np.float64)
+    phi = isolated_phi_2d(rho, E, eps)
+    if f32:
+        F = neg_grad_2d(phi.astype(F32), h).astype(F32)
+        a, _ = gather_f32(F, pos, G, E, False)
+        return (a * np.asarray(mask, F32)[:, None]).astype(np.float64)
+    F = neg_grad_2d(phi, h)
+    out = gather_ref(F, pos, G, E, False)
+    return out[:, :2] * np.asarray(mask, np.float64)[:, None]
+
+
+# ----------------------------------------------------------------------------------
+# FP64 direct sums (scripts/scatter_scaling_ops.py:57-72) and Ewald
+# ----------------------------------------------------------------------------------
+def direct_sum(targets, sources, eps: float, mass=None, target_index=None, chunk=2048):
+    """a_t = sum_j m_j (x_j - x_t) (|x_j - x_t|^2 + eps^2)^-1.5, self pair excluded."""
+    tg = np.asarray(targets, np.float64)
+    src = np.asarray(sources, np.float64)
+    m = np.ones(len(src)) if mass is None else np.asarray(mass, np.float64)
+    out = np.zeros_like(tg)
+    for s in range(0, len(tg), chunk):
+        d = src[None, :, :] - tg[s:s + chunk, None, :]
+        r2 = (d ** 2).sum(-1) + eps ** 2
+        inv = r2 ** -1.5
+        if target_index is not None:
+            ti = np.asarray(target_index)[s:s + chunk]
+            rows = np.nonzero(ti >= 0)[0]
+            inv[rows, ti[rows]] = 0.0
+        out[s:s + chunk] = (d * (inv * m[None, :])[..., None]).sum(1)
+    return out
+
+
+def ewald_unit(x, alpha=2.0, nmax=2, hmax2=10):
+    """Periodic (unit box) acceleration at displacements x (K,3) from a unit mass at the origin,
+    including every image (no minimum-image split). Hernquist, Bouchet & Suto (1991)."""
+    x = np.asarray(x, np.float64)
+    a = np.zeros_like(x)
+    rng = range(-nmax, nmax + 1)
+    for nx in rng:
+        for ny in rng:
+            for nz in rng:
+                d = x - np.array([nx, ny, nz], np.float64)
+                r2 = (d ** 2).sum(-1)
+                r = np.sqrt(r2)
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    f = (_erfc(alpha * r) + 2 * alpha * r / np.sqrt(np.pi) * np.exp(-alpha ** 2 * r2)) / (r2 * r)
+                f = np.where(r2 > 0, f, 0.0)
+                a -= d * f[:, None]
+    hr = range(-3, 4)
+    for hx in hr:
+        for hy in hr:
+            for hz in hr:
+                h2 = hx * hx + hy * hy + hz * hz
+                if h2 == 0 or h2 > hmax2:
+                    continue
+                hv = np.array([hx, hy, hz], np.float64)
+                f = 2.0 / h2 * np.exp(-np.pi ** 2 * h2 / alpha ** 2) * np.sin(2 * np.pi * (x @ hv))
+                a -= f[:, None] * hv[None, :]
+    return a
+
+
+def _erfc(x):
+    from scipy.special import erfc
+
+    return erfc(x)
+
+
+def direct_sum_periodic(targets, sources, eps: float, box: float, mass=None, target_index=None):
+    """Periodic FP64 truth: softened minimum-image Newtonian + exact Ewald correction
+    (periodic sum minus the nearest image), evaluated without tabulation."""
+    tg = np.asarray(targets, np.float64)
+    src = np.asarray(sources, np.float64)
+    m = np.ones(len(src)) if mass is None else np.asarray(mass, np.float64)
+    out = np.zeros_like(tg)
+    for t in range(len(tg)):
+        d = src - tg[t]
+        d -= box * np.rint(d / box)
+        r2 = (d ** 2).sum(-1)
+        keep = np.ones(len(src), bool)
+        if target_index is not None and target_index[t] >= 0:
+            keep[target_index[t]] = False
+        inv = (r2 + eps ** 2) ** -1.5
+        a = (d * (inv * m)[:, None])[keep].sum(0)
+        u = -d / box
+        corr = ewald_unit(u)
+        r = np.sqrt(r2)[:, None] / box
+        with np.errstate(divide="ignore", invalid="ignore"):
+            newt = np.where(r > 0, -u / np.maximum(r, 1e-300) ** 3, 0.0)
+        corr = (corr - newt) / box ** 2
+        a += (corr * m[:, None])[keep].sum(0)
+        out[t] = a
+    return out
+
+
+# ----------------------------------------------------------------------------------
+# integrators
+# ----------------------------------------------------------------------------------
+def wrap_f32(x, E: float):
+    x = np.asarray(x, F32)
+    h = F32(E / 2)
+    x = np.where(x >= h, (x - F32(E)).astype(F32), x)
+    x = np.where(x < -h, (x + F32(E)).astype(F32), x)
+    return x.astype(F32)
+
+
+def run_kdk(pos, vel, mass, mask, G, E, dt, nsteps, force_fn):
+    """Merged kick-drift-kick as the GPU run loop: v += dt/2 a ; then per step x += dt v (wrapped),
+    a = F(x), v += dt a (last kick dt/2). force_fn(pos) -> acc (float32 arrays)."""
+    x = np.asarray(pos, F32).copy()
+    v = np.asarray(vel, F32).copy()
+    a = force_fn(x)
+    v = (v + (F32(0.5 * dt) * a).astype(F32)).astype(F32)
+    for s in range(nsteps):
+        x = wrap_f32((x + (F32(dt) * v).astype(F32)).astype(F32), E)
+        a = force_fn(x)
+        k = F32(dt) if s < nsteps - 1 else F32(0.5 * dt)
+        v = (v + (k * a).astype(F32)).astype(F32)
+    return x, v, a
+
+
+# ----------------------------------------------------------------------------------
+# metrics (scripts/pm_baseline_force_error.py:88-92)
+# ----------------------------------------------------------------------------------
+def errs(a, at, mask=None):
+    """Per-body |a - a_true| / rms(|a_true|) and |a - a_true| / |a_true|."""
+    a = np.asarray(a, np.float64)
+    at = np.asarray(at, np.float64)
+    m = np.ones(len(a)) if mask is None else np.asarray(mask, np.float64)
+    rms = np.sqrt((np.linalg.norm(at, axis=-1) ** 2 * m).sum() / m.sum())
+    e = np.linalg.norm(a - at, axis=-1) / rms
+    rel = np.linalg.norm(a - at, axis=-1) / np.maximum(np.linalg.norm(at, axis=-1), 1e-12)
+    return e[m > 0], rel[m > 0]
+
+
+def median_lower(x):
+    """torch.Tensor.median() as the reference's `stats` uses it (pm_baseline_force_error.py:95):
+    the lower of the two middle values for an even count, not their mean."""
+    x = np.sort(np.asarray(x).ravel())
+    return float(x[(len(x) - 1) // 2])
+
+
+def rel_rms(a, b):
+    """||a - b||_2 / ||b||_2 over all bodies and components."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))

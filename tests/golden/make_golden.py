@@ -1,0 +1,119 @@
+"""Generates tests/golden/*.npz from the reference implementation itself.
+
+Run in a container where the reference (Faraday-dot-py/Augur) is checked out:
+    AUGUR_REF=/root/reference python tests/golden/make_golden.py
+It imports the reference's own functions (ScatterField._corners / scatter / gather,
+pm_baseline_force_error.sample / pm_acc, scatter_scaling_ops.exact_acc), runs them on
+the CPU in float32/float64 exactly as the reference does, and stores inputs and outputs.
+The published plain-PM medians are copied from the reference's
+results/pm_baseline_force_error.json. Nothing at test time reads the reference.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import torch
+
+REF = Path(os.environ.get("AUGUR_REF", "/root/reference"))
+OUT = Path(__file__).resolve().parent
+sys.dont_write_bytecode = True
+sys.path.insert(0, str(REF))
+
+from scripts import pm_baseline_force_error as pbe  # noqa: E402
+from scripts import scatter_field as sf  # noqa: E402
+from scripts import scatter_scaling_ops as ops  # noqa: E402
+
+
+def cell_index_cases():
+    rng = np.random.default_rng(4738)
+    out = {}
+    for G, E in ((96, 1.0), (256, 1.0), (64, 1.0), (128, 64.0)):
+        D = 2 if E == 64.0 else 3
+        n = 4096
+        x = (rng.random((n, D)) - 0.5) * E
+        # stress the rounding: points within a few ulps of cell centres and faces
+        h = E / G
+        k = rng.integers(0, G, size=(n // 2, D))
+        near = (k + 0.5 * rng.integers(0, 2, size=(n // 2, D))) * h - E / 2
+        near = near + rng.integers(-3, 4, size=near.shape) * np.spacing(np.float32(np.abs(near) + 1e-3))
+        x[: n // 2] = near
+        x = x.astype(np.float32)
+        m = sf.ScatterField(grid=G, extent=E)
+        i0, w = m._corners(torch.from_numpy(x)[None])
+        out[f"G{G}_E{int(E)}_pos"] = x
+        out[f"G{G}_E{int(E)}_i0"] = i0[0].numpy().astype(np.int32)
+        out[f"G{G}_E{int(E)}_w"] = w[0].numpy()
+    np.savez_compressed(OUT / "cell_index.npz", **out)
+
+
+def scatter_gather_cases():
+    torch.manual_seed(4738)
+    m = sf.ScatterField(grid=32, extent=32.0)
+    g = torch.Generator().manual_seed(4738)
+    n = 400
+    pos = ((torch.rand(1, n, 2, generator=g) - 0.5) * 36.0).float()  # some bodies off the grid
+    vel = torch.randn(1, n, 2, generator=g).float()
+    mass = (0.5 + torch.rand(1, n, generator=g)).float()
+    mask = (torch.rand(1, n, generator=g) > 0.1).float()
+    grid = m.scatter(pos, vel, mass, mask)
+    field = torch.randn(1, 4, 32, 32, generator=g).float()
+    gat = m.gather(field, pos)
+    np.savez_compressed(OUT / "scatter_gather_2d.npz", pos=pos[0].numpy(), vel=vel[0].numpy(),
+                        mass=mass[0].numpy(), mask=mask[0].numpy(), grid=grid[0].numpy(),
+                        field=field[0].numpy(), gather=gat[0].numpy(), G=32, E=32.0)
+
+
+def pm_acc_cases():
+    """Scenes of scripts/pm_baseline_force_error.py main() with its seed and order, then the
+    reference's pm_acc in float32 on the CPU (G=128, extent=64, EPS=0.5)."""
+    model = sf.ScatterField(grid=128, extent=64.0, net="unet", recurrent=True, hidden_ch=0, dt=0.1, momfix=True,
+                            in_scale=1.0, potential=True, kernel=True, pp=2.0, split=True, verlet=True).eval()
+    rng = np.random.default_rng(4738)
+    pub = json.load(open(REF / "results" / "pm_baseline_force_error.json"))
+    out = {}
+    keep = {("plummer", 300), ("plummer", 1000), ("two_clump", 300), ("exp_disk", 300)}
+    for fam in pbe.FAMILIES:
+        for n in (300, 1000, 10000, 100000):
+            ns = pbe.NS[n]
+            pos_np = np.stack([pbe.sample(fam, n, rng, 1.0) for _ in range(ns)])
+            if (fam, n) not in keep:
+                continue  # the generator stream is consumed in the reference's order regardless
+            pos = torch.tensor(pos_np, dtype=torch.float32)
+            vel = torch.zeros_like(pos)
+            mass = torch.ones(ns, n)
+            mask = torch.ones(ns, n)
+            with torch.no_grad():
+                acc = pbe.pm_acc(model, pos, vel, mass, mask)
+            at = torch.stack([ops.exact_acc(p.double(), pbe.EPS) for p in pos])
+            e, _ = pbe.errs(acc.double(), at, mask.double())
+            key = f"{fam}_n{n}"
+            out[key + "_pos"] = pos.numpy()
+            out[key + "_acc"] = acc.numpy()
+            out[key + "_median_here"] = np.float64(e.median())
+            out[key + "_median_published"] = np.float64(pub[key]["plain_pm"]["norm_by_rms"]["median"])
+            out[key + "_p90_published"] = np.float64(pub[key]["plain_pm"]["norm_by_rms"]["p90"])
+    np.savez_compressed(OUT / "pm_acc_2d.npz", **out)
+
+
+def exact_acc_cases():
+    g = torch.Generator().manual_seed(9100)
+    out = {}
+    for D, n, eps in ((2, 300, 0.5), (3, 512, 1.0 / 64)):
+        pos = (torch.randn(n, D, generator=g, dtype=torch.float64) * 0.1)
+        out[f"d{D}_pos"] = pos.numpy()
+        out[f"d{D}_acc"] = ops.exact_acc(pos, eps).numpy()
+        out[f"d{D}_eps"] = np.float64(eps)
+    np.savez_compressed(OUT / "exact_acc.npz", **out)
+
+
+if __name__ == "__main__":
+    cell_index_cases()
+    scatter_gather_cases()
+    pm_acc_cases()
+    exact_acc_cases()
+    for p in sorted(OUT.glob("*.npz")):
+        print(p.name, p.stat().st_size)
