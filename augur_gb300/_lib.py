@@ -33,6 +33,7 @@ SIGNATURES = {
     "augur_pm_run_begin": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),
     "augur_pm_run_steps": (_i32, [_vp, _i32, _vp]),
     "augur_pm_run_end": (_i32, [_vp, _vp, _vp, _vp, _vp]),
+    "augur_pm_run_profile": (_i32, [_vp, _i32, _vp, _i32, _vp]),
     "augur_pm_last_launches": (_i64, [_vp]),
     "augur_pm_check": (_i32, [_vp, _vp]),
     "augur_direct_sum_fp64": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp]),

@@ -35,9 +35,10 @@ __device__ __forceinline__ float2 mul_pi(float2 a) { return make_float2(-a.y, a.
 // bit-exact CIC axis: u = (x + E/2)/h - 0.5 ; i0 = floor(u) ; w = u - i0
 // (scripts/scatter_field.py:179-182). Returns false for non-finite or huge u.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ bool cic_axis(float x, float half_ext, float h, int &i0, float &w) {
+__device__ __forceinline__ bool cic_axis(float x, float half_ext, float h, int &i0, float &w, float inv_h = 0.f) {
   float t = __fadd_rn(x, half_ext);
-  float u = __fsub_rn(__fdiv_rn(t, h), 0.5f);
+  // when h is a power of two, t / h == t * (1/h) exactly, so the multiply is bit-identical
+  float u = __fsub_rn(inv_h != 0.f ? __fmul_rn(t, inv_h) : __fdiv_rn(t, h), 0.5f);
   if (!(fabsf(u) < 1.0e9f)) {  // catches NaN and inf
     i0 = 0;
     w = 0.f;
@@ -52,6 +53,38 @@ __device__ __forceinline__ bool cic_axis(float x, float half_ext, float h, int &
 __device__ __forceinline__ int wrap_idx(int i, int G) {
   int r = i % G;
   return r < 0 ? r + G : r;
+}
+
+// wrap into [0, G): the common in-box cases without a division
+__device__ __forceinline__ int fwrap(int i, int G) {
+  if ((unsigned)i < (unsigned)G) return i;
+  if (i == -1) return G - 1;
+  if (i == G) return 0;
+  return wrap_idx(i, G);
+}
+
+// Division by a runtime-invariant divisor for dividends < 2^31 (Granlund & Montgomery,
+// PLDI 1994): q = umulhi(n, mul) >> shr with mul = ceil(2^(31+l) / d), l = ceil(log2 d).
+struct FastDiv {
+  uint32_t d, mul, shr;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  if (d <= 1) {
+    f.mul = 0;
+    f.shr = 0;
+    return f;
+  }
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  uint64_t p = 31 + l;
+  f.mul = (uint32_t)(((1ull << p) + d - 1) / d);
+  f.shr = (uint32_t)(p - 32);
+  return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  return f.mul ? (__umulhi(n, f.mul) >> f.shr) : n;
 }
 
 // weight factor of one axis for corner offset o (0 -> 1-w, 1 -> w), fp32 like the reference
@@ -100,6 +133,35 @@ __device__ __forceinline__ void dft(float2 *v, bool inv) {
     v[2] = csub(t0, t2);
     v[1] = cadd(t1, r3);
     v[3] = csub(t1, r3);
+  } else if constexpr (R == 16) {
+    // 16 = 4 x 4: DFT4 over n1 of x[4 n1 + n2], twiddle W16^(n2 k1), DFT4 over n2
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, r2 = 0.70710678118654752440f;
+    const float sg = inv ? 1.f : -1.f;
+    float2 y[4][4];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      float2 t[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+      dft<4>(t, inv);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = t[k1];
+    }
+    // twiddles W16^m, m = n2 * k1 (forward: exp(-2 pi i m / 16))
+    y[1][1] = cmul(y[1][1], make_float2(c1, sg * s1));
+    y[1][2] = cmul(y[1][2], make_float2(r2, sg * r2));
+    y[1][3] = cmul(y[1][3], make_float2(s1, sg * c1));
+    y[2][1] = cmul(y[2][1], make_float2(r2, sg * r2));
+    y[2][2] = inv ? mul_pi(y[2][2]) : mul_mi(y[2][2]);
+    y[2][3] = cmul(y[2][3], make_float2(-r2, sg * r2));
+    y[3][1] = cmul(y[3][1], make_float2(s1, sg * c1));
+    y[3][2] = cmul(y[3][2], make_float2(-r2, sg * r2));
+    y[3][3] = cmul(y[3][3], make_float2(-c1, -sg * s1));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      float2 t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+      dft<4>(t, inv);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+    }
   } else if constexpr (R == 8) {
     const float r2 = 0.70710678118654752440f;
     float2 e[4] = {v[0], v[2], v[4], v[6]};
@@ -122,32 +184,73 @@ __device__ __forceinline__ void dft(float2 *v, bool inv) {
   }
 }
 
-template <int R>
-__device__ __forceinline__ void fft_stage(const float2 *__restrict__ in, float2 *__restrict__ out, int L, int Ns,
-                                          int nb, int es, int bs, const float2 *__restrict__ tw, int twmul,
-                                          bool inv, int tid, int nt) {
-  const int nbf = L / R;
-  const int total = nb * nbf;
-  const int tstride = (L / (Ns * R)) * twmul;
-  for (int idx = tid; idx < total; idx += nt) {
+// ---------------------------------------------------------------------------------
+// Compile-time FFT: Stockham stages with the length (and, for column transforms, the
+// number of interleaved columns) as template parameters so that every index division
+// folds to shifts and multiplies. Radix order: 3s first, then 16s, then one 8, 4 or 2;
+// a radix-16 butterfly is done in registers as 4 x 4, so 128- and 256-point transforms
+// take two shared-memory passes.
+// ---------------------------------------------------------------------------------
+constexpr int fft_radix(int L, int s) {
+  int r[16] = {};
+  int n = 0, x = L;
+  while (x % 3 == 0) {
+    r[n++] = 3;
+    x /= 3;
+  }
+  while (x % 16 == 0) {
+    r[n++] = 16;
+    x /= 16;
+  }
+  if (x == 8 || x == 4 || x == 2) r[n++] = x;
+  return (s < n) ? r[s] : 0;
+}
+constexpr int fft_nstages(int L) {
+  int n = 0;
+  while (fft_radix(L, n)) ++n;
+  return n;
+}
+constexpr int fft_ns(int L, int s) {
+  int ns = 1;
+  for (int i = 0; i < s; ++i) ns *= fft_radix(L, i);
+  return ns;
+}
+
+// COLS == 0: nb rows of L contiguous elements, row stride bs (batch index slow).
+// COLS > 0 : COLS interleaved columns, element e of column b at buf[e*COLS + b].
+template <int R, int L, int NS, int COLS>
+__device__ __forceinline__ void fft_stage_t(const float2 *__restrict__ in, float2 *__restrict__ out, int nb, int bs,
+                                            const float2 *__restrict__ tw, int twmul, bool inv) {
+  constexpr int nbf = L / R;
+  constexpr int tstride = L / (NS * R);
+  const int total = (COLS > 0 ? COLS : nb) * nbf;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
     int b, j;
-    if (es == 1) {
+    if constexpr (COLS > 0) {
+      j = idx / COLS;
+      b = idx - j * COLS;
+    } else {
       b = idx / nbf;
       j = idx - b * nbf;
-    } else {
-      j = idx / nb;
-      b = idx - j * nb;
     }
-    const float2 *src = in + (size_t)b * bs;
-    float2 *dst = out + (size_t)b * bs;
+    const float2 *src;
+    float2 *dst;
+    constexpr int es = COLS > 0 ? COLS : 1;
+    if constexpr (COLS > 0) {
+      src = in + b;
+      dst = out + b;
+    } else {
+      src = in + (size_t)b * bs;
+      dst = out + (size_t)b * bs;
+    }
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = src[(j + r * nbf) * es];
-    const int k = j % Ns;
-    if (Ns > 1) {
+    const int k = j % NS;
+    if constexpr (NS > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        float2 t = tw[r * k * tstride];
+        float2 t = tw[r * k * tstride * twmul];
         if (inv) t.y = -t.y;
         v[r] = cmul(v[r], t);
       }
@@ -155,31 +258,156 @@ __device__ __forceinline__ void fft_stage(const float2 *__restrict__ in, float2 
     dft<R>(v, inv);
     const int base = (j - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[(base + r * Ns) * es] = v[r];
+    for (int r = 0; r < R; ++r) dst[(base + r * NS) * es] = v[r];
   }
 }
 
-// Runs all stages; returns the buffer holding the result (a or b).
-__device__ __forceinline__ float2 *fft_smem(const FftShape &sh, float2 *a, float2 *b, int nb, int es, int bs,
-                                            const float2 *tw, int twmul, bool inv) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  int Ns = 1;
-  float2 *in = a, *out = b;
-  for (int s = 0; s < sh.nstages; ++s) {
-    const int R = sh.radix[s];
-    switch (R) {
-      case 2: fft_stage<2>(in, out, sh.L, Ns, nb, es, bs, tw, twmul, inv, tid, nt); break;
-      case 3: fft_stage<3>(in, out, sh.L, Ns, nb, es, bs, tw, twmul, inv, tid, nt); break;
-      case 4: fft_stage<4>(in, out, sh.L, Ns, nb, es, bs, tw, twmul, inv, tid, nt); break;
-      default: fft_stage<8>(in, out, sh.L, Ns, nb, es, bs, tw, twmul, inv, tid, nt); break;
-    }
+template <int L, int COLS, int S = 0>
+__device__ __forceinline__ float2 *fft_t(float2 *in, float2 *out, int nb, int bs, const float2 *tw, int twmul,
+                                         bool inv) {
+  if constexpr (S < fft_nstages(L)) {
+    fft_stage_t<fft_radix(L, S), L, fft_ns(L, S), COLS>(in, out, nb, bs, tw, twmul, inv);
     __syncthreads();
-    Ns *= R;
-    float2 *t = in;
-    in = out;
-    out = t;
+    return fft_t<L, COLS, S + 1>(out, in, nb, bs, tw, twmul, inv);
+  } else {
+    return in;
   }
-  return in;
+}
+
+// ---------------------------------------------------------------------------------
+// Transform with caller-supplied first load and last store: stage 0 reads element e of
+// transform b through ld(b, e), the last stage writes through st(b, e, value), and the
+// stages in between ping-pong through shared memory (bufA, bufB; row stride bs in row
+// mode, column-interleaved in column mode). A two-stage length (128, 256, ...) touches
+// shared memory once. Ends with __syncthreads().
+// COLS == 0: nb transforms, thread index maps to (b slow, j fast).
+// COLS > 0 : COLS transforms, thread index maps to (j slow, b fast), smem buf[e*COLS + b].
+// ---------------------------------------------------------------------------------
+template <int R, int L, int NS, int COLS, class LD, class ST>
+__device__ __forceinline__ void fft_stage_io(int nb, LD &ld, ST &st, const float2 *__restrict__ tw, int twmul,
+                                             bool inv) {
+  constexpr int nbf = L / R;
+  constexpr int tstride = L / (NS * R);
+  const int total = (COLS > 0 ? COLS : nb) * nbf;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    int b, j;
+    if constexpr (COLS > 0) {
+      j = idx / COLS;
+      b = idx - j * COLS;
+    } else {
+      b = idx / nbf;
+      j = idx - b * nbf;
+    }
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = ld(b, j + r * nbf);
+    const int k = j % NS;
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        float2 t = tw[r * k * tstride * twmul];
+        if (inv) t.y = -t.y;
+        v[r] = cmul(v[r], t);
+      }
+    }
+    dft<R>(v, inv);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) st(b, base + r * NS, v[r]);
+  }
+}
+
+template <int L, int COLS, int S, class LD, class ST>
+__device__ __forceinline__ void fft_io_rec(int nb, LD &ld, ST &st, float2 *in, float2 *out, int bs,
+                                           const float2 *tw, int twmul, bool inv) {
+  constexpr int NSTG = fft_nstages(L);
+  constexpr int R = fft_radix(L, S);
+  constexpr int NS = fft_ns(L, S);
+  auto sld = [&](int b, int e) -> float2 { return COLS > 0 ? in[e * COLS + b] : in[b * bs + e]; };
+  auto sst = [&](int b, int e, float2 v) {
+    if (COLS > 0) out[e * COLS + b] = v;
+    else out[b * bs + e] = v;
+  };
+  if constexpr (NSTG == 1) {
+    fft_stage_io<R, L, NS, COLS>(nb, ld, st, tw, twmul, inv);
+    __syncthreads();
+  } else if constexpr (S == 0) {
+    fft_stage_io<R, L, NS, COLS>(nb, ld, sst, tw, twmul, inv);
+    __syncthreads();
+    fft_io_rec<L, COLS, S + 1>(nb, ld, st, out, in, bs, tw, twmul, inv);
+  } else if constexpr (S == NSTG - 1) {
+    fft_stage_io<R, L, NS, COLS>(nb, sld, st, tw, twmul, inv);
+    __syncthreads();
+  } else {
+    fft_stage_io<R, L, NS, COLS>(nb, sld, sst, tw, twmul, inv);
+    __syncthreads();
+    fft_io_rec<L, COLS, S + 1>(nb, ld, st, out, in, bs, tw, twmul, inv);
+  }
+}
+
+template <int L, int COLS, class LD, class ST>
+__device__ __forceinline__ void fft_io(int nb, LD ld, ST st, float2 *bufA, float2 *bufB, int bs, const float2 *tw,
+                                       int twmul, bool inv) {
+  fft_io_rec<L, COLS, 0>(nb, ld, st, bufA, bufB, bs, tw, twmul, inv);
+}
+
+#define AUGUR_FFT_LENGTHS(X) \
+  X(8) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048)
+
+// Calls fft_io<N, COLS>(args...) for the runtime length L (one of AUGUR_FFT_LENGTHS).
+#define AUGUR_FFT_IO(L, COLS, ...)                         \
+  switch (L) {                                            \
+    case 8: fft_io<8, COLS>(__VA_ARGS__); break;          \
+    case 16: fft_io<16, COLS>(__VA_ARGS__); break;        \
+    case 24: fft_io<24, COLS>(__VA_ARGS__); break;        \
+    case 32: fft_io<32, COLS>(__VA_ARGS__); break;        \
+    case 48: fft_io<48, COLS>(__VA_ARGS__); break;        \
+    case 64: fft_io<64, COLS>(__VA_ARGS__); break;        \
+    case 96: fft_io<96, COLS>(__VA_ARGS__); break;        \
+    case 128: fft_io<128, COLS>(__VA_ARGS__); break;      \
+    case 192: fft_io<192, COLS>(__VA_ARGS__); break;      \
+    case 256: fft_io<256, COLS>(__VA_ARGS__); break;      \
+    case 384: fft_io<384, COLS>(__VA_ARGS__); break;      \
+    case 512: fft_io<512, COLS>(__VA_ARGS__); break;      \
+    case 768: fft_io<768, COLS>(__VA_ARGS__); break;      \
+    case 1024: fft_io<1024, COLS>(__VA_ARGS__); break;    \
+    case 1536: fft_io<1536, COLS>(__VA_ARGS__); break;    \
+    case 2048: fft_io<2048, COLS>(__VA_ARGS__); break;    \
+    default: break;                                       \
+  }
+
+inline bool fft_length_supported(int L) {
+  switch (L) {
+#define AUGUR_CASE(N) \
+  case N: return true;
+    AUGUR_FFT_LENGTHS(AUGUR_CASE)
+#undef AUGUR_CASE
+    default: return false;
+  }
+}
+
+// Row transforms: nb rows of length L, row stride bs. Returns the result buffer.
+__device__ __forceinline__ float2 *fft_rows(int L, float2 *a, float2 *b, int nb, int bs, const float2 *tw, int twmul,
+                                            bool inv) {
+  switch (L) {
+#define AUGUR_CASE(N) \
+  case N: return fft_t<N, 0>(a, b, nb, bs, tw, twmul, inv);
+    AUGUR_FFT_LENGTHS(AUGUR_CASE)
+#undef AUGUR_CASE
+    default: return nullptr;
+  }
+}
+
+// Column transforms: COLS interleaved columns of length L.
+template <int COLS>
+__device__ __forceinline__ float2 *fft_cols(int L, float2 *a, float2 *b, const float2 *tw, int twmul, bool inv) {
+  switch (L) {
+#define AUGUR_CASE(N) \
+  case N: return fft_t<N, COLS>(a, b, COLS, 0, tw, twmul, inv);
+    AUGUR_FFT_LENGTHS(AUGUR_CASE)
+#undef AUGUR_CASE
+    default: return nullptr;
+  }
 }
 
 }  // namespace augur

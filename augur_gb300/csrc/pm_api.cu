@@ -30,6 +30,14 @@ struct augur_pm_plan {
   int cur;
   uint32_t *key, *slot, *row_count, *row_start, *tile_sum, *tile_off;
   unsigned *d_err, *d_mmax;
+  // deposit work items (row blocks split into body chunks) and partial fixed-point tiles
+  int nblk;
+  uint32_t *dep_nch, *dep_item_off, *dep_slot_off, *dep_counters, *dep_item_blk;
+  uint2 *dep_seg_tab;
+  size_t dep_items_max;
+  unsigned long long *dep_scratch;
+  size_t dep_slots;
+  int64_t cur_n;  // bodies in the sorted state
   float2 *spec, *spec3, *khat;
   float4 *F4;
   float *real_tmp, *phi2d, *rho2d;
@@ -100,6 +108,13 @@ int dalloc(augur_pm_plan *p, T **ptr, size_t count) {
 
 unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+constexpr uint32_t DEP_CHUNK_MIN = 16384;
+uint32_t dep_chunk(int64_t n) {
+  int64_t c = (n + 1023) / 1024;
+  return (uint32_t)std::max<int64_t>(DEP_CHUNK_MIN, c);
+}
+size_t dep_slots_bound(int64_t n) { return (size_t)8 * (size_t)((n + dep_chunk(n) - 1) / dep_chunk(n)) + 1; }
+
 cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
 // ---- pipeline pieces ----------------------------------------------------------------
@@ -107,6 +122,7 @@ cudaStream_t S(void *s) { return (cudaStream_t)s; }
 int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *acc, const float *mass,
                   const float *mask, int64_t n, bool drift, float dt, cudaStream_t st) {
   const GridParams &g = p->gp;
+  p->cur_n = n;
   if (cudaMemsetAsync(p->row_count, 0, sizeof(uint32_t) * p->nrow, st) != cudaSuccess) return AUGUR_ECUDA;
   if (cudaMemsetAsync(p->d_mmax, 0, sizeof(unsigned), st) != cudaSuccess) return AUGUR_ECUDA;
   const unsigned nb = blocks_for(n, 256);
@@ -148,6 +164,7 @@ int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *a
 // re-sort the run state after a gather that produced keys + histogram
 int resort(augur_pm_plan *p, cudaStream_t st) {
   const int64_t n = p->run_n;
+  p->cur_n = n;
   scan_local_kernel<<<p->ntiles, 1024, 0, st>>>(p->row_count, p->row_start, p->tile_sum, p->nrow);
   AUGUR_LAUNCH_CHECK(p);
   scan_tiles_kernel<<<1, 1024, 0, st>>>(p->tile_sum, p->tile_off, p->ntiles);
@@ -171,32 +188,39 @@ DepositArgs dep_args(const augur_pm_plan *p) {
   a.fsh = p->sh_M;
   a.twmul = p->Lt / p->M;
   a.Lt = p->Lt;
+  a.nblk = p->nblk;
+  a.chunk = dep_chunk(p->cur_n);
+  a.fdG = make_fastdiv(p->G);
+  a.fdRR = make_fastdiv(a.RY * a.RZ);
+  a.fdRY = make_fastdiv(a.RY);
   return a;
 }
 
-unsigned dep_blocks(const augur_pm_plan *p) {
-  const int G = p->G;
-  return p->dim == 3 ? (unsigned)((G / p->dep_RY) * (G / p->dep_RZ)) : (unsigned)(G / p->dep_RY);
+// work-item plan + deposit of the sorted state: MODE 0 writes rho, MODE 1 the x-transformed spectrum
+template <int D, int MODE>
+int launch_deposit(augur_pm_plan *p, float *rho, float2 *spec, cudaStream_t st) {
+  DepositArgs a = dep_args(p);
+  deposit_plan_kernel<D><<<1, 1024, 0, st>>>(p->row_start, p->tile_off, a, p->dep_nch, p->dep_item_off,
+                                              p->dep_slot_off, p->dep_seg_tab, p->dep_item_blk, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
+  const int64_t items = (int64_t)p->nblk + 4 * ((p->cur_n + a.chunk - 1) / a.chunk) + 1;
+  if ((size_t)items > p->dep_items_max) return AUGUR_ERANGE;
+  deposit_kernel<D, MODE><<<(unsigned)items, 512, p->smem_dep, st>>>(
+      p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
+      p->dep_item_blk, p->dep_scratch, p->dep_counters);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
 }
 
 int deposit_rho(augur_pm_plan *p, float *rho, cudaStream_t st) {
-  DepositArgs a = dep_args(p);
-  size_t sm = (size_t)a.RY * a.RZ * p->G * 12 + (size_t)a.RY * a.RZ * 8;
-  if (p->dim == 3)
-    deposit_kernel<3, 0><<<dep_blocks(p), 512, sm, st>>>(p->pos4[p->cur], p->row_start, p->tile_off, p->d_mmax, a,
-                                                          p->tw, rho, nullptr, p->d_err);
-  else
-    deposit_kernel<2, 0><<<dep_blocks(p), 512, sm, st>>>(p->pos4[p->cur], p->row_start, p->tile_off, p->d_mmax, a,
-                                                          p->tw, rho, nullptr, p->d_err);
-  AUGUR_LAUNCH_CHECK(p);
-  return AUGUR_OK;
+  return p->dim == 3 ? launch_deposit<3, 0>(p, rho, nullptr, st) : launch_deposit<2, 0>(p, rho, nullptr, st);
 }
 
 int fft_rows(augur_pm_plan *p, float2 *data, int64_t nrows, bool inverse, cudaStream_t st) {
   const int L = p->L;
   const int RB = p->rows_RB;
-  fft_rows_kernel<<<blocks_for(nrows, RB), 256, p->smem_rows, st>>>(data, nrows, RB, L, p->sh_L, p->Lt / L, p->Lt,
-                                                                     p->tw, inverse ? 1 : 0);
+  fft_rows_kernel<<<blocks_for(nrows, RB), 256, p->smem_rows, st>>>(data, nrows, RB, L, make_fastdiv(L), p->Lt / L,
+                                                                     p->Lt, p->tw, inverse ? 1 : 0);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -214,8 +238,10 @@ int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   ga.fsh = p->sh_L;
   ga.kfund = (float)(2.0 * M_PI / p->extent);
   ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
-  fft_z_green_kernel<<<(unsigned)((M + 1) * (G / p->green_TY)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
-                                                                                           p->spec3);
+  if (p->green_TY == 16)
+    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+  else
+    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
   AUGUR_LAUNCH_CHECK(p);
   rc = fft_rows(p, p->spec3, (int64_t)ncomp * (M + 1) * G, true, st);
   if (rc) return rc;
@@ -230,6 +256,9 @@ int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   ca.scale = 1.f;
   ca.fsh = p->sh_M;
   ca.twmul = p->Lt / M;
+  ca.fdRB = make_fastdiv(ca.RB);
+  ca.fdM = make_fastdiv(ca.L / 2);
+  ca.fdL = make_fastdiv(ca.L);
   c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec3, ca, p->tw,
                                                                                  reinterpret_cast<float *>(F4));
   AUGUR_LAUNCH_CHECK(p);
@@ -246,6 +275,8 @@ int r2c_rows(augur_pm_plan *p, const float *in, int Lin, int nin, int nout, floa
   ra.Lt = p->Lt;
   ra.fsh = p->sh_M;
   ra.twmul = p->Lt / p->M;
+  ra.fdL = make_fastdiv(ra.L);
+  ra.fdRB = make_fastdiv(ra.RB);
   r2c_rows_kernel<<<blocks_for(nout, ra.RB), 256, p->smem_r2c, st>>>(in, ra, p->tw, out);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
@@ -275,6 +306,9 @@ int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream
   ca.scale = (float)(h * h / ((double)L * L));
   ca.fsh = p->sh_M;
   ca.twmul = p->Lt / p->M;
+  ca.fdRB = make_fastdiv(ca.RB);
+  ca.fdM = make_fastdiv(ca.L / 2);
+  ca.fdL = make_fastdiv(ca.L);
   c2r_rows_kernel<false><<<(unsigned)((G + p->c2r_RB - 1) / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec, ca, p->tw,
                                                                                                p->phi2d);
   AUGUR_LAUNCH_CHECK(p);
@@ -286,10 +320,8 @@ int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream
 // sorted bodies -> F4 (the grid force of the plan's mode)
 int grid_force(augur_pm_plan *p, int ncomp, cudaStream_t st) {
   if (p->mode == AUGUR_MODE_PERIODIC) {
-    DepositArgs a = dep_args(p);
-    deposit_kernel<3, 1><<<dep_blocks(p), 512, p->smem_dep, st>>>(p->pos4[p->cur], p->row_start, p->tile_off,
-                                                                   p->d_mmax, a, p->tw, nullptr, p->spec, p->d_err);
-    AUGUR_LAUNCH_CHECK(p);
+    int rc = launch_deposit<3, 1>(p, nullptr, p->spec, st);
+    if (rc) return rc;
     return periodic_tail(p, ncomp, p->F4, st);
   }
   int rc = deposit_rho(p, p->rho2d, st);
@@ -351,7 +383,8 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
   if (!p) return AUGUR_OK;
   void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
-                  p->F4, p->real_tmp, p->phi2d, p->rho2d};
+                  p->F4, p->real_tmp, p->phi2d, p->rho2d, p->dep_nch, p->dep_item_off, p->dep_slot_off,
+                  p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -387,13 +420,19 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   g.half_ext = (float)(extent / 2.0);
   g.ext = (float)extent;
   g.inv_hD = (float)(1.0 / (dim == 3 ? h * h * h : h * h));
+  {
+    int ex = 0;
+    float mant = std::frexp(g.h, &ex);
+    g.inv_h = (mant == 0.5f) ? 1.0f / g.h : 0.0f;  // exact reciprocal of a power of two
+  }
   p->nrow = (dim == 3) ? G * G : G + 2;
   g.nrow = p->nrow;
   p->ntiles = (p->nrow + SCAN_TILE - 1) / SCAN_TILE;
   p->L = g.periodic ? G : 2 * G;
   p->M = p->L / 2;
   p->Lt = p->L;
-  if (!factor(p->M, p->sh_M) || !factor(p->L, p->sh_L)) {
+  if (!factor(p->M, p->sh_M) || !factor(p->L, p->sh_L) || !fft_length_supported(p->M) ||
+      !fft_length_supported(p->L)) {
     delete p;
     return AUGUR_EINVAL;
   }
@@ -417,11 +456,11 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   p->rows_RB = p->L >= 4096 ? 1 : 4096 / p->L;
   p->r2c_RB = 16;
   const int M = p->M, L = p->L, Lt = p->Lt;
-  p->smem_dep = (size_t)p->dep_RY * p->dep_RZ * G * 12 + (size_t)p->dep_RY * p->dep_RZ * 8 + (size_t)Lt * 8;
+  p->smem_dep = (size_t)p->dep_RY * p->dep_RZ * (G + 2) * 12 + (size_t)Lt * 8;
   p->smem_green = (size_t)3 * G * p->green_TY * 8 + (size_t)Lt * 8;
   p->smem_c2r = (size_t)2 * p->c2r_RB * (M + 1) * 8 + (size_t)(g.periodic ? 4 : 1) * p->c2r_RB * L * 4 + (size_t)Lt * 8;
   p->smem_rows = (size_t)2 * p->rows_RB * (L + 1) * 8 + (size_t)Lt * 8;
-  p->smem_r2c = (size_t)2 * p->r2c_RB * (M + 1) * 8 + (size_t)Lt * 8;
+  p->smem_r2c = (size_t)3 * p->r2c_RB * (M + 1) * 8 + (size_t)Lt * 8;
 
   int rc = AUGUR_OK;
   const int64_t N = max_bodies;
@@ -442,6 +481,16 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   rc |= dalloc(p, &p->d_mmax, 1);
   rc |= dalloc(p, &p->spec, nspec);
   rc |= dalloc(p, &p->F4, ncell);
+  p->nblk = (dim == 3) ? (G / p->dep_RY) * (G / p->dep_RZ) : G / p->dep_RY;
+  p->dep_slots = dep_slots_bound(N);
+  rc |= dalloc(p, &p->dep_nch, (size_t)p->nblk);
+  rc |= dalloc(p, &p->dep_item_off, (size_t)p->nblk + 1);
+  rc |= dalloc(p, &p->dep_slot_off, (size_t)p->nblk);
+  rc |= dalloc(p, &p->dep_counters, (size_t)p->nblk);
+  p->dep_items_max = (size_t)p->nblk + 4 * (size_t)((N + dep_chunk(N) - 1) / dep_chunk(N)) + 1;
+  rc |= dalloc(p, &p->dep_item_blk, p->dep_items_max);
+  rc |= dalloc(p, &p->dep_seg_tab, (size_t)p->nblk * (MAXSEGB + 1));
+  rc |= dalloc(p, &p->dep_scratch, p->dep_slots * (size_t)p->dep_RY * p->dep_RZ * G);
   if (dim == 3) {
     rc |= dalloc(p, &p->spec3, 4 * nspec);
   } else {
@@ -458,6 +507,7 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   cudaMemset(p->row_start, 0, sizeof(uint32_t) * (size_t)(p->ntiles + 1) * SCAN_TILE);
   cudaMemset(p->d_err, 0, sizeof(unsigned));
   cudaMemset(p->d_mmax, 0, sizeof(unsigned));
+  cudaMemset(p->dep_counters, 0, sizeof(uint32_t) * p->nblk);
   // twiddles exp(-2 pi i t / Lt) in double, rounded once to float
   std::vector<float2> tw(Lt);
   for (int t = 0; t < Lt; ++t) {
@@ -472,7 +522,8 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   cudaFuncSetAttribute(deposit_kernel<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
   cudaFuncSetAttribute(deposit_kernel<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
   cudaFuncSetAttribute(deposit_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
-  cudaFuncSetAttribute(fft_z_green_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
+  cudaFuncSetAttribute(fft_z_green_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
+  cudaFuncSetAttribute(fft_z_green_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
   cudaFuncSetAttribute(c2r_rows_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
   cudaFuncSetAttribute(c2r_rows_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
   cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_rows);
@@ -643,6 +694,79 @@ int augur_pm_run_steps(augur_pm_plan *p, int k, void *stream) {
     if (rc) return rc;
   }
   return AUGUR_OK;
+}
+
+int augur_pm_run_profile(augur_pm_plan *p, int k, float *stage_ms, int nstage, void *stream) {
+  if (!p || !p->run_active || k < 1 || !stage_ms || nstage < AUGUR_PM_NSTAGE) return AUGUR_EINVAL;
+  if (p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  cudaEvent_t ev[AUGUR_PM_NSTAGE + 1];
+  for (int i = 0; i <= AUGUR_PM_NSTAGE; ++i)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) return AUGUR_ECUDA;
+  double acc[AUGUR_PM_NSTAGE] = {0};
+  int rc = AUGUR_OK;
+  const int G = p->G, M = p->M;
+  for (int s = 0; s < k && rc == AUGUR_OK; ++s) {
+    cudaEventRecord(ev[0], st);
+    rc = resort(p, st);
+    cudaEventRecord(ev[1], st);
+    if (!rc) rc = launch_deposit<3, 1>(p, nullptr, p->spec, st);
+    cudaEventRecord(ev[2], st);
+    if (!rc) rc = fft_rows(p, p->spec, (int64_t)(M + 1) * G, false, st);
+    cudaEventRecord(ev[3], st);
+    if (!rc) {
+      GreenArgs ga;
+      ga.G = G;
+      ga.TY = p->green_TY;
+      ga.ncomp = 3;
+      ga.Lt = p->Lt;
+      ga.fsh = p->sh_L;
+      ga.kfund = (float)(2.0 * M_PI / p->extent);
+      ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
+      if (p->green_TY == 16)
+        fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
+                                                                                          p->spec3);
+      else
+        fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
+                                                                                         p->spec3);
+    }
+    cudaEventRecord(ev[4], st);
+    if (!rc) rc = fft_rows(p, p->spec3, (int64_t)3 * (M + 1) * G, true, st);
+    cudaEventRecord(ev[5], st);
+    if (!rc) {
+      C2RArgs ca;
+      ca.L = G;
+      ca.nrows = G * G;
+      ca.RB = p->c2r_RB;
+      ca.ncomp = 3;
+      ca.Lt = p->Lt;
+      ca.nkeep = G * G;
+      ca.Lkeep = G;
+      ca.scale = 1.f;
+      ca.fsh = p->sh_M;
+      ca.twmul = p->Lt / M;
+      ca.fdRB = make_fastdiv(ca.RB);
+      ca.fdM = make_fastdiv(ca.L / 2);
+      ca.fdL = make_fastdiv(ca.L);
+  ca.fdRB = make_fastdiv(ca.RB);
+  ca.fdM = make_fastdiv(ca.L / 2);
+  ca.fdL = make_fastdiv(ca.L);
+      c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, p->smem_c2r, st>>>(
+          p->spec3, ca, p->tw, reinterpret_cast<float *>(p->F4));
+    }
+    cudaEventRecord(ev[6], st);
+    if (!rc) rc = run_gather(p, p->run_dt, 1, nullptr, st);
+    cudaEventRecord(ev[7], st);
+    if (cudaEventSynchronize(ev[7]) != cudaSuccess) rc = AUGUR_ECUDA;
+    for (int i = 0; i < AUGUR_PM_NSTAGE && rc == AUGUR_OK; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+      acc[i] += ms;
+    }
+  }
+  for (int i = 0; i <= AUGUR_PM_NSTAGE; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < AUGUR_PM_NSTAGE; ++i) stage_ms[i] = (float)(acc[i] / k);
+  return rc;
 }
 
 int augur_pm_run_end(augur_pm_plan *p, float *pos, float *vel, float *acc_out, void *stream) {

@@ -27,6 +27,7 @@ struct GridParams {
   float half_ext; // fp32(extent / 2)
   float ext;      // fp32(extent)
   float inv_hD;   // fp32(1 / h^D) (density scale of ScatterField.scatter, in_scale = 1)
+  float inv_h;    // 1/h when h is a power of two (exact), else 0 (use the IEEE division)
 };
 
 // fixed-point scale of the deposit, derived on the device from max(m*mask)
@@ -39,8 +40,9 @@ __device__ __forceinline__ QScale qscale_from_mmax(const unsigned *mmax_bits, fl
   float mmax = __uint_as_float(*mmax_bits);
   int e = 0;
   if (mmax > 0.f) frexpf(mmax, &e);  // mmax = f * 2^e, f in [0.5, 1)
-  // every contribution c <= mmax < 2^e, so c * 2^(32-e) < 2^32
-  int S = 32 - e;
+  // every contribution c <= mmax < 2^e, so c * 2^(26-e) < 2^26 and the sum of one warp's
+  // 32 quanta fits a 32-bit reduction
+  int S = 26 - e;
   int S1 = S / 2, S2 = S - S1;
   QScale q;
   q.qs1 = ldexpf(1.f, S1);
@@ -57,9 +59,9 @@ __device__ __forceinline__ uint32_t row_begin(const uint32_t *start, const uint3
 // when some corner lands on the grid, else the discard bucket G+1.
 __device__ __forceinline__ uint32_t row_key(const GridParams &g, int ix, int iy, int iz) {
   if (g.D == 3) {
-    return (uint32_t)(wrap_idx(iz, g.G) * g.G + wrap_idx(iy, g.G));
+    return (uint32_t)(fwrap(iz, g.G) * g.G + fwrap(iy, g.G));
   }
-  if (g.periodic) return (uint32_t)wrap_idx(iy, g.G);
+  if (g.periodic) return (uint32_t)fwrap(iy, g.G);
   bool on = (ix >= -1) && (ix < g.G) && (iy >= -1) && (iy < g.G);
   return on ? (uint32_t)(iy + 1) : (uint32_t)(g.G + 1);
 }
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(256) keys_hist_aos_kernel(float *__restrict__ 
     float w;
     bool ok = true;
 #pragma unroll
-    for (int d = 0; d < D; ++d) ok &= cic_axis(x[d], g.half_ext, g.h, i0[d], w);
+    for (int d = 0; d < D; ++d) ok &= cic_axis(x[d], g.half_ext, g.h, i0[d], w, g.inv_h);
     if (!ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
     k = row_key(g, i0[0], i0[1], i0[2]);
     mm = __fmul_rn(mass[i], mask[i]);
@@ -263,6 +265,136 @@ __global__ void __launch_bounds__(256) scatter_sorted_kernel(const float4 *__res
 }
 
 // ---------------------------------------------------------------------------------
+// Deposit geometry: row blocks of RY x RZ grid rows and their work items.
+// ---------------------------------------------------------------------------------
+struct DepositArgs {
+  GridParams g;
+  int RY, RZ;
+  FftShape fsh;   // complex length M = G/2 (MODE 1)
+  int twmul;      // table stride for the length-M transform
+  int Lt;         // twiddle table length
+  int nblk;       // row blocks
+  uint32_t chunk; // bodies per work item
+  FastDiv fdG, fdRR, fdRY;
+};
+
+// Calls f(first, last) for every contiguous run of sorted bodies that can touch row
+// block b: base rows [y0-1, y0+RY-1] x [z0-1, z0+RZ-1] (periodic wrap), or base rows
+// y0-1 .. y0+RY-1 <-> keys y0 .. y0+RY for the isolated 2D grid.
+template <int D, class F>
+__device__ __forceinline__ void block_segments(const DepositArgs &a, int b, const uint32_t *start,
+                                               const uint32_t *tile_off, F f) {
+  const int G = a.g.G, RY = a.RY, RZ = a.RZ;
+  const int nyb = G / RY;
+  const int y0 = (b % nyb) * RY;
+  const int z0 = (D == 3) ? (b / nyb) * RZ : 0;
+  auto add = [&](uint32_t r0, uint32_t r1) {
+    uint32_t lo = row_begin(start, tile_off, r0), hi = row_begin(start, tile_off, r1);
+    if (hi > lo) f(lo, hi);
+  };
+  auto ylist = [&](uint32_t rb) {
+    if (RY < G) {
+      int yh = wrap_idx(y0 - 1, G);
+      add(rb + yh, rb + yh + 1);
+      add(rb + y0, rb + y0 + RY);
+    } else {
+      add(rb, rb + G);
+    }
+  };
+  if (D == 3) {
+    const int nz = (RZ < G) ? RZ + 1 : G;
+    const int zs = (RZ < G) ? z0 - 1 : 0;
+    for (int t = 0; t < nz; ++t) ylist((uint32_t)wrap_idx(zs + t, G) * G);
+  } else if (a.g.periodic) {
+    ylist(0);
+  } else {
+    add(y0, y0 + RY + 1);
+  }
+}
+
+// Work items: every row block gets max(1, ceil(bodies / chunk)) items. One CTA records each
+// block's body segments (seg_tab[b] = {first body, prefix count} pairs), scans the per-block
+// item counts into item_off (nblk + 1 entries) and slot_off (partial-tile slots of blocks
+// split over more than one item), and lists the block of every item in item_blk.
+constexpr int MAXSEGB = 32;  // segments per row block: 2 * (RZ + 1) with RZ <= 15
+
+template <int D>
+__global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__restrict__ start,
+                                                            const uint32_t *__restrict__ tile_off, DepositArgs a,
+                                                            uint32_t *__restrict__ nch, uint32_t *__restrict__ item_off,
+                                                            uint32_t *__restrict__ slot_off,
+                                                            uint2 *__restrict__ seg_tab, uint32_t *__restrict__ item_blk,
+                                                            unsigned *__restrict__ err) {
+  __shared__ uint32_t wsum[2][32];
+  const int nb = a.nblk, tid = threadIdx.x, nt = blockDim.x;
+  for (int b = tid; b < nb; b += nt) {
+    uint32_t cnt = 0;
+    int ns = 0;
+    uint2 *tab = seg_tab + (size_t)b * (MAXSEGB + 1);
+    block_segments<D>(a, b, start, tile_off, [&](uint32_t lo, uint32_t hi) {
+      if (ns < MAXSEGB) {
+        tab[1 + ns] = make_uint2(lo, cnt);
+        ++ns;
+        cnt += hi - lo;
+      } else {
+        set_err(err, AUGUR_ERRBIT_RANGE);
+      }
+    });
+    tab[0] = make_uint2((uint32_t)ns, cnt);
+    nch[b] = cnt == 0 ? 1u : (cnt + a.chunk - 1) / a.chunk;
+  }
+  __syncthreads();
+  const int per = (nb + nt - 1) / nt;
+  const int b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
+  uint32_t si = 0, ss = 0;
+  for (int b = b0; b < b1; ++b) {
+    uint32_t c = nch[b];
+    si += c;
+    ss += c > 1 ? c : 0;
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  uint32_t ii = si, is = ss;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t u = __shfl_up_sync(0xffffffffu, ii, o), v = __shfl_up_sync(0xffffffffu, is, o);
+    if (lane >= o) {
+      ii += u;
+      is += v;
+    }
+  }
+  if (lane == 31) {
+    wsum[0][warp] = ii;
+    wsum[1][warp] = is;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t x = lane < (nt >> 5) ? wsum[0][lane] : 0u, y = lane < (nt >> 5) ? wsum[1][lane] : 0u;
+    uint32_t xi = x, yi = y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t u = __shfl_up_sync(0xffffffffu, xi, o), v = __shfl_up_sync(0xffffffffu, yi, o);
+      if (lane >= o) {
+        xi += u;
+        yi += v;
+      }
+    }
+    wsum[0][lane] = xi - x;
+    wsum[1][lane] = yi - y;
+  }
+  __syncthreads();
+  uint32_t ri = wsum[0][warp] + ii - si, rs = wsum[1][warp] + is - ss;
+  for (int b = b0; b < b1; ++b) {
+    uint32_t c = nch[b];
+    item_off[b] = ri;
+    slot_off[b] = rs;
+    for (uint32_t j = 0; j < c; ++j) item_blk[ri + j] = (uint32_t)b;
+    ri += c;
+    rs += c > 1 ? c : 0;
+  }
+  if (tid == nt - 1) item_off[nb] = ri;
+}
+
+// ---------------------------------------------------------------------------------
 // K2 (+K3a): deterministic CIC deposit of one block of grid rows, accumulated in
 // 64-bit fixed point in shared memory with warp-aggregated atomics (integer sums are
 // associative, so the result is independent of body order and scheduling), then
@@ -272,171 +404,193 @@ __global__ void __launch_bounds__(256) scatter_sorted_kernel(const float4 *__res
 // Block = RY consecutive y rows x RZ consecutive z planes (2D: RZ = 1). Bodies that
 // touch the block are those whose base row lies in [y0-1, y0+RY-1] x [z0-1, z0+RZ-1];
 // with the state sorted by base row they form at most 2*(RZ+1) contiguous segments.
+// A block with more than `chunk` bodies is split over several CTAs (work items); each
+// writes its fixed-point tile to scratch and the CTA that finishes last (counter +
+// threadfence, no waiting) adds the others' tiles before converting.
 // ---------------------------------------------------------------------------------
-struct DepositArgs {
-  GridParams g;
-  int RY, RZ;
-  FftShape fsh;   // complex length M = G/2 (MODE 1)
-  int twmul;      // table stride for the length-M transform
-  int Lt;         // twiddle table length
-};
-
 template <int D, int MODE>
 __global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__ pos4,
-                                                      const uint32_t *__restrict__ start,
-                                                      const uint32_t *__restrict__ tile_off,
                                                       const unsigned *__restrict__ mmax_bits, DepositArgs a,
                                                       const float2 *__restrict__ twg, float *__restrict__ rho_out,
-                                                      float2 *__restrict__ spec_out, unsigned *__restrict__ err) {
+                                                      float2 *__restrict__ spec_out, unsigned *__restrict__ err,
+                                                      const uint32_t *__restrict__ item_off,
+                                                      const uint32_t *__restrict__ slot_off,
+                                                      const uint2 *__restrict__ seg_tab,
+                                                      const uint32_t *__restrict__ item_blk,
+                                                      unsigned long long *__restrict__ scratch,
+                                                      unsigned *__restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ long long s_beg[MAXSEG];
-  __shared__ long long s_pre[MAXSEG + 1];
-  __shared__ int s_nseg;
+  __shared__ long long s_beg[MAXSEGB];
+  __shared__ long long s_pre[MAXSEGB + 1];
+  __shared__ int s_nseg, s_last;
 
   const GridParams &g = a.g;
   const int G = g.G, RY = a.RY, RZ = a.RZ, RR = RY * RZ;
-  const int nyb = G / RY;
-  const int y0 = (blockIdx.x % nyb) * RY;
-  const int z0 = (D == 3) ? (blockIdx.x / nyb) * RZ : 0;
   const int tid = threadIdx.x, nt = blockDim.x;
+  const uint32_t item = blockIdx.x;
+  if (item >= item_off[a.nblk]) return;  // uniform across the CTA
+  const int blk = (int)item_blk[item];
+  const uint32_t part = item - item_off[blk];
+  const uint32_t nparts = item_off[blk + 1] - item_off[blk];
+  const int nyb = G / RY;
+  const int y0 = (blk % nyb) * RY;
+  const int z0 = (D == 3) ? (blk / nyb) * RZ : 0;
   const int RS = G + 2;  // fp32 row stride (keeps complex rows 8-byte aligned and padded)
 
+  // [accumulator / transform scratch: RR*(G+2)*8 bytes][fp32 rows: RR*RS*4][twiddles]
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem);
-  float *rows = reinterpret_cast<float *>(smem + (size_t)RR * G * 8);
-  float2 *tw = reinterpret_cast<float2 *>(smem + (size_t)RR * G * 8 + (size_t)RR * RS * 4);
+  float *rows = reinterpret_cast<float *>(smem + (size_t)RR * RS * 8);
+  float2 *tw = reinterpret_cast<float2 *>(smem + (size_t)RR * RS * 8 + (size_t)RR * RS * 4);
 
+  const uint2 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
+  if (tid <= MAXSEGB) {
+    uint2 t = tab[tid];
+    if (tid == 0) {
+      s_nseg = (int)t.x;
+      s_pre[t.x] = t.y;  // total
+    } else if (tid - 1 < (int)tab[0].x) {
+      s_beg[tid - 1] = t.x;
+      s_pre[tid - 1] = t.y;
+    }
+  }
   for (int e = tid; e < RR * G; e += nt) acc[e] = 0ull;
   if (MODE == 1)
     for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
-
-  if (tid == 0) {
-    int ns = 0;
-    auto add = [&](uint32_t r0, uint32_t r1) {  // rows [r0, r1)
-      uint32_t b = row_begin(start, tile_off, r0), e = row_begin(start, tile_off, r1);
-      if (e > b && ns < MAXSEG) {
-        s_beg[ns] = b;
-        s_pre[ns + 1] = (long long)(e - b);
-        ++ns;
-      }
-    };
-    if (D == 3) {
-      const int nz = (RZ < G) ? RZ + 1 : G;
-      const int zs = (RZ < G) ? z0 - 1 : 0;
-      for (int t = 0; t < nz; ++t) {
-        int iz = wrap_idx(zs + t, G);
-        uint32_t rb = (uint32_t)iz * G;
-        if (RY < G) {
-          int yh = wrap_idx(y0 - 1, G);
-          add(rb + yh, rb + yh + 1);
-          add(rb + y0, rb + y0 + RY);
-        } else {
-          add(rb, rb + G);
-        }
-      }
-    } else if (g.periodic) {
-      if (RY < G) {
-        int yh = wrap_idx(y0 - 1, G);
-        add(yh, yh + 1);
-        add(y0, y0 + RY);
-      } else {
-        add(0, G);
-      }
-    } else {
-      // isolated 2D: base rows y0-1 .. y0+RY-1  <->  keys y0 .. y0+RY
-      add(y0, y0 + RY + 1);
-    }
-    s_pre[0] = 0;
-    for (int s = 0; s < ns; ++s) s_pre[s + 1] += s_pre[s];
-    s_nseg = ns;
-  }
   __syncthreads();
 
   const QScale qs = qscale_from_mmax(mmax_bits, g.inv_hD);
   const int nseg = s_nseg;
-  const long long total = s_pre[nseg];
+  const long long f_lo = (long long)part * a.chunk;
+  const long long f_hi = min(s_pre[nseg], f_lo + (long long)a.chunk);
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  int wseg = 0;  // segment of the warp's first body; only moves forward
 
-  for (long long f0 = (long long)warp * 32; f0 < total; f0 += (long long)nwarp * 32) {
+  for (long long f0 = f_lo + (long long)warp * 32; f0 < f_hi; f0 += (long long)nwarp * 32) {
     const long long f = f0 + lane;
-    const bool valid = f < total;
+    const bool valid = f < f_hi;
+    while (wseg + 1 < nseg && s_pre[wseg + 1] <= f0) ++wseg;
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) {
-      int lo = 0, hi = nseg - 1;  // find s with s_pre[s] <= f < s_pre[s+1]
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (s_pre[mid] <= f) lo = mid;
-        else hi = mid - 1;
-      }
-      p = pos4[s_beg[lo] + (f - s_pre[lo])];
+      int sg = wseg;
+      while (sg + 1 < nseg && s_pre[sg + 1] <= f) ++sg;
+      p = pos4[s_beg[sg] + (f - s_pre[sg])];
     }
     int ix = 0, iy = 0, iz = 0;
     float wx = 0.f, wy = 0.f, wz = 0.f;
-    bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx) & cic_axis(p.y, g.half_ext, g.h, iy, wy);
-    if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz);
+    bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, iy, wy, g.inv_h);
+    if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz, g.inv_h);
     if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
     const bool live = valid && ok && p.w > 0.f;
+    // x corners of this body: cells bx and bx1 of a row (periodic wrap or grid bounds)
+    int bx = ix, bx1 = ix + 1;
+    bool inx0 = true, inx1 = true;
+    if (g.periodic) {
+      bx = fwrap(ix, G);
+      bx1 = (bx + 1 == G) ? 0 : bx + 1;
+    } else {
+      inx0 = (ix >= 0) && (ix < G);
+      inx1 = (ix + 1 >= 0) && (ix + 1 < G);
+    }
+    const float wx0 = axis_w(wx, 0), wx1 = axis_w(wx, 1);
 #pragma unroll
-    for (int ox = 0; ox < 2; ++ox) {
+    for (int oy = 0; oy < 2; ++oy) {
 #pragma unroll
-      for (int oy = 0; oy < 2; ++oy) {
-#pragma unroll
-        for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
-          unsigned target = 0xffffffffu;
-          uint32_t q = 0;
-          if (live) {
-            int cx = ix + ox, cy = iy + oy, cz = iz + oz;
-            bool in;
-            if (g.periodic) {
-              cx = wrap_idx(cx, G);
-              cy = wrap_idx(cy, G);
-              int ly = cy - y0;
-              if (ly < 0) ly += G;
-              int lz = 0;
-              if (D == 3) {
-                cz = wrap_idx(cz, G);
-                lz = cz - z0;
-                if (lz < 0) lz += G;
-              }
-              in = (ly < RY) && (lz < RZ);
-              if (in) target = (unsigned)((lz * RY + ly) * G + cx);
-            } else {
-              int ly = cy - y0;
-              in = (cx >= 0) && (cx < G) && (ly >= 0) && (ly < RY);
-              if (in) target = (unsigned)(ly * G + cx);
+      for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
+        // key identifies the (row, x pair) of this (y, z) corner pair; both x corners share it
+        unsigned key = 0xffffffffu;
+        uint32_t q0 = 0, q1 = 0;
+        int rowbase = 0;
+        if (live) {
+          bool in;
+          if (g.periodic) {
+            int cy = fwrap(iy + oy, G);
+            int ly = cy - y0;
+            if (ly < 0) ly += G;
+            int lz = 0;
+            if (D == 3) {
+              int cz = fwrap(iz + oz, G);
+              lz = cz - z0;
+              if (lz < 0) lz += G;
             }
-            if (in) {
-              float wt = __fmul_rn(axis_w(wx, ox), axis_w(wy, oy));
-              if (D == 3) wt = __fmul_rn(wt, axis_w(wz, oz));
-              float c = __fmul_rn(wt, p.w);
-              q = __float2uint_rz(__fmul_rn(__fmul_rn(c, qs.qs1), qs.qs2));
+            in = (ly < RY) && (lz < RZ);
+            rowbase = (lz * RY + ly) * G;
+            if (in) key = (unsigned)(rowbase + bx);
+          } else {
+            int ly = iy + oy - y0;
+            in = (ly >= 0) && (ly < RY) && (inx0 || inx1);
+            rowbase = ly * G;
+            if (in) key = (unsigned)(ly * (G + 1) + ix + 1);
+          }
+          if (in) {
+            // weight order of the reference: ((w_x * w_y) * w_z) * m
+            const float wyt = axis_w(wy, oy), wzt = axis_w(wz, oz);
+            float w0 = __fmul_rn(wx0, wyt), w1 = __fmul_rn(wx1, wyt);
+            if (D == 3) {
+              w0 = __fmul_rn(w0, wzt);
+              w1 = __fmul_rn(w1, wzt);
+            }
+            if (inx0) q0 = __float2uint_rz(__fmul_rn(__fmul_rn(__fmul_rn(w0, p.w), qs.qs1), qs.qs2));
+            if (inx1) q1 = __float2uint_rz(__fmul_rn(__fmul_rn(__fmul_rn(w1, p.w), qs.qs1), qs.qs2));
+          }
+        }
+        unsigned long long *r0 = nullptr, *r1 = nullptr;
+        if (key != 0xffffffffu) {
+          if (g.periodic) {
+            r0 = &acc[rowbase + bx];
+            r1 = &acc[rowbase + bx1];
+          } else {
+            r0 = inx0 ? &acc[rowbase + ix] : nullptr;
+            r1 = inx1 ? &acc[rowbase + ix + 1] : nullptr;
+          }
+        }
+        // warp aggregation only when neighbouring lanes share a key
+        unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+        bool dup = (lane > 0) && (key != 0xffffffffu) && (prev == key);
+        if (__any_sync(0xffffffffu, dup)) {
+          unsigned peers = __match_any_sync(0xffffffffu, key);
+          if (key != 0xffffffffu) {
+            uint32_t s0 = __reduce_add_sync(peers, q0);
+            uint32_t s1 = __reduce_add_sync(peers, q1);
+            if (lane == __ffs(peers) - 1) {
+              if (r0 && s0) atomicAdd(r0, (unsigned long long)s0);
+              if (r1 && s1) atomicAdd(r1, (unsigned long long)s1);
             }
           }
-          // warp aggregation only when neighbouring lanes share a target
-          unsigned prev = __shfl_up_sync(0xffffffffu, target, 1);
-          bool dup = (lane > 0) && (target != 0xffffffffu) && (prev == target);
-          if (__any_sync(0xffffffffu, dup)) {
-            unsigned peers = __match_any_sync(0xffffffffu, target);
-            if (target != 0xffffffffu) {
-              uint32_t slo = __reduce_add_sync(peers, q & 0xffffu);
-              uint32_t shi = __reduce_add_sync(peers, q >> 16);
-              if (lane == __ffs(peers) - 1)
-                atomicAdd(&acc[target], ((unsigned long long)shi << 16) + (unsigned long long)slo);
-            }
-          } else if (target != 0xffffffffu && q) {
-            atomicAdd(&acc[target], (unsigned long long)q);
-          }
+        } else if (key != 0xffffffffu) {
+          if (r0 && q0) atomicAdd(r0, (unsigned long long)q0);
+          if (r1 && q1) atomicAdd(r1, (unsigned long long)q1);
         }
       }
     }
   }
   __syncthreads();
 
+  if (nparts > 1) {
+    // publish this part's tile, then let the last part to arrive sum all of them
+    const size_t tile = (size_t)RR * G;
+    unsigned long long *mine = scratch + (size_t)(slot_off[blk] + part) * tile;
+    for (int e = tid; e < RR * G; e += nt) mine[e] = acc[e];
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = (atomicAdd(&counters[blk], 1u) == nparts - 1) ? 1 : 0;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (uint32_t o = 0; o < nparts; ++o) {
+      if (o == part) continue;
+      const unsigned long long *other = scratch + (size_t)(slot_off[blk] + o) * tile;
+      for (int e = tid; e < RR * G; e += nt) acc[e] += __ldcg(&other[e]);
+    }
+    if (tid == 0) counters[blk] = 0u;
+    __syncthreads();
+  }
+
   // fixed point -> float32 density rows
   for (int e = tid; e < RR * G; e += nt) {
-    int rr = e / G, x = e - rr * G;
+    int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
     float v = __fmul_rn(__ull2float_rn(acc[e]), qs.outscale);
     if (MODE == 0) {
-      int zz = rr / RY, yy = rr - zz * RY;
+      int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
       size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
       rho_out[row * G + x] = v;
     } else {
@@ -446,16 +600,23 @@ __global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__
   if (MODE == 0) return;
   __syncthreads();
 
-  // R2C along x: rows viewed as M = G/2 complex values, stride RS/2 = M+1
+  // R2C along x: rows viewed as M = G/2 complex values, stride RS/2 = M+1; the transform
+  // reads them, ping-pongs through the (now free) accumulator area and lands back on them
   const int M = G / 2, MS = M + 1;
-  float2 *A = reinterpret_cast<float2 *>(rows);
-  float2 *B = reinterpret_cast<float2 *>(smem);  // acc area is free now
-  float2 *Z = fft_smem(a.fsh, A, B, RR, 1, MS, tw, a.twmul, false);
+  float2 *Z = reinterpret_cast<float2 *>(rows);
+  float2 *TA = reinterpret_cast<float2 *>(smem);
+  float2 *TB = TA + (size_t)RR * MS;
+  {
+    const float2 *src = Z;
+    auto ld = [&](int b, int e) -> float2 { return src[b * MS + e]; };
+    auto st = [&](int b, int e, float2 v) { Z[b * MS + e] = v; };
+    AUGUR_FFT_IO(M, 0, RR, ld, st, TA, TB, MS, tw, a.twmul, false);
+  }
   // post-process X_k = (Z_k + conj Z_{M-k})/2 - i/2 W^k (Z_k - conj Z_{M-k}), k = 0..M
   const int tstep = a.Lt / G;
   const size_t plane = (size_t)(D == 3 ? G : 1) * G;  // rows per kx plane
   for (int e = tid; e < (M + 1) * RR; e += nt) {
-    int kx = e / RR, rr = e - kx * RR;
+    int kx = (int)fdiv(e, a.fdRR), rr = e - kx * RR;
     float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
     float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
     float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
@@ -463,7 +624,7 @@ __global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__
     float2 w = tw[kx * tstep];
     float2 t = cmul(w, od);
     float2 X = make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
-    int zz = rr / RY, yy = rr - zz * RY;
+    int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
     size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
     spec_out[(size_t)kx * plane + row] = X;
   }
@@ -478,6 +639,7 @@ struct RowsArgs {
   int L, Lin, nin, nout, RB, Lt;
   FftShape fsh;  // complex length L/2
   int twmul;     // for the length L/2 transform
+  FastDiv fdL, fdRB;
 };
 
 __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__ in, RowsArgs a,
@@ -486,23 +648,29 @@ __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__
   const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB;
   float2 *A = reinterpret_cast<float2 *>(smem);
   float2 *B = A + (size_t)RB * MS;
-  float2 *tw = B + (size_t)RB * MS;
+  float2 *C = B + (size_t)RB * MS;
+  float2 *tw = C + (size_t)RB * MS;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = blockIdx.x * RB;
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
   float *Af = reinterpret_cast<float *>(A);
   for (int e = tid; e < RB * L; e += nt) {
-    int rr = e / L, x = e - rr * L;
+    int rr = (int)fdiv(e, a.fdL), x = e - rr * L;
     int r = r0 + rr;
     float v = 0.f;
     if (r < a.nin && x < a.Lin) v = in[(size_t)r * a.Lin + x];
     Af[rr * 2 * MS + x] = v;
   }
   __syncthreads();
-  float2 *Z = fft_smem(a.fsh, A, B, RB, 1, MS, tw, a.twmul, false);
+  float2 *Z = A;
+  {
+    auto ld = [&](int b, int e) -> float2 { return A[b * MS + e]; };
+    auto st = [&](int b, int e, float2 v) { Z[b * MS + e] = v; };
+    AUGUR_FFT_IO(M, 0, RB, ld, st, B, C, MS, tw, a.twmul, false);
+  }
   const int tstep = a.Lt / L;
   for (int e = tid; e < (M + 1) * RB; e += nt) {
-    int kx = e / RB, rr = e - kx * RB;
+    int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
     int r = r0 + rr;
     if (r >= a.nout) continue;
     float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
@@ -514,9 +682,10 @@ __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__
   }
 }
 
-// In-place FFT of contiguous complex rows of length L (rows = lines along y).
+// In-place FFT of contiguous complex rows of length L (rows = lines along y): the first
+// stage reads HBM, the last writes HBM, the stages between go through shared memory.
 __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data, int64_t nrows, int RB, int L,
-                                                       FftShape fsh, int twmul, int Lt,
+                                                       FastDiv fdL, int twmul, int Lt,
                                                        const float2 *__restrict__ twg, int inverse) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int LS = L + 1;
@@ -527,16 +696,22 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data
   const int64_t r0 = (int64_t)blockIdx.x * RB;
   const int nr = (int)min((int64_t)RB, nrows - r0);
   for (int e = tid; e < Lt; e += nt) tw[e] = twg[e];
-  for (int e = tid; e < nr * L; e += nt) {
-    int rr = e / L, x = e - rr * L;
-    A[rr * LS + x] = data[(r0 + rr) * L + x];
+  float2 *base = data + r0 * L;
+  if (L <= 16) {  // single-stage lengths: stage through shared memory (in place)
+    for (int e = tid; e < nr * L; e += nt) {
+      int rr = (int)fdiv(e, fdL), x = e - rr * L;
+      B[rr * LS + x] = base[(size_t)rr * L + x];
+    }
+    __syncthreads();
+    auto ld = [&](int b, int e) -> float2 { return B[b * LS + e]; };
+    auto st = [&](int b, int e, float2 v) { base[(size_t)b * L + e] = v; };
+    AUGUR_FFT_IO(L, 0, nr, ld, st, A, A, LS, tw, twmul, inverse != 0);
+    return;
   }
   __syncthreads();
-  float2 *R = fft_smem(fsh, A, B, nr, 1, LS, tw, twmul, inverse != 0);
-  for (int e = tid; e < nr * L; e += nt) {
-    int rr = e / L, x = e - rr * L;
-    data[(r0 + rr) * L + x] = R[rr * LS + x];
-  }
+  auto ld = [&](int b, int e) -> float2 { return base[(size_t)b * L + e]; };
+  auto st = [&](int b, int e, float2 v) { base[(size_t)b * L + e] = v; };
+  AUGUR_FFT_IO(L, 0, nr, ld, st, A, B, LS, tw, twmul, inverse != 0);
 }
 
 // ---------------------------------------------------------------------------------
@@ -553,11 +728,12 @@ struct GreenArgs {
   float gfac;      // -4 pi G_newton / G^3
 };
 
+template <int TY>
 __global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
                                                           const float2 *__restrict__ twg,
                                                           float2 *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int G = a.G, TY = a.TY, M = G / 2;
+  const int G = a.G, M = G / 2;
   const int nyt = G / TY;
   const int kx = blockIdx.x / nyt;
   const int y0 = (blockIdx.x % nyt) * TY;
@@ -569,51 +745,37 @@ __global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restri
   float2 *C = B + (size_t)G * TY;
   float2 *tw = C + (size_t)G * TY;
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
-  const float2 *src = spec + (size_t)kx * plane;
-  for (int e = tid; e < G * TY; e += nt) {
-    int z = e / TY, t = e - z * TY;
-    B[e] = src[(size_t)z * G + y0 + t];
-  }
   __syncthreads();
-  float2 *R = fft_smem(a.fsh, B, C, TY, TY, 1, tw, 1, false);
-  // Green's function
+  const float2 *src = spec + (size_t)kx * plane + y0;
   const float mx = (float)kx;
-  for (int e = tid; e < G * TY; e += nt) {
-    int z = e / TY, t = e - z * TY;
-    int ky = y0 + t;
-    float my = (float)(ky < M ? ky : ky - G);
-    float mz = (float)(z < M ? z : z - G);
-    float m2 = mx * mx + my * my + mz * mz;
-    float2 v = R[e];
-    float f = (m2 > 0.f) ? a.gfac / (a.kfund * a.kfund * m2) : 0.f;
-    P[e] = make_float2(v.x * f, v.y * f);
+  // forward z transform from HBM; the last stage applies the Green's function on its way to P
+  {
+    auto ld = [&](int b, int e) -> float2 { return src[(size_t)e * G + b]; };
+    auto st = [&](int b, int e, float2 v) {
+      const int ky = y0 + b;
+      const float my = (float)(ky < M ? ky : ky - G);
+      const float mz = (float)(e < M ? e : e - G);
+      const float m2 = mx * mx + my * my + mz * mz;
+      const float f = (m2 > 0.f) ? a.gfac / (a.kfund * a.kfund * m2) : 0.f;
+      P[e * TY + b] = make_float2(v.x * f, v.y * f);
+    };
+    AUGUR_FFT_IO(G, TY, TY, ld, st, B, C, 0, tw, 1, false);
   }
-  __syncthreads();
   for (int c = 0; c < a.ncomp; ++c) {
-    for (int e = tid; e < G * TY; e += nt) {
-      int z = e / TY, t = e - z * TY;
-      float2 ph = P[e];
-      float2 o;
-      if (c == 3) {
-        o = ph;
-      } else {
-        int idx = (c == 0) ? kx : (c == 1 ? y0 + t : z);
-        float m;
-        if (c == 0) m = (idx == M) ? 0.f : (float)idx;
-        else m = (idx == M) ? 0.f : (float)(idx < M ? idx : idx - G);
-        float k = a.kfund * m;
-        o = make_float2(k * ph.y, -k * ph.x);  // -i k phi
-      }
-      B[e] = o;
-    }
-    __syncthreads();
-    float2 *Q = fft_smem(a.fsh, B, C, TY, TY, 1, tw, 1, true);
-    float2 *dst = out + c * cstride + (size_t)kx * plane;
-    for (int e = tid; e < G * TY; e += nt) {
-      int z = e / TY, t = e - z * TY;
-      dst[(size_t)z * G + y0 + t] = Q[e];
-    }
-    __syncthreads();
+    float2 *dst = out + c * cstride + (size_t)kx * plane + y0;
+    // inverse z transform of -i k_c phi_k (or phi_k for c == 3), the derivative applied on load
+    auto ld = [&](int b, int e) -> float2 {
+      const float2 ph = P[e * TY + b];
+      if (c == 3) return ph;
+      const int idx = (c == 0) ? kx : (c == 1 ? y0 + b : e);
+      float m;
+      if (c == 0) m = (idx == M) ? 0.f : (float)idx;
+      else m = (idx == M) ? 0.f : (float)(idx < M ? idx : idx - G);
+      const float k = a.kfund * m;
+      return make_float2(k * ph.y, -k * ph.x);  // -i k phi
+    };
+    auto st = [&](int b, int e, float2 v) { dst[(size_t)e * G + b] = v; };
+    AUGUR_FFT_IO(G, TY, TY, ld, st, B, C, 0, tw, 1, true);
   }
 }
 
@@ -634,6 +796,7 @@ struct C2RArgs {
   float scale;
   FftShape fsh;  // complex length L/2
   int twmul;
+  FastDiv fdRB, fdM, fdL;
 };
 
 template <bool OUT4>
@@ -654,38 +817,32 @@ __global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict_
   for (int c = 0; c < nc; ++c) {
     const float2 *src = in + c * cstride;
     for (int e = tid; e < (M + 1) * RB; e += nt) {
-      int kx = e / RB, rr = e - kx * RB;
+      int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
       int r = r0 + rr;
       float2 v = (r < a.nrows) ? src[(size_t)kx * a.nrows + r] : make_float2(0.f, 0.f);
       if (kx == 0 || kx == M) v.y = 0.f;  // imaginary part of DC and Nyquist is ignored
       X[rr * MS + kx] = v;
     }
     __syncthreads();
-    // pre-process: E_k = X_k + conj X_{M-k} ; O_k = (X_k - conj X_{M-k}) W^{-k} ; Z_k = E_k + i O_k
-    for (int e = tid; e < M * RB; e += nt) {
-      int rr = e / M, k = e - rr * M;
-      float2 xk = X[rr * MS + k];
-      float2 xc = cconj(X[rr * MS + (M - k)]);
-      float2 E = cadd(xk, xc);
-      float2 w = tw[k * tstep];
-      float2 O = cmul(csub(xk, xc), cconj(w));
-      Y[rr * MS + k] = make_float2(E.x - O.y, E.y + O.x);
-    }
-    __syncthreads();
-    float2 *R = fft_smem(a.fsh, Y, X, RB, 1, MS, tw, a.twmul, true);
+    // inverse transform whose first stage computes the pre-process on load:
+    // E_k = X_k + conj X_{M-k} ; O_k = (X_k - conj X_{M-k}) W^{-k} ; Z_k = E_k + i O_k
     float *dst = res + (size_t)c * RB * L;
-    for (int e = tid; e < RB * M; e += nt) {
-      int rr = e / M, k = e - rr * M;
-      float2 v = R[rr * MS + k];
-      dst[rr * L + 2 * k] = v.x * a.scale;
-      dst[rr * L + 2 * k + 1] = v.y * a.scale;
-    }
-    __syncthreads();
+    auto ld = [&](int b, int k) -> float2 {
+      float2 xk = X[b * MS + k];
+      float2 xc = cconj(X[b * MS + (M - k)]);
+      float2 E = cadd(xk, xc);
+      float2 O = cmul(csub(xk, xc), cconj(tw[k * tstep]));
+      return make_float2(E.x - O.y, E.y + O.x);
+    };
+    auto st = [&](int b, int k, float2 v) {
+      *reinterpret_cast<float2 *>(&dst[b * L + 2 * k]) = make_float2(v.x * a.scale, v.y * a.scale);
+    };
+    AUGUR_FFT_IO(M, 0, RB, ld, st, X, Y, MS, tw, a.twmul, true);
   }
   if (OUT4) {
     float4 *o4 = reinterpret_cast<float4 *>(out);
     for (int e = tid; e < RB * L; e += nt) {
-      int rr = e / L, x = e - rr * L;
+      int rr = (int)fdiv(e, a.fdL), x = e - rr * L;
       int r = r0 + rr;
       if (r >= a.nrows) continue;
       float4 v;
@@ -697,7 +854,7 @@ __global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict_
     }
   } else {
     for (int e = tid; e < RB * L; e += nt) {
-      int rr = e / L, x = e - rr * L;
+      int rr = (int)fdiv(e, a.fdL), x = e - rr * L;
       int r = r0 + rr;
       if (r >= a.nkeep || x >= a.Lkeep) continue;
       out[(size_t)r * a.Lkeep + x] = res[rr * L + x];
@@ -763,32 +920,41 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
   }
   int ix = 0, iy = 0, iz = 0;
   float wx = 0.f, wy = 0.f, wz = 0.f;
-  bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx) & cic_axis(p.y, g.half_ext, g.h, iy, wy);
-  if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz);
+  bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, iy, wy, g.inv_h);
+  if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz, g.inv_h);
   if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
   float ax = 0.f, ay = 0.f, az = 0.f, ph = 0.f;
   if (valid && ok) {
+    int cxs[2], cys[2], czs[2] = {0, 0};
+    bool inx[2] = {true, true}, iny[2] = {true, true};
+    if (g.periodic) {
+      cxs[0] = fwrap(ix, G);
+      cxs[1] = cxs[0] + 1 == G ? 0 : cxs[0] + 1;
+      cys[0] = fwrap(iy, G);
+      cys[1] = cys[0] + 1 == G ? 0 : cys[0] + 1;
+      if (D == 3) {
+        czs[0] = fwrap(iz, G);
+        czs[1] = czs[0] + 1 == G ? 0 : czs[0] + 1;
+      }
+    } else {
+#pragma unroll
+      for (int o = 0; o < 2; ++o) {
+        inx[o] = (ix + o >= 0) && (ix + o < G);
+        iny[o] = (iy + o >= 0) && (iy + o < G);
+        cxs[o] = min(max(ix + o, 0), G - 1);
+        cys[o] = min(max(iy + o, 0), G - 1);
+      }
+    }
 #pragma unroll
     for (int ox = 0; ox < 2; ++ox) {
 #pragma unroll
       for (int oy = 0; oy < 2; ++oy) {
 #pragma unroll
         for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
-          int cx = ix + ox, cy = iy + oy, cz = iz + oz;
           float wt = __fmul_rn(axis_w(wx, ox), axis_w(wy, oy));
           if (D == 3) wt = __fmul_rn(wt, axis_w(wz, oz));
-          bool in = true;
-          if (g.periodic) {
-            cx = wrap_idx(cx, G);
-            cy = wrap_idx(cy, G);
-            if (D == 3) cz = wrap_idx(cz, G);
-          } else {
-            in = (cx >= 0) && (cx < G) && (cy >= 0) && (cy < G);
-            cx = min(max(cx, 0), G - 1);
-            cy = min(max(cy, 0), G - 1);
-            if (!in) wt = 0.f;
-          }
-          size_t cell = (D == 3) ? ((size_t)cz * G + cy) * G + cx : (size_t)cy * G + cx;
+          if (!(inx[ox] && iny[oy])) wt = 0.f;
+          size_t cell = (D == 3) ? ((size_t)czs[oz] * G + cys[oy]) * G + cxs[ox] : (size_t)cys[oy] * G + cxs[ox];
           float4 f = __ldg(&F4[cell]);
           ax = __fadd_rn(ax, __fmul_rn(f.x, wt));
           ay = __fadd_rn(ay, __fmul_rn(f.y, wt));
@@ -844,8 +1010,8 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
         p.z = xs[2];
         int jx = 0, jy = 0, jz = 0;
         float u;
-        bool ok2 = cic_axis(p.x, g.half_ext, g.h, jx, u) & cic_axis(p.y, g.half_ext, g.h, jy, u);
-        if (D == 3) ok2 &= cic_axis(p.z, g.half_ext, g.h, jz, u);
+        bool ok2 = cic_axis(p.x, g.half_ext, g.h, jx, u, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, jy, u, g.inv_h);
+        if (D == 3) ok2 &= cic_axis(p.z, g.half_ext, g.h, jz, u, g.inv_h);
         if (!ok2) set_err(err, AUGUR_ERRBIT_NONFINITE);
         k = row_key(g, jx, jy, jz);
       }
@@ -895,7 +1061,7 @@ __global__ void cell_index_kernel(const float *__restrict__ pos, int64_t n, Grid
   for (int d = 0; d < D; ++d) {
     int c;
     float f;
-    if (!cic_axis(pos[i * D + d], g.half_ext, g.h, c, f)) set_err(err, AUGUR_ERRBIT_NONFINITE);
+    if (!cic_axis(pos[i * D + d], g.half_ext, g.h, c, f, g.inv_h)) set_err(err, AUGUR_ERRBIT_NONFINITE);
     i0[i * D + d] = c;
     w[i * D + d] = f;
   }

@@ -188,6 +188,16 @@ class PMPlan:
     def run_steps(self, k: int) -> None:
         self._call("augur_pm_run_steps", int(k))
 
+    STAGES = ("sort", "deposit_r2c", "fft_y_fwd", "fft_z_green", "fft_y_inv", "c2r", "gather_kd")
+
+    def run_profile(self, k: int) -> dict:
+        """Mean device ms per stage over k steps of an active run (CUDA events between stages)."""
+        out = (C.c_float * len(self.STAGES))()
+        with torch.cuda.device(self.device):
+            rc = self.lib.augur_pm_run_profile(self._p, int(k), out, len(self.STAGES), _stream(self.device))
+        _lib.check(rc, "augur_pm_run_profile")
+        return dict(zip(self.STAGES, [float(x) for x in out]))
+
     def run_end(self, pos, vel, want_acc: bool = False):
         acc = torch.empty_like(pos) if want_acc else None
         self._call("augur_pm_run_end", pos.data_ptr(), vel.data_ptr(), _ptr(acc))

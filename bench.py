@@ -1,0 +1,329 @@
+"""Benchmark of the plain-PM gravity step at 3M bodies on a 256^3 periodic grid.
+
+One step = one leapfrog step of the whole scene on the GPU: re-sort by grid row, CIC
+deposit + x R2C, y/z FFTs with the Green's function and spectral gradient, C2R, gather +
+kick-drift. Inputs (3M-body Plummer sphere, a=0.05, in a unit periodic box; seeded,
+synthetic) are resident in HBM before the timed region; the per-step working set
+(~1.5 GB of traffic over ~0.8 GB of buffers) is larger than the 129 MB L2, so no flush.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). Under torchrun each rank runs an independent replica
+(scenes are independent; the PM step has no inter-GPU exchange) and value is the
+whole-job rate over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+import torch
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "body-steps/s at 3M bodies: CNN-corrected vs plain PM at equal force error"
+STAGES = ("sort", "deposit_r2c", "fft_y_fwd", "fft_z_green", "fft_y_inv", "c2r", "gather_kd")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(n: int, G: int) -> dict:
+    """Algorithmic bytes per launch of each stage (unpadded, FP32). C = half spectrum."""
+    C = 8 * (G // 2 + 1) * G * G
+    G3 = G ** 3
+    return {
+        "sort": 0,  # implementation overhead, not algorithmic
+        "deposit_r2c": 16 * n + C,  # read bodies (x, y, z, m), write the x-transformed spectrum
+        "fft_y_fwd": 2 * C,
+        "fft_z_green": 4 * C,  # read 1 spectrum, write 3 gradient spectra
+        "fft_y_inv": 6 * C,
+        "c2r": 3 * C + 12 * G3,
+        "gather_kd": 12 * G3 + 64 * n,  # force grid + body state read and written
+    }
+
+
+def step_bytes(n: int, G: int) -> int:
+    """Algorithmic bytes of one PM step: 48 N + 32 G^3 + 8 C."""
+    C = 8 * (G // 2 + 1) * G * G
+    return 48 * n + 32 * G ** 3 + 8 * C
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.proc = None
+        try:
+            uuid = str(torch.cuda.get_device_properties(device).uuid)
+            ident = uuid if uuid.startswith("GPU-") else f"GPU-{uuid}"
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={ident}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            return None
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+                pw.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        load = [s for s, p in zip(sm, pw) if p > 0.3 * max(pw)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_inputs(n: int, seed: int, scene: str = "plummer"):
+    from augur_gb300 import scenes
+
+    return scenes.make_scene(scene, n, seed=seed)
+
+
+def cpu_baseline_run(n, G, dt, budget_s=20.0):
+    """The reference-idiom torch CPU step (oracle/pm_torch_cpu.py) on this host's cores,
+    on the full workload for as many steps as fit in the budget (at least one)."""
+    from oracle.pm_torch_cpu import TorchCPUPM
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    pos, vel, mass = make_inputs(n, 9100)
+    p, v, m = torch.from_numpy(pos), torch.from_numpy(vel), torch.from_numpy(mass)
+    sim = TorchCPUPM(G)
+    sim.begin(p, v, m, dt)
+    t0 = time.perf_counter()
+    sim.step(p, v, m, dt)
+    t1 = time.perf_counter() - t0
+    steps = 1
+    extra = max(0, min(9, int(budget_s / max(t1, 1e-3)) - 1))
+    t0 = time.perf_counter()
+    for _ in range(extra):
+        sim.step(p, v, m, dt)
+    if extra:
+        t1 = (t1 + time.perf_counter() - t0)
+        steps += extra
+    return {"value": n * steps / t1, "unit": "body-steps/s", "cores": torch.get_num_threads(), "kind": "port",
+            "sample": f"{steps} step(s) of the full {n}-body / {G}^3 workload (oracle/pm_torch_cpu.py, float32)",
+            "s_per_step": t1 / steps}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    n, G = args.bodies, args.grid
+    cb = cpu_baseline_run(n, G, args.dt, budget_s=max(5.0, 60.0 / max(1, args.steps)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "body-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["s_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config(args):
+    kind = {"plummer": "Plummer sphere (a=0.05)", "uniform": "uniform box", "clumpy": "64-clump scene",
+            "disk": "exponential disk", "flyby": "Plummer flyby"}[args.scene]
+    return {"workload": f"plain PM step, {args.bodies}-body {kind} in a unit periodic box, "
+                        f"{args.grid}^3 FP32 grid, leapfrog dt={args.dt}",
+            "bodies": args.bodies, "grid": args.grid, "scene": args.scene, "seed": 9100, "dt": args.dt,
+            "l2": "per-step traffic ~1.5 GB over ~0.8 GB of buffers > 129 MB L2; no flush"}
+
+
+def accuracy(plan, pos_d, mass_d, n, G, ns=4096, seed=9100):
+    """Plain-PM force error vs the FP64 periodic (Ewald) direct sum on ns sampled bodies."""
+    from augur_gb300 import direct_sum_fp64
+
+    ones = torch.ones(n, device=pos_d.device)
+    acc = plan.force(pos_d, mass_d, ones).double()
+    idx = torch.from_numpy(np.random.default_rng(seed).choice(n, ns, replace=False)).to(pos_d.device)
+    src = pos_d.double()
+    truth = direct_sum_fp64(src[idx].contiguous(), src, mass_d.double(), eps=1.0 / 256, box=1.0,
+                            target_index=idx.contiguous())
+    a = acc[idx]
+    d = (a - truth).norm(dim=1)
+    rms = truth.norm(dim=1).pow(2).mean().sqrt()
+    e = (d / rms).cpu().numpy()
+    return {"vs": "FP64 periodic direct sum (min-image + Ewald), eps=1/256, 4096 sampled bodies",
+            "rel_rms": float((d.pow(2).mean().sqrt() / rms).item()),
+            "median_norm_by_rms": float(np.sort(e)[(len(e) - 1) // 2]), "p90_norm_by_rms": float(np.quantile(e, 0.9))}
+
+
+def run_ours(args, world, rank, local):
+    from augur_gb300 import PMPlan
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    n, G, dt = args.bodies, args.grid, args.dt
+    pos, vel, mass = make_inputs(n, 9100 + rank, args.scene)
+    pos_d, vel_d, mass_d = (torch.from_numpy(x).to(dev) for x in (pos, vel, mass))
+    ones = torch.ones(n, device=dev)
+    plan = PMPlan(3, G, n, "periodic", 1.0, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    p, v = pos_d.clone(), vel_d.clone()
+    plan.run_begin(p, v, mass_d, ones, dt=dt)
+    plan.run_steps(args.warmup)
+    torch.cuda.synchronize(dev)
+
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    plan.run_steps(args.steps)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    launches = plan.last_launches
+    plan.check()
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms = ms_total / args.steps
+
+    stages = plan.run_profile(20)
+    plan.run_end(p, v)
+    torch.cuda.synchronize(dev)
+
+    # end to end through the public API: a velocity-Verlet step on caller tensors that live in
+    # pinned host memory, copied in and out every step
+    h_pos, h_vel = torch.from_numpy(pos).pin_memory(), torch.from_numpy(vel).pin_memory()
+    h_acc = torch.zeros_like(h_pos).pin_memory()
+    d_pos, d_vel, d_acc = torch.empty_like(pos_d), torch.empty_like(vel_d), torch.empty_like(pos_d)
+    k_e2e = max(3, min(args.steps, 50))
+
+    def e2e_step(first):
+        d_pos.copy_(h_pos, non_blocking=True)
+        d_vel.copy_(h_vel, non_blocking=True)
+        d_acc.copy_(h_acc, non_blocking=True)
+        plan.step(d_pos, d_vel, d_acc, mass_d, ones, dt=dt, have_acc=not first)
+        h_pos.copy_(d_pos, non_blocking=True)
+        h_vel.copy_(d_vel, non_blocking=True)
+        h_acc.copy_(d_acc, non_blocking=True)
+
+    e2e_step(True)
+    e2e_step(False)
+    torch.cuda.synchronize(dev)
+    e0.record(st)
+    for _ in range(k_e2e):
+        e2e_step(False)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / k_e2e
+
+    acc_info = None
+    if not args.no_accuracy and rank == 0:
+        acc_info = accuracy(plan, pos_d, mass_d, n, G)
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    sb = stage_bytes(n, G)
+    dom = max(stages, key=stages.get)
+    ach = sb[dom] / (stages[dom] * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "ncu_traffic.json"
+    if tp.exists():
+        tr = json.loads(tp.read_text()).get(f"{n}x{G}", {})
+        traffic = tr.get(dom)
+    B = step_bytes(n, G)
+    cb = cpu_baseline_run(n, G, dt) if (world == 1 and not args.no_cpu) else None
+    line = {
+        "metric": METRIC, "value": world * n / (ms * 1e-3), "unit": "body-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(args),
+        "form": "plain PM",
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": sb[dom]},
+        "step_roofline": {"bound": "hbm", "algorithmic_bytes": B, "achieved": B / (ms * 1e-3) / 1e9, "peak": peak,
+                          "unit": "GB/s", "frac": B / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind},
+        "stages_ms": stages,
+        "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "body-steps/s", "h2d_bytes_per_step": 36 * n,
+                "d2h_bytes_per_step": 36 * n, "api": "augur_gb300.PMPlan.step (augur_pm_step) on pinned host buffers"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "accuracy": acc_info,
+        "cpu_baseline": None if cb is None else {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--bodies", type=int, default=3_000_000)
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scene", default="plummer", choices=("plummer", "uniform", "clumpy", "disk", "flyby"))
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

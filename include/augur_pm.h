@@ -149,6 +149,16 @@ int augur_pm_run_steps(augur_pm_plan *plan, int k, void *stream);
 int augur_pm_run_end(augur_pm_plan *plan, float *pos, float *vel, float *acc_out,
                      void *stream);
 
+/*
+ * Measurement aid: k merged steps like augur_pm_run_steps with a CUDA event recorded on
+ * the stream between the stages of each step; synchronises after every step and writes
+ * the mean device milliseconds per stage to stage_ms[0..AUGUR_PM_NSTAGE-1] in the order
+ * sort (scan + scatter), deposit + x R2C, forward y FFT, z FFT + Green + gradient +
+ * inverse z, inverse y FFT, x C2R, gather + kick-drift + keys. Requires an active run.
+ */
+#define AUGUR_PM_NSTAGE 7
+int augur_pm_run_profile(augur_pm_plan *plan, int k, float *stage_ms, int nstage, void *stream);
+
 /* Kernel launches issued by the last plan call (for launch accounting). */
 int64_t augur_pm_last_launches(const augur_pm_plan *plan);
 

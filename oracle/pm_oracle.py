@@ -66,10 +66,11 @@ def corner_weight(w, o, D):
 # ----------------------------------------------------------------------------------
 def qscale(mm):
     """Fixed-point scale of the deterministic deposit: contributions c <= max(m) < 2^e
-    are quantised as trunc(c * 2^(32-e)) into uint32 and summed exactly in uint64."""
+    are quantised as trunc(c * 2^(26-e)) (< 2^26, so 32 of them fit a 32-bit warp sum)
+    and summed exactly in uint64."""
     mmax = float(np.max(mm)) if mm.size else 0.0
     e = math.frexp(mmax)[1] if mmax > 0 else 0
-    S = 32 - e
+    S = 26 - e
     S1 = int(S / 2)
     return F32(math.ldexp(1.0, S1)), F32(math.ldexp(1.0, S - S1)), S
 
