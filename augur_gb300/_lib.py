@@ -38,6 +38,16 @@ SIGNATURES = {
     "augur_pm_check": (_i32, [_vp, _vp]),
     "augur_direct_sum_fp64": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp]),
     "augur_energy_fp64": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp]),
+    # include/augur_cnn.h
+    "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp]),
+    "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
+    "augur_cnn_wgrad": (_i32, [_i32, _vp, _vp, _i32, _i32, _vp, _i32, _vp, _vp]),
+    "augur_cnn_prep_weights": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "augur_cnn_input": (_i32, [_vp, _vp, _i64, _f32, _f32, _vp, _vp]),
+    "augur_cnn_adamw": (_i32, [_vp, _vp, _vp, _vp, _i32, _f32, _f32, _f32, _f32, _f32, _i32, _vp]),
+    "augur_cnn_gather_transpose": (_i32, [_vp, _vp, _i64, _i32, _f64, _vp, _vp]),
+    "augur_cnn_pack_dout": (_i32, [_vp, _i64, _f32, _vp, _vp]),
+    "augur_cnn_gelu_bwd": (_i32, [_vp, _vp, _i64, _vp, _vp]),
 }
 
 _lib = None

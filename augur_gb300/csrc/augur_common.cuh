@@ -15,6 +15,7 @@
 
 #define AUGUR_ERRBIT_NONFINITE 1u
 #define AUGUR_ERRBIT_RANGE 2u
+#define AUGUR_ERRBIT_TIMEOUT 4u
 
 namespace augur {
 

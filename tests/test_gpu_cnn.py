@@ -1,0 +1,148 @@
+"""GPU CNN kernels (tcgen05 forward and data gradient, CUDA-core input layer and weight
+gradients) against a plain PyTorch fp32 CPU reference of the same network.
+
+Tolerances: forward 5e-3 relative RMS (the reference rounds activations to BF16 at the same
+points as the kernels; what remains is FP32 accumulation order); gradients 3e-2 relative RMS
+and cosine > 0.999 against fp32 autograd (the kernels keep activations and dz in BF16)."""
+import math
+
+import numpy as np
+import pytest
+import torch
+import torch.nn.functional as F
+
+from augur_gb300.cnn import GridCNN
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda:0")
+
+
+def bf(t):
+    return t.to(torch.bfloat16).float()
+
+
+def rel_rms(a, b):
+    return float(((a - b) ** 2).sum().sqrt() / (b ** 2).sum().sqrt().clamp_min(1e-30))
+
+
+def torch_weights(net: GridCNN):
+    """(n, c, 3, 3, 3) torch-layout weights from the flat parameters (fp32, CPU)."""
+    out = {}
+    for name in ["in", "mid0", "mid1", "mid2", "out"]:
+        w = net.view[f"w_{name}"].detach().cpu()
+        out[name] = (w.view(w.shape[0], 3, 3, 3, w.shape[2]).permute(0, 4, 1, 2, 3).contiguous(),
+                     net.view[f"b_{name}"].detach().cpu().clone())
+    return out
+
+
+def ref_forward(x, tw, out_scale, round_bf16=True):
+    r = bf if round_bf16 else (lambda t: t)
+    z0 = F.conv3d(x, tw["in"][0], tw["in"][1], padding=1)
+    h = r(F.gelu(z0))
+    for i in range(3):
+        wmid = bf(tw[f"mid{i}"][0]) if round_bf16 else tw[f"mid{i}"][0]
+        z = F.conv3d(h, wmid, tw[f"mid{i}"][1], padding=1)
+        h = r(h + F.gelu(z))
+    wout = bf(tw["out"][0]) if round_bf16 else tw["out"][0]
+    return out_scale * F.conv3d(h, wout, tw["out"][1], padding=1)
+
+
+def make_net(seed=1, out_nonzero=True):
+    net = GridCNN(DEV, seed=seed, out_scale=0.7)
+    if out_nonzero:
+        g = torch.Generator().manual_seed(seed + 100)
+        net.view["w_out"].copy_((torch.rand(3, 27, 32, generator=g) * 2 - 1) / math.sqrt(27 * 32))
+        net.view["b_out"].copy_(torch.rand(3, generator=g) - 0.5)
+        for i in range(3):
+            net.view[f"b_mid{i}"].copy_((torch.rand(32, generator=g) - 0.5) * 0.2)
+        net.prepare()
+    return net
+
+
+def inputs(B, G, seed=0):
+    g = torch.Generator().manual_seed(seed)
+    x = bf(torch.randn(B, 2, G, G, G, generator=g))
+    xd = x.permute(0, 2, 3, 4, 1).contiguous().to(DEV).to(torch.bfloat16).view(-1)
+    return x, xd
+
+
+@pytest.mark.parametrize("B,G", [(1, 16), (2, 24), (1, 130)])
+def test_forward_matches_torch(B, G):
+    net = make_net()
+    x, xd = inputs(B, G)
+    field = torch.zeros(B * G ** 3 * 4, device=DEV)
+    net.forward(xd, B, G, field)
+    net.check()
+    ours = field.view(B, G, G, G, 4)[..., :3].permute(0, 4, 1, 2, 3).cpu()
+    ref = ref_forward(x, torch_weights(net), net.out_scale)
+    assert rel_rms(ours, ref) < 5e-3
+    assert float(field.view(-1, 4)[:, 3].abs().max()) == 0.0
+
+
+def test_forward_adds_into_the_force_grid():
+    net = make_net(seed=3)
+    B, G = 1, 16
+    x, xd = inputs(B, G, seed=5)
+    base = torch.randn(B * G ** 3 * 4, device=DEV)
+    field = base.clone()
+    net.forward(xd, B, G, field)
+    field0 = torch.zeros_like(base)
+    net.forward(xd, B, G, field0)
+    assert torch.allclose(field, base + field0, atol=1e-5)
+
+
+def test_zero_initialised_output_layer_gives_zero_correction():
+    net = GridCNN(DEV, seed=7)
+    B, G = 1, 16
+    _, xd = inputs(B, G)
+    field = torch.zeros(B * G ** 3 * 4, device=DEV)
+    net.forward(xd, B, G, field)
+    assert float(field.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("B,G", [(1, 16), (2, 20)])
+def test_backward_matches_torch_autograd(B, G):
+    net = make_net(seed=11)
+    x, xd = inputs(B, G, seed=2)
+    gfield = torch.randn(B, G, G, G, 3, generator=torch.Generator().manual_seed(9))
+    field = torch.zeros(B * G ** 3 * 4, device=DEV)
+    net.forward(xd, B, G, field, train=True)
+    d4 = torch.zeros(B, G, G, G, 4)
+    d4[..., :3] = gfield
+    net.backward(d4.view(-1).to(DEV), B, G)
+    net.check()
+    # reference: fp32 autograd with the same (bf16-rounded where the kernels round) weights
+    tw = torch_weights(net)
+    params = {k: (v[0].clone().requires_grad_(True), v[1].clone().requires_grad_(True)) for k, v in tw.items()}
+    for k in ["mid0", "mid1", "mid2", "out"]:
+        params[k] = (bf(params[k][0].detach()).requires_grad_(True), params[k][1])
+    y = ref_forward(x, params, net.out_scale, round_bf16=False)
+    (y * gfield.permute(0, 4, 1, 2, 3)).sum().backward()
+    for name in ["in", "mid0", "mid1", "mid2", "out"]:
+        gw = net.gview[f"w_{name}"].detach().cpu()
+        gw = gw.view(gw.shape[0], 3, 3, 3, gw.shape[2]).permute(0, 4, 1, 2, 3)
+        rw = params[name][0].grad
+        cos = float((gw * rw).sum() / (gw.norm() * rw.norm()))
+        assert rel_rms(gw, rw) < 3e-2, name
+        assert cos > 0.999, name
+        gb = net.gview[f"b_{name}"].detach().cpu()
+        assert rel_rms(gb, params[name][1].grad) < 3e-2, name
+
+
+def test_gather_transpose_is_the_adjoint_of_the_gather():
+    from augur_gb300 import PMPlan, scenes
+
+    G, n = 16, 2000
+    pos, _, _ = scenes.make_scene("uniform", n, seed=3)
+    plan = PMPlan(3, G, n, "periodic", 1.0)
+    p = torch.from_numpy(pos).to(DEV)
+    Fg = torch.randn(G, G, G, 4, device=DEV)
+    Fg[..., 3] = 0
+    a, _ = plan.gather(Fg.contiguous(), p)
+    v = torch.randn(n, 3, device=DEV)
+    out = torch.zeros(G ** 3 * 4, device=DEV)
+    net = GridCNN(DEV)
+    net._call("augur_cnn_gather_transpose", p.data_ptr(), v.data_ptr(), n, G, 1.0, out.data_ptr())
+    lhs = float((a.double() * v.double()).sum())
+    rhs = float((Fg.view(-1).double() * out.double()).sum())
+    assert abs(lhs - rhs) < 1e-4 * abs(lhs)
