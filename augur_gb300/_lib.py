@@ -34,6 +34,11 @@ SIGNATURES = {
     "augur_pm_run_steps": (_i32, [_vp, _i32, _vp]),
     "augur_pm_run_end": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "augur_pm_run_profile": (_i32, [_vp, _i32, _vp, _i32, _vp]),
+    "augur_pm_run_load": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),
+    "augur_pm_run_grid": (_i32, [_vp, _vp, _i32, _vp]),
+    "augur_pm_force_grid": (_vp, [_vp]),
+    "augur_pm_run_kick": (_i32, [_vp, _f32, _i32, _vp, _vp, _f32, _vp]),
+    "augur_pm_run_unload": (_i32, [_vp, _vp, _vp, _vp]),
     "augur_pm_last_launches": (_i64, [_vp]),
     "augur_pm_check": (_i32, [_vp, _vp]),
     "augur_direct_sum_fp64": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp]),

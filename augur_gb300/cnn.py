@@ -124,8 +124,8 @@ class GridCNN:
         return ws
 
     def input(self, rho: torch.Tensor, force4: torch.Tensor) -> torch.Tensor:
-        """x (nvox, 2) bf16 = (rho_scale * rho, phi_scale * phi) from the density grid and the
-        potential lane of the PM force grid."""
+        """x (nvox, 2) bf16 = (log(1 + rho_scale * rho), phi_scale * phi) from the density grid and
+        the potential lane of the PM force grid."""
         nv = rho.numel()
         x = torch.empty(nv * 2, dtype=torch.bfloat16, device=self.device)
         self._call("augur_cnn_input", rho.data_ptr(), force4.data_ptr(), nv, self.rho_scale, self.phi_scale,
@@ -186,6 +186,14 @@ class GridCNN:
                    parts, gi.data_ptr())
         self.gview["w_in"].copy_(gi[:W * 27 * 2].view(W, 27, 2))
         self.gview["b_in"].copy_(gi[W * 27 * 2:])
+
+    def clip_grad_norm(self, max_norm: float = 1.0) -> float:
+        """Scale the gradients to norm <= max_norm (the reference clips at 1.0,
+        scripts/train_scatter_field.py:228); returns the norm before clipping."""
+        gn = float(self.grads.norm())
+        if gn > max_norm and math.isfinite(gn):
+            self.grads.mul_(max_norm / gn)
+        return gn
 
     def adamw(self, lr: float = 3e-4, betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.01) -> None:
         self.adam_step += 1

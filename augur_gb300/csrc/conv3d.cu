@@ -355,14 +355,15 @@ __global__ void prep_weights_kernel(const float *__restrict__ w, int Nreal, int 
   out[((size_t)(k / 8) * N + n) * 8 + (k % 8)] = __float2bfloat16_rn(v);
 }
 
-// x (B, G^3, 2) bf16 from the density and potential grids: x0 = rho_scale * rho,
-// x1 = phi_scale * phi (phi read from lane 3 of the PM force grid).
+// x (B, G^3, 2) bf16 from the density and potential grids: x0 = log(1 + rho_scale * rho)
+// (the density spans four decades in a Plummer core), x1 = phi_scale * phi (phi read from
+// lane 3 of the PM force grid).
 __global__ void cnn_input_kernel(const float *__restrict__ rho, const float4 *__restrict__ F, int64_t nv,
                                  float rho_scale, float phi_scale, bf16 *__restrict__ x) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   *reinterpret_cast<__nv_bfloat162 *>(x + v * 2) =
-      __floats2bfloat162_rn(rho_scale * rho[v], phi_scale * F[v].w);
+      __floats2bfloat162_rn(log1pf(fmaxf(rho_scale * rho[v], 0.f)), phi_scale * F[v].w);
 }
 
 // AdamW (decoupled weight decay), fp32 master weights.

@@ -44,6 +44,9 @@ struct augur_pm_plan {
   int64_t run_n;
   float run_dt;
   int run_active;
+  int ncomp_last;  // components of the last force grid (3, or 4 with the potential)
+  double *epart;   // energy tap partials
+  unsigned epart_n;
   int64_t launches;
   size_t bytes;
 };
@@ -317,10 +320,12 @@ int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream
   return AUGUR_OK;
 }
 
-// sorted bodies -> F4 (the grid force of the plan's mode)
-int grid_force(augur_pm_plan *p, int ncomp, cudaStream_t st) {
+// sorted bodies -> F4 (the grid force of the plan's mode); rho_out (optional) also
+// receives the density grid
+int grid_force(augur_pm_plan *p, int ncomp, cudaStream_t st, float *rho_out = nullptr) {
+  p->ncomp_last = ncomp;
   if (p->mode == AUGUR_MODE_PERIODIC) {
-    int rc = launch_deposit<3, 1>(p, nullptr, p->spec, st);
+    int rc = rho_out ? launch_deposit<3, 2>(p, rho_out, p->spec, st) : launch_deposit<3, 1>(p, nullptr, p->spec, st);
     if (rc) return rc;
     return periodic_tail(p, ncomp, p->F4, st);
   }
@@ -335,6 +340,8 @@ GatherArgs gather_args(const augur_pm_plan *p, float kick, float dt, int drift) 
   a.kick = kick;
   a.dt = dt;
   a.drift = drift;
+  a.esync = 0.f;
+  a.epart = nullptr;
   return a;
 }
 
@@ -384,7 +391,7 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
   void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
                   p->F4, p->real_tmp, p->phi2d, p->rho2d, p->dep_nch, p->dep_item_off, p->dep_slot_off,
-                  p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab};
+                  p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -520,6 +527,7 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   }
   // dynamic shared memory opt-in
   cudaFuncSetAttribute(deposit_kernel<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
+  cudaFuncSetAttribute(deposit_kernel<3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
   cudaFuncSetAttribute(deposit_kernel<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
   cudaFuncSetAttribute(deposit_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
   cudaFuncSetAttribute(fft_z_green_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
@@ -650,14 +658,81 @@ int augur_pm_step(augur_pm_plan *p, float *pos, float *vel, float *acc, const fl
   return AUGUR_OK;
 }
 
-static int run_gather(augur_pm_plan *p, float kick, int drift, float *acc_out, cudaStream_t st) {
+static int run_gather(augur_pm_plan *p, float kick, int drift, float *acc_out, cudaStream_t st,
+                      double *energy_out = nullptr, float esync = 0.f) {
   const int64_t n = p->run_n;
   if (n == 0) return AUGUR_OK;
   GatherArgs a = gather_args(p, kick, p->run_dt, drift);
-  gather_kernel<3, MODE_KD><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a,
-                                                                acc_out, nullptr, nullptr, p->key, p->slot,
-                                                                p->row_count, p->d_err);
+  const unsigned nb = blocks_for(n, 256);
+  if (energy_out) {
+    if (!p->epart || p->epart_n < nb) {
+      if (p->epart) cudaFree(p->epart);
+      p->epart = nullptr;
+      if (cudaMalloc(&p->epart, sizeof(double) * 2 * nb) != cudaSuccess) return AUGUR_ENOMEM;
+      p->epart_n = nb;
+    }
+    a.epart = p->epart;
+    a.esync = esync;
+  }
+  gather_kernel<3, MODE_KD><<<nb, 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc_out, nullptr,
+                                                 nullptr, p->key, p->slot, p->row_count, p->d_err);
   AUGUR_LAUNCH_CHECK(p);
+  if (energy_out) {
+    energy_fold_kernel<<<1, 32, 0, st>>>(p->epart, (int)nb, energy_out);
+    AUGUR_LAUNCH_CHECK(p);
+  }
+  return AUGUR_OK;
+}
+
+int augur_pm_run_load(augur_pm_plan *p, const float *pos, const float *vel, const float *mass, const float *mask,
+                      int64_t n, float dt, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
+  if (n > 0 && (!pos || !vel || !mass || !mask)) return AUGUR_EINVAL;
+  p->launches = 0;
+  p->run_n = n;
+  p->run_dt = dt;
+  rc = sort_from_aos(p, const_cast<float *>(pos), vel, nullptr, mass, mask, n, false, 0.f, S(stream));
+  if (rc) return rc;
+  p->run_active = 2;  // loaded and sorted; the next grid call needs no re-sort
+  return AUGUR_OK;
+}
+
+int augur_pm_run_grid(augur_pm_plan *p, float *rho_out, int with_phi, void *stream) {
+  if (!p || !p->run_active) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  if (p->run_active == 1) {
+    int rc = resort(p, st);
+    if (rc) return rc;
+  }
+  p->run_active = 3;  // grid computed; the kick comes next
+  return grid_force(p, with_phi ? 4 : 3, st, rho_out);
+}
+
+float *augur_pm_force_grid(augur_pm_plan *p) { return p ? reinterpret_cast<float *>(p->F4) : nullptr; }
+
+int augur_pm_run_kick(augur_pm_plan *p, float kick, int drift, float *acc_out, double *energy_out, float esync,
+                      void *stream) {
+  if (!p || p->run_active != 3) return AUGUR_EINVAL;
+  if (energy_out && p->ncomp_last < 4) return AUGUR_EINVAL;  // the potential lane is needed
+  p->launches = 0;
+  int rc = run_gather(p, kick, drift, acc_out, S(stream), energy_out, esync);
+  p->run_active = 1;  // a re-sort is due before the next grid
+  return rc;
+}
+
+int augur_pm_run_unload(augur_pm_plan *p, float *pos, float *vel, void *stream) {
+  if (!p || !p->run_active) return AUGUR_EINVAL;
+  if (p->run_n > 0 && (!pos || !vel)) return AUGUR_EINVAL;
+  p->launches = 0;
+  const int64_t n = p->run_n;
+  if (n > 0) {
+    unsort_kernel<3><<<blocks_for(n, 256), 256, 0, S(stream)>>>(p->pos4[p->cur], p->vel4[p->cur], n, pos, vel);
+    AUGUR_LAUNCH_CHECK(p);
+  }
+  p->run_active = 0;
   return AUGUR_OK;
 }
 
@@ -682,7 +757,7 @@ int augur_pm_run_begin(augur_pm_plan *p, const float *pos, const float *vel, con
 }
 
 int augur_pm_run_steps(augur_pm_plan *p, int k, void *stream) {
-  if (!p || !p->run_active || k < 0) return AUGUR_EINVAL;
+  if (!p || p->run_active != 1 || k < 0) return AUGUR_EINVAL;
   cudaStream_t st = S(stream);
   p->launches = 0;
   for (int s = 0; s < k; ++s) {
@@ -697,7 +772,7 @@ int augur_pm_run_steps(augur_pm_plan *p, int k, void *stream) {
 }
 
 int augur_pm_run_profile(augur_pm_plan *p, int k, float *stage_ms, int nstage, void *stream) {
-  if (!p || !p->run_active || k < 1 || !stage_ms || nstage < AUGUR_PM_NSTAGE) return AUGUR_EINVAL;
+  if (!p || p->run_active != 1 || k < 1 || !stage_ms || nstage < AUGUR_PM_NSTAGE) return AUGUR_EINVAL;
   if (p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
   cudaStream_t st = S(stream);
   cudaEvent_t ev[AUGUR_PM_NSTAGE + 1];
@@ -770,7 +845,7 @@ int augur_pm_run_profile(augur_pm_plan *p, int k, float *stage_ms, int nstage, v
 }
 
 int augur_pm_run_end(augur_pm_plan *p, float *pos, float *vel, float *acc_out, void *stream) {
-  if (!p || !p->run_active) return AUGUR_EINVAL;
+  if (!p || p->run_active != 1) return AUGUR_EINVAL;
   if (p->run_n > 0 && (!pos || !vel)) return AUGUR_EINVAL;
   cudaStream_t st = S(stream);
   p->launches = 0;

@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
 // 64-bit fixed point in shared memory with warp-aggregated atomics (integer sums are
 // associative, so the result is independent of body order and scheduling), then
 // either written as float32 density rows (MODE 0) or transformed along x in shared
-// memory (R2C, MODE 1) and written to the half spectrum spec[kx][row].
+// memory (R2C, MODE 1) and written to the half spectrum spec[kx][row] (MODE 2: both).
 //
 // Block = RY consecutive y rows x RZ consecutive z planes (2D: RZ = 1). Bodies that
 // touch the block are those whose base row lies in [y0-1, y0+RY-1] x [z0-1, z0+RZ-1];
@@ -585,17 +585,16 @@ __global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__
     __syncthreads();
   }
 
-  // fixed point -> float32 density rows
+  // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
   for (int e = tid; e < RR * G; e += nt) {
     int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
     float v = __fmul_rn(__ull2float_rn(acc[e]), qs.outscale);
-    if (MODE == 0) {
+    if (MODE != 1) {
       int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
       size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
       rho_out[row * G + x] = v;
-    } else {
-      rows[rr * RS + x] = v;
     }
+    if (MODE != 0) rows[rr * RS + x] = v;
   }
   if (MODE == 0) return;
   __syncthreads();
@@ -900,6 +899,8 @@ struct GatherArgs {
   GridParams g;
   float kick, dt;
   int drift;
+  float esync;    // energy tap: kinetic energy at v + esync * a (the synchronised velocity)
+  double *epart;  // energy tap: per-block (kinetic, potential) partial sums, or null
 };
 
 template <int D, int MODE>
@@ -992,6 +993,33 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
       ax = __fmul_rn(ax, mk);
       ay = __fmul_rn(ay, mk);
       az = __fmul_rn(az, mk);
+    }
+    if (a.epart) {  // energy at the synchronised time (uniform branch: every thread takes part)
+      double ek = 0.0, ep = 0.0;
+      if (valid) {
+        const float vx = v.x + a.esync * ax, vy = v.y + a.esync * ay, vz = v.z + a.esync * az;
+        ek = 0.5 * (double)p.w * (double)(vx * vx + vy * vy + vz * vz);
+        ep = 0.5 * (double)p.w * (double)(ph * mk);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ek += __shfl_xor_sync(0xffffffffu, ek, o);
+        ep += __shfl_xor_sync(0xffffffffu, ep, o);
+      }
+      __shared__ double sred[2][8];
+      const int w = threadIdx.x >> 5;
+      if ((threadIdx.x & 31) == 0) {
+        sred[0][w] = ek;
+        sred[1][w] = ep;
+      }
+      __syncthreads();
+      if (threadIdx.x < 2) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sred[threadIdx.x][q];
+        a.epart[(size_t)blockIdx.x * 2 + threadIdx.x] = t;
+      }
+    }
+    if (valid) {
       v.x = __fadd_rn(v.x, __fmul_rn(a.kick, ax));
       v.y = __fadd_rn(v.y, __fmul_rn(a.kick, ay));
       if (D == 3) v.z = __fadd_rn(v.z, __fmul_rn(a.kick, az));
@@ -1031,6 +1059,20 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
       }
     }
   }
+}
+
+// Fixed-order sum of the gather's per-block energy partials: out[0] kinetic, out[1] potential.
+__global__ void energy_fold_kernel(const double *__restrict__ epart, int nblk, double *__restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= 2) return;
+  double s = 0.0, c = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    const double v = epart[(size_t)b * 2 + q];
+    const double t = s + v;
+    c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+    s = t;
+  }
+  out[q] = s + c;
 }
 
 // Write the sorted state back to the caller's order (end of a run).

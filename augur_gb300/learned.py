@@ -1,0 +1,246 @@
+"""CNN-corrected PM: training data, training, evaluation, and the corrected leapfrog step.
+
+The correction is learned from pairs the method generates itself: for each seeded snapshot
+the plain-PM force and the FP64 (Ewald-periodic) direct-sum force at sampled bodies; the
+label is their difference (the role of the reference's truth-vs-model force error,
+scripts/pm_baseline_force_error.py:88-92, turned into a training target). The network sees
+the CIC density and PM potential grids and outputs a 3-channel correction field that is
+CIC-gathered at the bodies and added to the PM force.
+
+Plain PM is the fallback and the judge: FallbackMonitor reverts a scene to plain PM when its
+relative energy drift exceeds 5% or the predicted correction grows beyond a fraction of the
+PM force (the reference's energy drift diagnostic, scripts/scatter_field.py:759-765, :874).
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import scenes
+from .cnn import GridCNN
+from .pm import PMPlan, direct_sum_fp64
+
+
+# ---------------------------------------------------------------------------------------------
+# data
+# ---------------------------------------------------------------------------------------------
+def make_snapshot(plan: PMPlan, net: GridCNN, kind: str, n: int, seed: int, n_targets: int = 8192,
+                  eps: float = 1.0 / 256, box: float = 1.0) -> dict:
+    """One labelled snapshot on plan's grid: CNN input x (bf16), target positions and the
+    (FP64 direct sum - PM) force at them."""
+    dev = plan.device
+    pos, _, mass = scenes.make_scene(kind, n, seed=seed, box=box)
+    p = torch.from_numpy(pos).to(dev)
+    m = torch.from_numpy(mass).to(dev)
+    ones = torch.ones(n, device=dev)
+    rho = plan.deposit(p, m, ones)
+    F4 = plan.poisson(rho)
+    rng = np.random.default_rng(seed + 17)
+    idx = torch.from_numpy(rng.choice(n, size=min(n_targets, n), replace=False)).to(dev)
+    tpos = p[idx].contiguous()
+    pm, _ = plan.gather(F4, tpos)
+    src = p.double()
+    truth = direct_sum_fp64(src[idx].contiguous(), src, m.double(), eps=eps, box=box, target_index=idx.contiguous())
+    x = net.input(rho, F4)
+    return {"kind": kind, "seed": seed, "x": x, "tpos": tpos, "pm": pm, "truth": truth.float(),
+            "label": (truth - pm.double()).float()}
+
+
+def make_dataset(plan, net, n, count, seed0, kinds=scenes.SCENES, n_targets=8192, eps=1.0 / 256, log=None):
+    out = []
+    t0 = time.time()
+    for i in range(count):
+        out.append(make_snapshot(plan, net, kinds[i % len(kinds)], n, seed0 + i, n_targets, eps))
+        if log and (i + 1) % max(1, count // 10) == 0:
+            log(f"snapshots {i + 1}/{count} ({time.time() - t0:.1f} s)")
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# training
+# ---------------------------------------------------------------------------------------------
+def _predict(plan: PMPlan, field: torch.Tensor, B: int, snaps) -> list:
+    G = plan.grid
+    f = field.view(B, G, G, G, 4)
+    return [plan.gather(f[b], s["tpos"])[0] for b, s in enumerate(snaps)]
+
+
+def train(net: GridCNN, plan: PMPlan, data: list, steps: int, batch: int = 4, lr: float = 3e-4,
+          weight_decay: float = 0.01, seed: int = 4738, log=None, log_every: int = 100, clip: float = 1.0,
+          warmup: int = 50) -> list:
+    """AdamW on loss = mean over the batch's snapshots of sum |pred - label|^2 / sum |label|^2, with
+    linear warm-up then cosine decay of the learning rate, gradient-norm clipping and skipping
+    of non-finite steps (scripts/train_scatter_field.py:190, :228-235)."""
+    G = plan.grid
+    rng = np.random.default_rng(seed)
+    hist = []
+    field = torch.zeros(batch * G ** 3 * 4, device=plan.device)
+    dfield = torch.zeros_like(field)
+    t0 = time.time()
+    window, skipped = [], 0
+    for it in range(1, steps + 1):
+        pick = rng.choice(len(data), size=batch, replace=len(data) < batch)
+        snaps = [data[i] for i in pick]
+        x = torch.cat([s["x"] for s in snaps])
+        field.zero_()
+        net.forward(x, batch, G, field, train=True)
+        preds = _predict(plan, field, batch, snaps)
+        loss = 0.0
+        dfield.zero_()
+        d4 = dfield.view(batch, G ** 3 * 4)
+        for b, (s, pr) in enumerate(zip(snaps, preds)):
+            # each snapshot normalised by its own residual energy, so that scenes with small
+            # forces (a uniform box) weigh as much as concentrated ones
+            den = batch * max(float((s["label"] ** 2).sum()), 1e-30)
+            diff = pr - s["label"]
+            loss += float((diff ** 2).sum()) / den
+            g = (2.0 / den) * diff
+            net._call("augur_cnn_gather_transpose", s["tpos"].data_ptr(), g.contiguous().data_ptr(),
+                      s["tpos"].shape[0], G, plan.extent, d4[b].data_ptr())
+        net.backward(dfield, batch, G)
+        gn = net.clip_grad_norm(clip)
+        if not (math.isfinite(loss) and math.isfinite(gn)):
+            skipped += 1
+            continue
+        sched = min(1.0, it / max(1, warmup)) * (0.55 + 0.45 * math.cos(math.pi * it / steps))
+        net.adamw(lr=lr * sched, weight_decay=weight_decay)
+        window.append(loss)
+        if it % log_every == 0 or it == steps:
+            net.check()
+            hist.append({"step": it, "loss": float(np.mean(window)), "grad_norm": gn, "skipped": skipped,
+                         "s": time.time() - t0})
+            window = []
+            if log:
+                log(f"step {it} loss {hist[-1]['loss']:.4f} |g| {gn:.3g} ({time.time() - t0:.1f} s)")
+    return hist
+
+
+# ---------------------------------------------------------------------------------------------
+# evaluation
+# ---------------------------------------------------------------------------------------------
+def errors(a: torch.Tensor, truth: torch.Tensor) -> dict:
+    d = (a.double() - truth.double()).norm(dim=1)
+    rms = truth.double().norm(dim=1).pow(2).mean().sqrt()
+    e = (d / rms).cpu().numpy()
+    return {"rel_rms": float(d.pow(2).mean().sqrt() / rms), "median_norm_by_rms": float(np.sort(e)[(len(e) - 1) // 2]),
+            "p90_norm_by_rms": float(np.quantile(e, 0.9))}
+
+
+def evaluate(net: GridCNN, plan: PMPlan, data: list) -> dict:
+    """Force error vs the FP64 direct sum with and without the learned correction: per scene
+    kind (bodies of all that kind's snapshots pooled) and over all kinds (mean of the kinds)."""
+    G = plan.grid
+    field = torch.zeros(G ** 3 * 4, device=plan.device)
+    pooled: dict = {}
+    for s in data:
+        field.zero_()
+        net.forward(s["x"], 1, G, field)
+        corr = plan.gather(field.view(G, G, G, 4), s["tpos"])[0]
+        d = pooled.setdefault(s["kind"], {"pm": [], "cnn": [], "truth": []})
+        d["pm"].append(s["pm"])
+        d["cnn"].append(s["pm"] + corr)
+        d["truth"].append(s["truth"])
+    out = {"by_kind": {}}
+    for kind, d in pooled.items():
+        t = torch.cat(d["truth"])
+        out["by_kind"][kind] = {"plain_pm": errors(torch.cat(d["pm"]), t), "cnn": errors(torch.cat(d["cnn"]), t)}
+    for form in ("plain_pm", "cnn"):
+        rows = [v[form] for v in out["by_kind"].values()]
+        out[form] = {m: float(np.mean([r[m] for r in rows])) for m in rows[0]}
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# fallback and the corrected leapfrog
+# ---------------------------------------------------------------------------------------------
+class FallbackMonitor:
+    """Reverts to plain PM when |E - E0| / |E0| > drift_max or when the rms predicted correction
+    exceeds corr_max times the rms PM force. Once reverted, the scene stays on plain PM."""
+
+    def __init__(self, drift_max: float = 0.05, corr_max: float = 0.5):
+        self.drift_max, self.corr_max = drift_max, corr_max
+        self.e0 = None
+        self.reverted = False
+        self.reason = None
+        self.history = []
+
+    def observe(self, energy: float | None = None, corr_ratio: float | None = None) -> bool:
+        """Record one check; returns True while the learned correction stays enabled."""
+        if self.reverted:
+            return False
+        if energy is not None:
+            if self.e0 is None:
+                self.e0 = energy
+            drift = abs(energy - self.e0) / max(abs(self.e0), 1e-300)
+            self.history.append(("drift", drift))
+            if not math.isfinite(energy) or drift > self.drift_max:
+                self.reverted, self.reason = True, f"energy drift {drift:.3g} > {self.drift_max}"
+        if corr_ratio is not None:
+            self.history.append(("corr", corr_ratio))
+            if not math.isfinite(corr_ratio) or corr_ratio > self.corr_max:
+                self.reverted, self.reason = True, f"correction/force {corr_ratio:.3g} > {self.corr_max}"
+        return not self.reverted
+
+
+class CorrectedPM:
+    """Leapfrog of one scene on the PM run loop with the CNN correction added to the force grid
+    between the Poisson solve and the gather. check_every: steps between monitor checks (the
+    check step also solves for the potential lane for the energy)."""
+
+    def __init__(self, plan: PMPlan, net: GridCNN | None, monitor: FallbackMonitor | None = None,
+                 check_every: int = 10):
+        self.plan, self.net = plan, net
+        self.monitor = monitor or FallbackMonitor()
+        self.check_every = check_every
+        G = plan.grid
+        self.rho = torch.empty((G,) * 3, device=plan.device)
+        self.energy = torch.zeros(2, dtype=torch.float64, device=plan.device)
+        self.nstep = 0
+        self.last_energy = None
+
+    def _grid(self, check: bool):
+        use = self.net is not None and not self.monitor.reverted
+        F4 = self.plan.run_grid(self.rho if use else None, with_phi=use or check)
+        if use:
+            pm_rms = None
+            if check:
+                pm_rms = float(F4[..., :3].pow(2).sum(-1).mean().sqrt())
+                before = F4[..., :3].clone()
+            x = self.net.input(self.rho, F4)
+            self.net.forward(x, 1, self.plan.grid, F4.view(-1))
+            if check:
+                corr = float((F4[..., :3] - before).pow(2).sum(-1).mean().sqrt())
+                self.monitor.observe(corr_ratio=corr / max(pm_rms, 1e-30))
+        return F4
+
+    def begin(self, pos, vel, mass=None, mask=None, dt: float = 5e-4):
+        self.dt = dt
+        self.plan.run_load(pos, vel, mass, mask, dt=dt)
+        self._grid(True)
+        self.plan.run_kick(0.5 * dt, True, energy_out=self.energy, esync=0.0)
+        self._record()
+
+    def steps(self, k: int):
+        for _ in range(k):
+            self.nstep += 1
+            check = self.check_every > 0 and self.nstep % self.check_every == 0
+            self._grid(check)
+            if check:
+                self.plan.run_kick(self.dt, True, energy_out=self.energy, esync=0.5 * self.dt)
+                self._record()
+            else:
+                self.plan.run_kick(self.dt, True)
+
+    def end(self, pos, vel):
+        self._grid(True)
+        self.plan.run_kick(0.5 * self.dt, False, energy_out=self.energy, esync=0.5 * self.dt)
+        self._record()
+        self.plan.run_unload(pos, vel)
+
+    def _record(self):
+        ke, pe = self.energy.tolist()
+        self.last_energy = ke + pe
+        self.monitor.observe(energy=self.last_energy)

@@ -43,6 +43,14 @@ def _need(t: torch.Tensor, name: str, dtype=torch.float32, shape=None, device=No
     return t
 
 
+class _DeviceBuffer:
+    """__cuda_array_interface__ view of plan-owned device memory (float32)."""
+
+    def __init__(self, addr: int, nbytes: int, device):
+        self.__cuda_array_interface__ = {"shape": (nbytes // 4,), "typestr": "<f4", "data": (int(addr), False),
+                                         "version": 3, "strides": None}
+
+
 class PMPlan:
     """One grid geometry + workspace for up to ``max_bodies`` bodies.
 
@@ -187,6 +195,44 @@ class PMPlan:
 
     def run_steps(self, k: int) -> None:
         self._call("augur_pm_run_steps", int(k))
+
+    # ---- run loop in pieces (the CNN-corrected step edits the force grid in between) ---------
+    def run_load(self, pos, vel, mass=None, mask=None, dt: float = 1e-3) -> None:
+        n = self._n(pos)
+        _need(vel, "vel", shape=pos.shape, device=self.device)
+        mass, mask = self._mm(n, mass, mask)
+        self._keep = (mass, mask)
+        self._call("augur_pm_run_load", pos.data_ptr(), vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), n,
+                   float(dt))
+
+    def run_grid(self, rho_out: torch.Tensor | None = None, with_phi: bool = False) -> torch.Tensor:
+        """Deposit + solve for the current state; returns the plan's force grid (G,)*3 + (4,) (a view
+        of plan-owned memory, valid until the next grid call)."""
+        if rho_out is not None:
+            _need(rho_out, "rho_out", shape=self.grid_shape, device=self.device)
+        self._call("augur_pm_run_grid", _ptr(rho_out), int(bool(with_phi)))
+        return self.force_grid()
+
+    def force_grid(self) -> torch.Tensor:
+        addr = self.lib.augur_pm_force_grid(self._p)
+        if not addr:
+            raise RuntimeError("augur_pm_force_grid returned NULL")
+        n = self.grid ** self.dim * 4
+        holder = _DeviceBuffer(addr, n * 4, self.device)
+        return torch.as_tensor(holder, device=self.device).view(self.grid_shape + (4,))
+
+    def run_kick(self, kick: float, drift: bool, want_acc_like: torch.Tensor | None = None,
+                 energy_out: torch.Tensor | None = None, esync: float = 0.0):
+        """Gather + kick (+ drift). energy_out: device float64 (2,) <- (kinetic at v + esync a,
+        potential), needs the preceding run_grid(with_phi=True)."""
+        acc = torch.empty_like(want_acc_like) if want_acc_like is not None else None
+        if energy_out is not None:
+            _need(energy_out, "energy_out", torch.float64, shape=(2,), device=self.device)
+        self._call("augur_pm_run_kick", float(kick), int(bool(drift)), _ptr(acc), _ptr(energy_out), float(esync))
+        return acc
+
+    def run_unload(self, pos, vel) -> None:
+        self._call("augur_pm_run_unload", pos.data_ptr(), vel.data_ptr())
 
     STAGES = ("sort", "deposit_r2c", "fft_y_fwd", "fft_z_green", "fft_y_inv", "c2r", "gather_kd")
 

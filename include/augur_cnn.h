@@ -61,7 +61,7 @@ int augur_cnn_wgrad(int kind, const void *h, const void *dz, int batch, int grid
 int augur_cnn_prep_weights(const float *w, int n_out, int c_in, int cin_pad, int n_pad, int flip, void *out,
                            void *stream);
 
-/* x (nvox, 2) bf16 = (rho_scale * rho, phi_scale * force4.w). */
+/* x (nvox, 2) bf16 = (log(1 + rho_scale * rho), phi_scale * force4.w). */
 int augur_cnn_input(const float *rho, const float *force4, int64_t nvox, float rho_scale, float phi_scale, void *x,
                     void *stream);
 

@@ -150,6 +150,30 @@ int augur_pm_run_end(augur_pm_plan *plan, float *pos, float *vel, float *acc_out
                      void *stream);
 
 /*
+ * Run loop in pieces, for callers that modify the force grid between the Poisson solve
+ * and the gather (the CNN-corrected step adds its correction field there):
+ *   run_load   sort the caller's bodies into the device state (no force yet)
+ *   run_grid   re-sort if a kick moved the bodies, deposit (density also written to
+ *              rho_out when not NULL), FFT solve; with_phi = 1 fills the potential lane
+ *   force_grid the plan's float4 force grid (G^3 cells: a_x, a_y, a_z, phi), device memory
+ *   run_kick   gather the grid at the bodies, v += kick * a; drift = 1 also moves the
+ *              bodies x += dt * v (wrapped) and prepares the next sort; acc_out as run_end.
+ *              energy_out (device, 2 doubles, may be NULL; needs a with_phi grid) receives
+ *              sum m |v + esync a|^2 / 2 and sum m phi / 2 over the bodies (fixed-order sums):
+ *              esync = dt/2 gives the energy at the synchronised time of a merged step
+ *   run_unload write positions and velocities back in the caller's order
+ * A leapfrog step is run_grid + run_kick(dt, 1); the opening and closing half kicks use
+ * kick = dt/2 (drift 1 and 0). Replaces the body of Sim.tick (scripts/scatter_bh_1b.py:133-138).
+ */
+int augur_pm_run_load(augur_pm_plan *plan, const float *pos, const float *vel, const float *mass,
+                      const float *mask, int64_t n, float dt, void *stream);
+int augur_pm_run_grid(augur_pm_plan *plan, float *rho_out, int with_phi, void *stream);
+float *augur_pm_force_grid(augur_pm_plan *plan);
+int augur_pm_run_kick(augur_pm_plan *plan, float kick, int drift, float *acc_out, double *energy_out,
+                      float esync, void *stream);
+int augur_pm_run_unload(augur_pm_plan *plan, float *pos, float *vel, void *stream);
+
+/*
  * Measurement aid: k merged steps like augur_pm_run_steps with a CUDA event recorded on
  * the stream between the stages of each step; synchronises after every step and writes
  * the mean device milliseconds per stage to stage_ms[0..AUGUR_PM_NSTAGE-1] in the order
