@@ -85,9 +85,11 @@ class GridCNN:
                 "step": self.adam_step, "scales": (self.rho_scale, self.phi_scale, self.out_scale)}
 
     def load_state_dict(self, d: dict) -> None:
+        """Loads parameters and scales; AdamW moments when present (inference weights omit them)."""
         self.params.copy_(d["params"].to(self.device))
-        self.m.copy_(d["m"].to(self.device))
-        self.v.copy_(d["v"].to(self.device))
+        if "m" in d:
+            self.m.copy_(d["m"].to(self.device))
+            self.v.copy_(d["v"].to(self.device))
         self.adam_step = int(d["step"])
         self.rho_scale, self.phi_scale, self.out_scale = d["scales"]
         self.prepare()

@@ -51,41 +51,49 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 struct ConvArgs {
   int B, G;
-  int ntiles;        // B * G * G * ceil(G / 128)
   int xseg;          // ceil(G / 128)
+  int yc;            // y rows per work unit
+  int nyc;           // ceil(G / yc)
+  int nunits;        // B * G * xseg * nyc
   float out_scale;   // EPI_OUT: added field = out_scale * (acc + bias)
 };
+
+constexpr int RING = 5;  // y rows of input slabs kept per z plane (rows y-1 .. y+2 plus one being freed)
 
 // ---------------------------------------------------------------------------------------
 // tcgen05 implicit-GEMM 3x3x3 conv. CIN in {16, 32}, N in {16, 32}.
 //   EPI_FWD: z = acc + b ; h = h_in + gelu(z)         out0 = h (bf16), out1 = z (bf16, optional)
 //   EPI_OUT: y = out_scale * (acc + b)[0..2]          out0 = F (float4 grid, y added to lanes 0..2)
 //   EPI_BWD: g = acc + resid (fp32, optional)         out0 = g (fp32), out1 = g * gelu'(zprev) (bf16)
+//
+// Work unit = (batch, z, x segment, chunk of yc consecutive y rows). The CTA walks y inside
+// the unit keeping a ring of RING input rows per z plane in shared memory, so each new tile
+// loads one y row for each of the three z planes (prefetched one tile ahead with cp.async);
+// the 54 MMAs of tile y go to TMEM accumulator y & 1 while the epilogue of tile y-1 reads
+// the other one.
 // ---------------------------------------------------------------------------------------
 template <int CIN, int N, int EPI>
-__global__ void __launch_bounds__(CONV_THREADS) conv_tc_kernel(const bf16 *__restrict__ in,
-                                                               const bf16 *__restrict__ wB,
-                                                               const float *__restrict__ bias,
-                                                               const void *__restrict__ resid,
-                                                               const bf16 *__restrict__ zprev, void *__restrict__ out0,
-                                                               bf16 *__restrict__ out1, ConvArgs a,
-                                                               unsigned *__restrict__ err) {
+__global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const bf16 *__restrict__ in,
+                                                                  const bf16 *__restrict__ wB,
+                                                                  const float *__restrict__ bias,
+                                                                  const void *__restrict__ resid,
+                                                                  const bf16 *__restrict__ zprev,
+                                                                  void *__restrict__ out0, bf16 *__restrict__ out1,
+                                                                  ConvArgs a, unsigned *__restrict__ err) {
   constexpr int CB = CIN / 8;                  // 16-byte channel blocks per voxel
   constexpr int KSTEP_PER_TAP = CIN / 16;      // K = 16 per MMA
   constexpr int WBYTES = 27 * CIN * N * 2;     // weights, UMMA B layout
   constexpr int SLAB_BYTES = CB * SLAB * 16;
+  constexpr int SLAB_STRIDE = ((SLAB_BYTES + 127) / 128) * 128;
   constexpr uint32_t IDESC = idesc_bf16_f32(CONV_M, N);
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;
-  unsigned char *sSlab0 = smem + ((WBYTES + 127) / 128) * 128;
-  unsigned char *sSlab1 = sSlab0 + ((SLAB_BYTES + 127) / 128) * 128;
+  unsigned char *sSlab = smem + ((WBYTES + 127) / 128) * 128;  // [3 z planes][RING rows]
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t s_tmem;
-  __shared__ int s_fail;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int G = a.G;
-  // weights -> shared memory
   {
     const uint4 *src = reinterpret_cast<const uint4 *>(wB);
     uint4 *dst = reinterpret_cast<uint4 *>(sW);
@@ -95,10 +103,9 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_tc_kernel(const bf16 *__res
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     mbar_fence_init();
-    s_fail = 0;
   }
   if (warp == 0) {
-    tmem_alloc(&s_tmem, 32);
+    tmem_alloc(&s_tmem, 64);  // two 32-column accumulators
     tmem_relinquish();
   }
   fence_async_smem();
@@ -106,73 +113,31 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_tc_kernel(const bf16 *__res
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
-  uint32_t commits[2] = {0, 0};  // commits issued to each barrier (all threads track them)
-  const uint32_t slab_addr[2] = {smem_u32(sSlab0), smem_u32(sSlab1)};
+  const uint32_t slab0 = smem_u32(sSlab);
   const uint32_t w_addr = smem_u32(sW);
-  unsigned char *slab_ptr[2] = {sSlab0, sSlab1};
+  uint32_t commits[2] = {0, 0};
   bool ok = true;
 
-  for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x) {
-    int t = tile;
-    const int xs = t % a.xseg;
-    t /= a.xseg;
-    const int y = t % G;
-    t /= G;
-    const int z = t % G;
-    const int b = t / G;
-    const int x0 = xs * CONV_M;
-    const size_t bbase = (size_t)b * G * G * G;
-
-    for (int p = 0; p < 9 && ok; ++p) {
-      const int dz = p / 3, dy = p % 3;
-      const int buf = p & 1;
-      if (commits[buf] > 0) {  // the MMAs that read this buffer last time must be done
-        if (!mbar_wait_bounded(&mbar[buf], (commits[buf] - 1) & 1, WAIT_BUDGET)) {
-          ok = false;
-          break;
-        }
-      }
-      const int zz = z + dz - 1, yy = y + dy - 1;
-      const bool rowok = (zz >= 0) && (zz < G) && (yy >= 0) && (yy < G);
-      const bf16 *rowp = in + (bbase + ((size_t)zz * G + yy) * G) * CIN;
-      for (int c = tid; c < SLAB * CB; c += CONV_THREADS) {
-        const int r = c / CB, cb = c - r * CB;
-        const int xx = x0 - 1 + r;
-        const bool v = rowok && xx >= 0 && xx < G;
-        const bf16 *src = v ? rowp + (size_t)xx * CIN + cb * 8 : in;
-        cp_async16(slab_addr[buf] + (uint32_t)(cb * SLAB + r) * 16u, src, v);
-      }
-      cp_async_wait_all();
-      fence_async_smem();
-      __syncthreads();
-      if (tid == 0) {
-        tc_fence_after();
-#pragma unroll
-        for (int dx = 0; dx < 3; ++dx) {
-          const int tap = (dz * 3 + dy) * 3 + dx;
-#pragma unroll
-          for (int kc = 0; kc < KSTEP_PER_TAP; ++kc) {
-            const uint64_t ad = smem_desc(slab_addr[buf] + (uint32_t)(2 * kc * SLAB * 16 + dx * 16), SLAB * 16, 128);
-            const int s = tap * KSTEP_PER_TAP + kc;
-            const uint64_t bd = smem_desc(w_addr + (uint32_t)(2 * s * N * 16), N * 16, 128);
-            umma_bf16(tmem, ad, bd, IDESC, (p | dx | kc) ? 1u : 0u);
-          }
-        }
-        umma_commit(&mbar[buf]);
-      }
-      commits[buf]++;
-      (void)slab_ptr;
+  auto slab_addr = [&](int dz, int row) -> uint32_t {
+    return slab0 + (uint32_t)((dz * RING + ((row + RING) % RING)) * SLAB_STRIDE);
+  };
+  // copy input row (z + dz - 1, row) of x segment x0 into its ring slot (zero outside the grid)
+  auto load_row = [&](size_t bbase, int z, int x0, int row) {
+    for (int c = tid; c < 3 * SLAB * CB; c += CONV_THREADS) {
+      const int dz = c / (SLAB * CB);
+      const int rem = c - dz * SLAB * CB;
+      const int r = rem / CB, cb = rem - r * CB;
+      const int zz = z + dz - 1, xx = x0 - 1 + r;
+      const bool v = zz >= 0 && zz < G && row >= 0 && row < G && xx >= 0 && xx < G;
+      const bf16 *src = v ? in + (bbase + ((size_t)zz * G + row) * G + xx) * CIN + cb * 8 : in;
+      cp_async16(slab_addr(dz, row) + (uint32_t)(cb * SLAB + r) * 16u, src, v);
     }
-    if (!ok) break;
-    // all MMAs of this tile: the last commit went to barrier 0 (p = 8), the one before to 1
-    if (!mbar_wait_bounded(&mbar[0], (commits[0] - 1) & 1, WAIT_BUDGET) ||
-        !mbar_wait_bounded(&mbar[1], (commits[1] - 1) & 1, WAIT_BUDGET)) {
-      ok = false;
-      break;
-    }
+  };
+  // epilogue of the tile at (bbase, z, y, x0) from accumulator acc_sel
+  auto epilogue = [&](size_t bbase, int z, int y, int x0, int acc_sel) {
     tc_fence_after();
     float acc[32];
-    tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), acc);
+    tmem_ld32(tmem + (uint32_t)(acc_sel * 32) + ((uint32_t)(warp * 32) << 16), acc);
     const int x = x0 + warp * 32 + lane;
     if (x < G) {
       const size_t vox = bbase + ((size_t)z * G + y) * G + x;
@@ -180,12 +145,19 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_tc_kernel(const bf16 *__res
         const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N;
         bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N;
 #pragma unroll
-        for (int n = 0; n < N; n += 2) {
-          float z0 = acc[n] + bias[n], z1 = acc[n + 1] + bias[n + 1];
-          __nv_bfloat162 hi = *reinterpret_cast<const __nv_bfloat162 *>(hin + n);
-          float h0 = __bfloat162float(hi.x) + gelu_f(z0), h1 = __bfloat162float(hi.y) + gelu_f(z1);
-          *reinterpret_cast<__nv_bfloat162 *>(hout + n) = __floats2bfloat162_rn(h0, h1);
-          if (out1) *reinterpret_cast<__nv_bfloat162 *>(out1 + vox * N + n) = __floats2bfloat162_rn(z0, z1);
+        for (int n = 0; n < N; n += 8) {
+          uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
+          const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
+          __align__(16) __nv_bfloat162 ho[4], zo[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float z0 = acc[n + 2 * q] + bias[n + 2 * q], z1 = acc[n + 2 * q + 1] + bias[n + 2 * q + 1];
+            ho[q] = __floats2bfloat162_rn(__bfloat162float(hp[q].x) + gelu_f(z0),
+                                          __bfloat162float(hp[q].y) + gelu_f(z1));
+            zo[q] = __floats2bfloat162_rn(z0, z1);
+          }
+          *reinterpret_cast<uint4 *>(hout + n) = *reinterpret_cast<uint4 *>(ho);
+          if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + n) = *reinterpret_cast<uint4 *>(zo);
         }
       } else if constexpr (EPI == EPI_OUT) {
         float4 *F = reinterpret_cast<float4 *>(out0) + vox;
@@ -198,27 +170,115 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_tc_kernel(const bf16 *__res
         const float *rin = reinterpret_cast<const float *>(resid);
         float *gout = reinterpret_cast<float *>(out0) + vox * N;
 #pragma unroll
-        for (int n = 0; n < N; ++n) {
-          float g = acc[n] + (rin ? rin[vox * N + n] : 0.f);
-          gout[n] = g;
-          if (out1) out1[vox * N + n] = __float2bfloat16_rn(g * gelu_grad(__bfloat162float(zprev[vox * N + n])));
+        for (int n = 0; n < N; n += 4) {
+          float4 g = make_float4(acc[n], acc[n + 1], acc[n + 2], acc[n + 3]);
+          if (rin) {
+            const float4 r = *reinterpret_cast<const float4 *>(rin + vox * N + n);
+            g.x += r.x;
+            g.y += r.y;
+            g.z += r.z;
+            g.w += r.w;
+          }
+          *reinterpret_cast<float4 *>(gout + n) = g;
+          if (out1) {
+            const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(zprev + vox * N + n);
+            const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(zprev + vox * N + n + 2);
+            __align__(8) __nv_bfloat162 o[2];
+            o[0] = __floats2bfloat162_rn(g.x * gelu_grad(__bfloat162float(z01.x)),
+                                         g.y * gelu_grad(__bfloat162float(z01.y)));
+            o[1] = __floats2bfloat162_rn(g.z * gelu_grad(__bfloat162float(z23.x)),
+                                         g.w * gelu_grad(__bfloat162float(z23.y)));
+            *reinterpret_cast<uint2 *>(out1 + vox * N + n) = *reinterpret_cast<uint2 *>(o);
+          }
         }
       }
     }
+  };
+
+  for (int unit = blockIdx.x; unit < a.nunits && ok; unit += gridDim.x) {
+    int t = unit;
+    const int yc = t % a.nyc;
+    t /= a.nyc;
+    const int xs = t % a.xseg;
+    t /= a.xseg;
+    const int z = t % G;
+    const int b = t / G;
+    const int x0 = xs * CONV_M;
+    const size_t bbase = (size_t)b * G * G * G;
+    const int ya = yc * a.yc, yb = min(G, ya + a.yc);
+    // warm-up: rows ya-1, ya, ya+1
+    load_row(bbase, z, x0, ya - 1);
+    load_row(bbase, z, x0, ya);
+    load_row(bbase, z, x0, ya + 1);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int y = ya; y < yb; ++y) {
+      // prefetch the row the next tile adds (its slot last served tile y-2, finished below)
+      load_row(bbase, z, x0, y + 2);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+      fence_async_smem();
+      __syncthreads();
+      const int sel = y & 1;
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(sel * 32);
+#pragma unroll 1
+        for (int pz = 0; pz < 3; ++pz) {
+#pragma unroll 1
+          for (int py = 0; py < 3; ++py) {
+            const uint32_t sa = slab_addr(pz, y + py - 1);
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx) {
+              const int tap = (pz * 3 + py) * 3 + dx;
+#pragma unroll
+              for (int kc = 0; kc < KSTEP_PER_TAP; ++kc) {
+                const uint64_t ad = smem_desc(sa + (uint32_t)(2 * kc * SLAB * 16 + dx * 16), SLAB * 16, 128);
+                const int s = tap * KSTEP_PER_TAP + kc;
+                const uint64_t bd = smem_desc(w_addr + (uint32_t)(2 * s * N * 16), N * 16, 128);
+                umma_bf16(d, ad, bd, IDESC, (pz | py | dx | kc) ? 1u : 0u);
+              }
+            }
+          }
+        }
+        umma_commit(&mbar[sel]);
+      }
+      commits[sel]++;
+      if (y > ya) {  // epilogue of the previous tile while this tile's MMAs run
+        const int ps = sel ^ 1;
+        const bool got = mbar_wait_bounded(&mbar[ps], (commits[ps] - 1) & 1, WAIT_BUDGET);
+        if (__syncthreads_or(!got)) {  // the give-up decision is the same in every thread
+          ok = false;
+          break;
+        }
+        epilogue(bbase, z, y - 1, x0, ps);
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+    if (!ok) break;
+    // last tile of the unit
+    const int ls = (yb - 1) & 1;
+    const bool got = mbar_wait_bounded(&mbar[ls], (commits[ls] - 1) & 1, WAIT_BUDGET);
+    if (__syncthreads_or(!got)) {
+      ok = false;
+      break;
+    }
+    epilogue(bbase, z, yb - 1, x0, ls);
+    asm volatile("cp.async.wait_all;" ::: "memory");  // the unit's last prefetch (beyond the chunk)
     tc_fence_before();
     __syncthreads();
   }
   if (!ok) {
     if (tid == 0) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
-    // let any MMA still in flight finish before the accumulator is released
     for (int bb = 0; bb < 2; ++bb)
       if (commits[bb] > 0) mbar_wait_bounded(&mbar[bb], (commits[bb] - 1) & 1, WAIT_BUDGET);
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, 32);
+    tmem_dealloc(tmem, 64);
   }
 }
 
@@ -443,20 +503,26 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   a.B = B;
   a.G = G;
   a.xseg = (G + CONV_M - 1) / CONV_M;
-  a.ntiles = B * G * G * a.xseg;
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // y chunk: long enough to amortise the 3-row warm-up, short enough to fill every SM
+  const int columns = B * G * a.xseg;
+  int yc = G;
+  while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
+  a.yc = yc;
+  a.nyc = (G + yc - 1) / yc;
+  a.nunits = columns * a.nyc;
   a.out_scale = out_scale;
   constexpr int WBYTES = 27 * CIN * N * 2;
-  constexpr int SLAB_BYTES = (CIN / 8) * SLAB * 16;
-  const size_t smem = ((WBYTES + 127) / 128) * 128 + 2 * (((SLAB_BYTES + 127) / 128) * 128);
+  constexpr int SLAB_STRIDE = ((((CIN / 8) * SLAB * 16) + 127) / 128) * 128;
+  const size_t smem = ((WBYTES + 127) / 128) * 128 + (size_t)3 * RING * SLAB_STRIDE;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(conv_tc_kernel<CIN, N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = std::min(a.ntiles, nsm * 2);
+  const int grid = std::min(a.nunits, nsm);
   conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(
       (const bf16 *)in, (const bf16 *)wB, bias, resid, (const bf16 *)zprev, out0, (bf16 *)out1, a, err);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;

@@ -112,6 +112,7 @@ int dalloc(augur_pm_plan *p, T **ptr, size_t count) {
 unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 constexpr uint32_t DEP_CHUNK_MIN = 16384;
+constexpr int DEP_THREADS = 256;
 uint32_t dep_chunk(int64_t n) {
   int64_t c = (n + 1023) / 1024;
   return (uint32_t)std::max<int64_t>(DEP_CHUNK_MIN, c);
@@ -208,7 +209,7 @@ int launch_deposit(augur_pm_plan *p, float *rho, float2 *spec, cudaStream_t st) 
   AUGUR_LAUNCH_CHECK(p);
   const int64_t items = (int64_t)p->nblk + 4 * ((p->cur_n + a.chunk - 1) / a.chunk) + 1;
   if ((size_t)items > p->dep_items_max) return AUGUR_ERANGE;
-  deposit_kernel<D, MODE><<<(unsigned)items, 512, p->smem_dep, st>>>(
+  deposit_kernel<D, MODE><<<(unsigned)items, DEP_THREADS, p->smem_dep, st>>>(
       p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
       p->dep_item_blk, p->dep_scratch, p->dep_counters);
   AUGUR_LAUNCH_CHECK(p);
@@ -446,7 +447,7 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   // tile shapes (the autotuner overrides these through augur_pm_plan_set_tiles)
   p->dep_RY = 16;
   if (dim == 3) {
-    int rr = 100000 / (12 * G);
+    int rr = 50000 / (12 * G);  // ~50 KB of shared memory: four 256-thread CTAs per SM
     int rz = rr / 16;
     if (rz < 1) {
       rz = 1;

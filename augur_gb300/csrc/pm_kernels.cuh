@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
 // threadfence, no waiting) adds the others' tiles before converting.
 // ---------------------------------------------------------------------------------
 template <int D, int MODE>
-__global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__ pos4,
+__global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restrict__ pos4,
                                                       const unsigned *__restrict__ mmax_bits, DepositArgs a,
                                                       const float2 *__restrict__ twg, float *__restrict__ rho_out,
                                                       float2 *__restrict__ spec_out, unsigned *__restrict__ err,
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(512) deposit_kernel(const float4 *__restrict__
     }
   }
   for (int e = tid; e < RR * G; e += nt) acc[e] = 0ull;
-  if (MODE == 1)
+  if (MODE != 0)
     for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
   __syncthreads();
 

@@ -175,23 +175,70 @@ def config(args):
             "l2": "per-step traffic ~1.5 GB over ~0.8 GB of buffers > 129 MB L2; no flush"}
 
 
-def accuracy(plan, pos_d, mass_d, n, G, ns=4096, seed=9100):
-    """Plain-PM force error vs the FP64 periodic (Ewald) direct sum on ns sampled bodies."""
+def fp64_truth(pos_d, mass_d, n, ns=4096, seed=9100):
+    """FP64 periodic (minimum image + Ewald) direct sum at ns sampled bodies, eps = 1/256."""
     from augur_gb300 import direct_sum_fp64
 
-    ones = torch.ones(n, device=pos_d.device)
-    acc = plan.force(pos_d, mass_d, ones).double()
     idx = torch.from_numpy(np.random.default_rng(seed).choice(n, ns, replace=False)).to(pos_d.device)
     src = pos_d.double()
     truth = direct_sum_fp64(src[idx].contiguous(), src, mass_d.double(), eps=1.0 / 256, box=1.0,
                             target_index=idx.contiguous())
-    a = acc[idx]
-    d = (a - truth).norm(dim=1)
+    return idx, truth
+
+
+def force_error(a, truth):
+    d = (a.double() - truth).norm(dim=1)
     rms = truth.norm(dim=1).pow(2).mean().sqrt()
     e = (d / rms).cpu().numpy()
     return {"vs": "FP64 periodic direct sum (min-image + Ewald), eps=1/256, 4096 sampled bodies",
             "rel_rms": float((d.pow(2).mean().sqrt() / rms).item()),
             "median_norm_by_rms": float(np.sort(e)[(len(e) - 1) // 2]), "p90_norm_by_rms": float(np.quantile(e, 0.9))}
+
+
+def cnn_form(args, pos, vel, mass, dev, idx, truth, st):
+    """The CNN-corrected step at 128^3 (trained weights) on the same bodies: body-steps/s and
+    force error, beside plain PM at 128^3."""
+    from augur_gb300 import PMPlan
+    from augur_gb300.cnn import GridCNN
+    from augur_gb300.learned import CorrectedPM, FallbackMonitor
+
+    ck = ROOT / "augur_gb300" / "weights" / "scatter_cnn_g128.pt"
+    if not ck.exists():
+        return {"unavailable": f"no trained weights at {ck.relative_to(ROOT)}"}
+    d = torch.load(ck, map_location="cpu", weights_only=False)
+    G = int(d["grid"])
+    n = args.bodies
+    plan = PMPlan(3, G, n, "periodic", 1.0, device=dev)
+    net = GridCNN(dev)
+    net.load_state_dict(d["net"])
+    p, v, m = (torch.from_numpy(x).to(dev) for x in (pos, vel, mass))
+    ones = torch.ones(n, device=dev)
+    # accuracy: PM on this grid with and without the correction, at the truth's bodies
+    rho = plan.deposit(p, m, ones)
+    F4 = plan.poisson(rho)
+    tp = p[idx].contiguous()
+    pm, _ = plan.gather(F4, tp)
+    field = torch.zeros(G ** 3 * 4, device=dev)
+    net.forward(net.input(rho, F4), 1, G, field)
+    corr, _ = plan.gather(field.view(G, G, G, 4), tp)
+    # throughput of the corrected leapfrog (monitor checks every 10 steps)
+    sim = CorrectedPM(plan, net, FallbackMonitor(), check_every=10)
+    sim.begin(p, v, m, ones, dt=args.dt)
+    sim.steps(3)
+    torch.cuda.synchronize(dev)
+    k = max(10, min(200, args.steps // 5))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    sim.steps(k)
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / k
+    sim.end(p, v)
+    net.check()
+    return {"form": "CNN-corrected PM", "grid": G, "value": n / (ms * 1e-3), "unit": "body-steps/s",
+            "ms_per_step": ms, "steps": k, "monitor_check_every": 10, "reverted_to_plain_pm": sim.monitor.reverted,
+            "accuracy": force_error(pm + corr, truth), "plain_pm_same_grid_accuracy": force_error(pm, truth),
+            "weights": str(ck.relative_to(ROOT)), "trained": {k2: d.get(k2) for k2 in ("bodies", "grid", "eps")}}
 
 
 def run_ours(args, world, rank, local):
@@ -266,9 +313,15 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1) / k_e2e
 
-    acc_info = None
+    acc_info, cnn_info = None, None
     if not args.no_accuracy and rank == 0:
-        acc_info = accuracy(plan, pos_d, mass_d, n, G)
+        idx, truth = fp64_truth(pos_d, mass_d, n)
+        acc_info = force_error(plan.force(pos_d, mass_d, ones)[idx], truth)
+        if not args.no_cnn:
+            cnn_info = cnn_form(args, pos, vel, mass, dev, idx, truth, st)
+            if "accuracy" in cnn_info:
+                cnn_info["equal_or_lower_error_than_plain_pm"] = \
+                    cnn_info["accuracy"]["rel_rms"] <= acc_info["rel_rms"]
 
     if rank != 0:
         return
@@ -299,6 +352,7 @@ def run_ours(args, world, rank, local):
         "gpu_launches": launches,
         "clocks": clk,
         "accuracy": acc_info,
+        "cnn_corrected": cnn_info,
         "cpu_baseline": None if cb is None else {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
     }
     print(json.dumps(line), flush=True)
@@ -315,6 +369,7 @@ def main():
     ap.add_argument("--dt", type=float, default=5e-4)
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cnn", action="store_true")
     ap.add_argument("--scene", default="plummer", choices=("plummer", "uniform", "clumpy", "disk", "flyby"))
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

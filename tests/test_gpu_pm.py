@@ -107,7 +107,7 @@ def test_nonfinite_positions_are_reported():
 # ---------------------------------------------------------------------------------------
 # K3 FFT Poisson + gradient
 # ---------------------------------------------------------------------------------------
-@pytest.mark.parametrize("G", [32, 64, 96, 128])
+@pytest.mark.parametrize("G", [32, 64, 96, 128, 256])
 def test_poisson_periodic_vs_oracle(G):
     pos, _, mass = scenes.make_scene("clumpy", 50000, seed=9300)
     rho = O.deposit_fixed(pos, mass, np.ones(len(pos)), G, 1.0, True)
