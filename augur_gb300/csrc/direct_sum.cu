@@ -252,9 +252,66 @@ __global__ void energy_final_kernel(const double *__restrict__ partial, int nblk
   else out[D + 2] = s;
 }
 
+// ---- allocation-free variant ------------------------------------------------------------
+// Scratch for the per-chunk partial sums of augur_direct_sum_fp64_noalloc: one file-scope
+// device array (4 MiB) that every GPU loading this library keeps until the process exits.
+constexpr int64_t DS_NOALLOC_DOUBLES = (int64_t)1 << 19;
+static __device__ __align__(256) double g_ds_noalloc_scratch[DS_NOALLOC_DOUBLES];
+
+double *g_ds_noalloc_ptr[64] = {nullptr};
+std::mutex g_ds_noalloc_mu;
+
+// Device address of the scratch array on the current device. In host code the array's name is
+// only a host-side stand-in, so the address comes from cudaGetSymbolAddress, once per device.
+int noalloc_scratch(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return AUGUR_ECUDA;
+  std::lock_guard<std::mutex> lk(g_ds_noalloc_mu);
+  if (!g_ds_noalloc_ptr[dev]) {
+    double *p = nullptr;
+    if (cudaGetSymbolAddress((void **)&p, g_ds_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return AUGUR_ECUDA;
+    }
+    g_ds_noalloc_ptr[dev] = p;
+  }
+  *out = g_ds_noalloc_ptr[dev];
+  return AUGUR_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int augur_direct_sum_fp64_noalloc(const double *targets, const int64_t *t_idx, int64_t T, const double *sources,
+                                  const double *mass, int64_t N, int dim, double eps, double *acc_out,
+                                  void *stream) {
+  if (T < 0 || N < 0 || (dim != 2 && dim != 3) || !(eps >= 0.0)) return AUGUR_EINVAL;
+  if (T == 0) return AUGUR_OK;
+  if (!targets || !acc_out || (N > 0 && !sources)) return AUGUR_EINVAL;
+  if (T * dim > DS_NOALLOC_DOUBLES) return AUGUR_ERANGE;  // more targets than the scratch holds
+  double *partial = nullptr;
+  int rc = noalloc_scratch(&partial);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t tblocks = (T + DS_THREADS - 1) / DS_THREADS;
+  int split = (int)std::max<int64_t>(1, std::min<int64_t>(64, 1216 / std::max<int64_t>(1, tblocks)));
+  if (N < (int64_t)split * DS_TILE) split = (int)std::max<int64_t>(1, N / DS_TILE);
+  split = (int)std::max<int64_t>(1, std::min<int64_t>(split, DS_NOALLOC_DOUBLES / (T * dim)));
+  const int64_t chunk = N > 0 ? (N + split - 1) / split : 1;
+  // every partial slot read below is written by the first kernel: nothing needs clearing
+  dim3 grid((unsigned)tblocks, (unsigned)split);
+  const double eps2 = eps * eps;
+  if (dim == 3)
+    direct_sum_partial_kernel<3, false><<<grid, DS_THREADS, 0, st>>>(targets, t_idx, T, sources, mass, N, chunk,
+                                                                     eps2, 0.0, nullptr, partial);
+  else
+    direct_sum_partial_kernel<2, false><<<grid, DS_THREADS, 0, st>>>(targets, t_idx, T, sources, mass, N, chunk,
+                                                                     eps2, 0.0, nullptr, partial);
+  const int64_t m = T * dim;
+  sum_partials_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(partial, split, m, acc_out);
+  return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
+}
 
 int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t T, const double *sources,
                           const double *mass, int64_t N, int dim, double eps, double box, double *acc_out,

@@ -206,6 +206,24 @@ int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t t
                           int dim, double eps, double box, double *acc_out, void *stream);
 
 /*
+ * The isolated FP64 direct sum above (box = 0) without any device allocation, for callers
+ * that cannot call cudaMalloc: code issuing work while a CUDA stream is being captured (where
+ * cudaMalloc is not allowed), and processes whose device memory is already reserved by
+ * another allocator (PyTorch's caching allocator keeps what it holds), where an extra
+ * allocation can fail. It has no counterpart in the reference.
+ * Its scratch is one static device array of 4 MiB (2^19 doubles) that every GPU loading
+ * this library keeps until the process exits; t * dim must not exceed 2^19 (else
+ * AUGUR_ERANGE). The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that call before any stream
+ * capture. All calls share the array: calls whose kernels overlap on the GPU (for example
+ * on two streams) race and give wrong results; serialise them on one stream. Results match
+ * augur_direct_sum_fp64 up to the order of the per-chunk partial sums.
+ */
+int augur_direct_sum_fp64_noalloc(const double *targets, const int64_t *t_idx, int64_t t,
+                                  const double *sources, const double *mass, int64_t n,
+                                  int dim, double eps, double *acc_out, void *stream);
+
+/*
  * Compensated FP64 reductions over bodies (scripts/scatter_field.py:759-769):
  * out[0] = kinetic energy sum m v^2 / 2, out[1..D] = momentum sum m v,
  * out[D+1] = mass sum, out[D+2] = PM potential energy sum m phi / 2 (phi may be NULL -> 0).
