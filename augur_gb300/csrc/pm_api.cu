@@ -33,7 +33,7 @@ struct augur_pm_plan {
   // deposit work items (row blocks split into body chunks) and partial fixed-point tiles
   int nblk;
   uint32_t *dep_nch, *dep_item_off, *dep_slot_off, *dep_counters, *dep_item_blk;
-  uint2 *dep_seg_tab;
+  uint4 *dep_seg_tab;
   size_t dep_items_max;
   unsigned long long *dep_scratch;
   size_t dep_slots;

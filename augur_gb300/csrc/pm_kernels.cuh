@@ -278,7 +278,7 @@ struct DepositArgs {
   FastDiv fdG, fdRR, fdRY;
 };
 
-// Calls f(first, last) for every contiguous run of sorted bodies that can touch row
+// Calls f(first, last, first_row_key) for every contiguous run of sorted bodies that can touch row
 // block b: base rows [y0-1, y0+RY-1] x [z0-1, z0+RZ-1] (periodic wrap), or base rows
 // y0-1 .. y0+RY-1 <-> keys y0 .. y0+RY for the isolated 2D grid.
 template <int D, class F>
@@ -290,7 +290,7 @@ __device__ __forceinline__ void block_segments(const DepositArgs &a, int b, cons
   const int z0 = (D == 3) ? (b / nyb) * RZ : 0;
   auto add = [&](uint32_t r0, uint32_t r1) {
     uint32_t lo = row_begin(start, tile_off, r0), hi = row_begin(start, tile_off, r1);
-    if (hi > lo) f(lo, hi);
+    if (hi > lo) f(lo, hi, r0);
   };
   auto ylist = [&](uint32_t rb) {
     if (RY < G) {
@@ -323,24 +323,24 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
                                                             const uint32_t *__restrict__ tile_off, DepositArgs a,
                                                             uint32_t *__restrict__ nch, uint32_t *__restrict__ item_off,
                                                             uint32_t *__restrict__ slot_off,
-                                                            uint2 *__restrict__ seg_tab, uint32_t *__restrict__ item_blk,
+                                                            uint4 *__restrict__ seg_tab, uint32_t *__restrict__ item_blk,
                                                             unsigned *__restrict__ err) {
   __shared__ uint32_t wsum[2][32];
   const int nb = a.nblk, tid = threadIdx.x, nt = blockDim.x;
   for (int b = tid; b < nb; b += nt) {
     uint32_t cnt = 0;
     int ns = 0;
-    uint2 *tab = seg_tab + (size_t)b * (MAXSEGB + 1);
-    block_segments<D>(a, b, start, tile_off, [&](uint32_t lo, uint32_t hi) {
+    uint4 *tab = seg_tab + (size_t)b * (MAXSEGB + 1);
+    block_segments<D>(a, b, start, tile_off, [&](uint32_t lo, uint32_t hi, uint32_t row0) {
       if (ns < MAXSEGB) {
-        tab[1 + ns] = make_uint2(lo, cnt);
+        tab[1 + ns] = make_uint4(lo, cnt, row0, 0u);
         ++ns;
         cnt += hi - lo;
       } else {
         set_err(err, AUGUR_ERRBIT_RANGE);
       }
     });
-    tab[0] = make_uint2((uint32_t)ns, cnt);
+    tab[0] = make_uint4((uint32_t)ns, cnt, 0u, 0u);
     nch[b] = cnt == 0 ? 1u : (cnt + a.chunk - 1) / a.chunk;
   }
   __syncthreads();
@@ -415,13 +415,14 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
                                                       float2 *__restrict__ spec_out, unsigned *__restrict__ err,
                                                       const uint32_t *__restrict__ item_off,
                                                       const uint32_t *__restrict__ slot_off,
-                                                      const uint2 *__restrict__ seg_tab,
+                                                      const uint4 *__restrict__ seg_tab,
                                                       const uint32_t *__restrict__ item_blk,
                                                       unsigned long long *__restrict__ scratch,
                                                       unsigned *__restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ long long s_beg[MAXSEGB];
   __shared__ long long s_pre[MAXSEGB + 1];
+  __shared__ uint32_t s_row[MAXSEGB];
   __shared__ int s_nseg, s_last;
 
   const GridParams &g = a.g;
@@ -442,15 +443,16 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   float *rows = reinterpret_cast<float *>(smem + (size_t)RR * RS * 8);
   float2 *tw = reinterpret_cast<float2 *>(smem + (size_t)RR * RS * 8 + (size_t)RR * RS * 4);
 
-  const uint2 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
+  const uint4 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
   if (tid <= MAXSEGB) {
-    uint2 t = tab[tid];
+    uint4 t = tab[tid];
     if (tid == 0) {
       s_nseg = (int)t.x;
       s_pre[t.x] = t.y;  // total
     } else if (tid - 1 < (int)tab[0].x) {
       s_beg[tid - 1] = t.x;
       s_pre[tid - 1] = t.y;
+      s_row[tid - 1] = t.z;
     }
   }
   for (int e = tid; e < RR * G; e += nt) acc[e] = 0ull;
@@ -463,67 +465,85 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   const long long f_lo = (long long)part * a.chunk;
   const long long f_hi = min(s_pre[nseg], f_lo + (long long)a.chunk);
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  int wseg = 0;  // segment of the warp's first body; only moves forward
 
-  for (long long f0 = f_lo + (long long)warp * 32; f0 < f_hi; f0 += (long long)nwarp * 32) {
-    const long long f = f0 + lane;
-    const bool valid = f < f_hi;
-    while (wseg + 1 < nseg && s_pre[wseg + 1] <= f0) ++wseg;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid) {
-      int sg = wseg;
-      while (sg + 1 < nseg && s_pre[sg + 1] <= f) ++sg;
-      p = pos4[s_beg[sg] + (f - s_pre[sg])];
-    }
-    int ix = 0, iy = 0, iz = 0;
-    float wx = 0.f, wy = 0.f, wz = 0.f;
-    bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, iy, wy, g.inv_h);
-    if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz, g.inv_h);
-    if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
-    const bool live = valid && ok && p.w > 0.f;
-    // x corners of this body: cells bx and bx1 of a row (periodic wrap or grid bounds)
-    int bx = ix, bx1 = ix + 1;
-    bool inx0 = true, inx1 = true;
-    if (g.periodic) {
-      bx = fwrap(ix, G);
-      bx1 = (bx + 1 == G) ? 0 : bx + 1;
-    } else {
-      inx0 = (ix >= 0) && (ix < G);
-      inx1 = (ix + 1 >= 0) && (ix + 1 < G);
-    }
-    const float wx0 = axis_w(wx, 0), wx1 = axis_w(wx, 1);
+  // One segment at a time: a segment is one base z row (one key range of sorted bodies), so
+  // which z corners of its bodies fall inside the block is the same for the whole segment.
+  for (int sg = 0; sg < nseg; ++sg) {
+    const long long s0 = max(f_lo, s_pre[sg]), s1 = min(f_hi, s_pre[sg + 1]);
+    if (s0 >= s1) continue;
+    const long long bias = s_beg[sg] - s_pre[sg];  // sorted body index = bias + f
+    int lzc[2] = {0, 0};
+    bool zin[2] = {true, false};
+    if (D == 3) {
+      const int bz = (int)(s_row[sg] / (uint32_t)G);
 #pragma unroll
-    for (int oy = 0; oy < 2; ++oy) {
+      for (int oz = 0; oz < 2; ++oz) {
+        int cz = bz + oz;
+        if (cz == G) cz = 0;
+        int lz = cz - z0;
+        if (lz < 0) lz += G;
+        lzc[oz] = lz;
+        zin[oz] = lz < RZ;
+      }
+    }
+    for (long long f0 = s0 + (long long)warp * 32; f0 < s1; f0 += (long long)nwarp * 32) {
+      const long long f = f0 + lane;
+      const bool valid = f < s1;
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (valid) p = pos4[bias + f];
+      int ix = 0, iy = 0, iz = 0;
+      float wx = 0.f, wy = 0.f, wz = 0.f;
+      bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, iy, wy, g.inv_h);
+      if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz, g.inv_h);
+      if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
+      const bool live = valid && ok && p.w > 0.f;
+      // x corners: cells bx and bx1 of a row (periodic wrap or grid bounds)
+      int bx = ix, bx1 = ix + 1;
+      bool inx0 = true, inx1 = true;
+      if (g.periodic) {
+        bx = fwrap(ix, G);
+        bx1 = (bx + 1 == G) ? 0 : bx + 1;
+      } else {
+        inx0 = (ix >= 0) && (ix < G);
+        inx1 = (ix + 1 >= 0) && (ix + 1 < G);
+      }
+      // y corners: local rows of the block
+      int lyc[2];
+      bool yin[2];
+      if (g.periodic) {
+        const int by = fwrap(iy, G);
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+          int cy = by + oy;
+          if (cy == G) cy = 0;
+          int ly = cy - y0;
+          if (ly < 0) ly += G;
+          lyc[oy] = ly;
+          yin[oy] = ly < RY;
+        }
+      } else {
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+          const int ly = iy + oy - y0;
+          lyc[oy] = ly;
+          yin[oy] = (ly >= 0) && (ly < RY) && (inx0 || inx1);
+        }
+      }
+      const float wx0 = axis_w(wx, 0), wx1 = axis_w(wx, 1);
 #pragma unroll
       for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz) {
-        // key identifies the (row, x pair) of this (y, z) corner pair; both x corners share it
-        unsigned key = 0xffffffffu;
-        uint32_t q0 = 0, q1 = 0;
-        int rowbase = 0;
-        if (live) {
-          bool in;
-          if (g.periodic) {
-            int cy = fwrap(iy + oy, G);
-            int ly = cy - y0;
-            if (ly < 0) ly += G;
-            int lz = 0;
-            if (D == 3) {
-              int cz = fwrap(iz + oz, G);
-              lz = cz - z0;
-              if (lz < 0) lz += G;
-            }
-            in = (ly < RY) && (lz < RZ);
-            rowbase = (lz * RY + ly) * G;
-            if (in) key = (unsigned)(rowbase + bx);
-          } else {
-            int ly = iy + oy - y0;
-            in = (ly >= 0) && (ly < RY) && (inx0 || inx1);
-            rowbase = ly * G;
-            if (in) key = (unsigned)(ly * (G + 1) + ix + 1);
-          }
-          if (in) {
+        if (!zin[oz]) continue;  // uniform across the warp
+        const float wzt = axis_w(wz, oz);
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+          // key identifies the (row, x pair) of this (y, z) corner pair; both x corners share it
+          unsigned key = 0xffffffffu;
+          uint32_t q0 = 0, q1 = 0;
+          const int rowbase = (lzc[oz] * RY + lyc[oy]) * G;
+          if (live && yin[oy]) {
+            key = g.periodic ? (unsigned)(rowbase + bx) : (unsigned)(lyc[oy] * (G + 1) + ix + 1);
             // weight order of the reference: ((w_x * w_y) * w_z) * m
-            const float wyt = axis_w(wy, oy), wzt = axis_w(wz, oz);
+            const float wyt = axis_w(wy, oy);
             float w0 = __fmul_rn(wx0, wyt), w1 = __fmul_rn(wx1, wyt);
             if (D == 3) {
               w0 = __fmul_rn(w0, wzt);
@@ -532,33 +552,25 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
             if (inx0) q0 = __float2uint_rz(__fmul_rn(__fmul_rn(__fmul_rn(w0, p.w), qs.qs1), qs.qs2));
             if (inx1) q1 = __float2uint_rz(__fmul_rn(__fmul_rn(__fmul_rn(w1, p.w), qs.qs1), qs.qs2));
           }
-        }
-        unsigned long long *r0 = nullptr, *r1 = nullptr;
-        if (key != 0xffffffffu) {
-          if (g.periodic) {
-            r0 = &acc[rowbase + bx];
-            r1 = &acc[rowbase + bx1];
-          } else {
-            r0 = inx0 ? &acc[rowbase + ix] : nullptr;
-            r1 = inx1 ? &acc[rowbase + ix + 1] : nullptr;
-          }
-        }
-        // warp aggregation only when neighbouring lanes share a key
-        unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
-        bool dup = (lane > 0) && (key != 0xffffffffu) && (prev == key);
-        if (__any_sync(0xffffffffu, dup)) {
-          unsigned peers = __match_any_sync(0xffffffffu, key);
-          if (key != 0xffffffffu) {
-            uint32_t s0 = __reduce_add_sync(peers, q0);
-            uint32_t s1 = __reduce_add_sync(peers, q1);
-            if (lane == __ffs(peers) - 1) {
-              if (r0 && s0) atomicAdd(r0, (unsigned long long)s0);
-              if (r1 && s1) atomicAdd(r1, (unsigned long long)s1);
+          const int c0 = g.periodic ? rowbase + bx : rowbase + ix;
+          const int c1 = g.periodic ? rowbase + bx1 : rowbase + ix + 1;
+          // warp aggregation only when neighbouring lanes share a key
+          const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+          const bool dup = (lane > 0) && (key != 0xffffffffu) && (prev == key);
+          if (__any_sync(0xffffffffu, dup)) {
+            const unsigned peers = __match_any_sync(0xffffffffu, key);
+            if (key != 0xffffffffu) {
+              const uint32_t s0q = __reduce_add_sync(peers, q0);
+              const uint32_t s1q = __reduce_add_sync(peers, q1);
+              if (lane == __ffs(peers) - 1) {
+                if (s0q) atomicAdd(&acc[c0], (unsigned long long)s0q);
+                if (s1q) atomicAdd(&acc[c1], (unsigned long long)s1q);
+              }
             }
+          } else if (key != 0xffffffffu) {
+            if (q0) atomicAdd(&acc[c0], (unsigned long long)q0);
+            if (q1) atomicAdd(&acc[c1], (unsigned long long)q1);
           }
-        } else if (key != 0xffffffffu) {
-          if (r0 && q0) atomicAdd(r0, (unsigned long long)q0);
-          if (r1 && q1) atomicAdd(r1, (unsigned long long)q1);
         }
       }
     }
