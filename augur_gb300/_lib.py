@@ -23,6 +23,9 @@ SIGNATURES = {
     "augur_pm_plan_create": (_i32, [C.POINTER(_vp), _i32, _i32, _i64, _i32, _f64, _f64, _f64]),
     "augur_pm_plan_destroy": (_i32, [_vp]),
     "augur_pm_plan_workspace_bytes": (_i64, [_vp]),
+    "augur_pm_plan_get_tiles": (_i32, [_vp, _vp]),
+    "augur_pm_plan_set_tiles": (_i32, [_vp, _vp]),
+    "augur_pm_plan_bind_force_grid": (_i32, [_vp, _vp]),
     "augur_pm_cell_index": (_i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "augur_pm_deposit": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "augur_pm_poisson": (_i32, [_vp, _vp, _vp, _vp]),
@@ -55,6 +58,21 @@ SIGNATURES = {
     "augur_cnn_pack_dout": (_i32, [_vp, _i64, _f32, _vp, _vp]),
     "augur_cnn_gelu_bwd": (_i32, [_vp, _vp, _i64, _vp, _vp]),
 }
+
+
+
+class Tiles(C.Structure):
+    """augur_pm_tiles: launch geometry of a plan's kernels (results do not depend on it)."""
+    _fields_ = [("deposit_rows_y", C.c_int), ("deposit_rows_z", C.c_int), ("deposit_chunk", C.c_int),
+                ("green_tile_y", C.c_int), ("c2r_rows", C.c_int), ("fft_rows", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "Tiles":
+        return cls(**{k: int(d[k]) for k, _ in cls._fields_})
+
 
 _lib = None
 

@@ -56,6 +56,7 @@ class GridCNN:
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.adam_step = 0
         self._ws: dict = {}
+        self.keep_workspaces = True  # one workspace per (batch, grid, train); False keeps only the last
         self._partial = None
         self.prepare()
 
@@ -116,20 +117,31 @@ class GridCNN:
         if ws is None:
             nv = B * G ** 3
             bf = dict(dtype=torch.bfloat16, device=self.device)
-            ws = {"h": [torch.empty(nv * W, **bf) for _ in range(4)]}
             if train:
+                ws = {"h": [torch.empty(nv * W, **bf) for _ in range(4)]}
                 ws["z"] = [torch.empty(nv * W, **bf) for _ in range(4)]
                 ws["dh"] = [torch.empty(nv * W, dtype=torch.float32, device=self.device) for _ in range(2)]
                 ws["dz"] = [torch.empty(nv * W, **bf) for _ in range(2)]
                 ws["dout16"] = torch.empty(nv * 16, **bf)
-            self._ws = {key: ws}
+            else:
+                # inference keeps no activations for a backward pass: two buffers in turn
+                a, b = (torch.empty(nv * W, **bf) for _ in range(2))
+                ws = {"h": [a, b, a, b]}
+            if not self.keep_workspaces:
+                self._ws = {}
+            self._ws[key] = ws
         return ws
 
-    def input(self, rho: torch.Tensor, force4: torch.Tensor) -> torch.Tensor:
+    def release_workspaces(self) -> None:
+        self._ws = {}
+
+    def input(self, rho: torch.Tensor, force4: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """x (nvox, 2) bf16 = (log(1 + rho_scale * rho), phi_scale * phi) from the density grid and
-        the potential lane of the PM force grid."""
+        the potential lane of the PM force grid; written to out (nvox * 2 bf16) when given."""
         nv = rho.numel()
-        x = torch.empty(nv * 2, dtype=torch.bfloat16, device=self.device)
+        x = torch.empty(nv * 2, dtype=torch.bfloat16, device=self.device) if out is None else out
+        if x.numel() != nv * 2 or x.dtype != torch.bfloat16:
+            raise ValueError("out must hold nvox * 2 bf16 values")
         self._call("augur_cnn_input", rho.data_ptr(), force4.data_ptr(), nv, self.rho_scale, self.phi_scale,
                    x.data_ptr())
         return x

@@ -8,7 +8,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "pm_kernels.cuh"
@@ -24,7 +27,9 @@ struct augur_pm_plan {
   int L, M, Lt;  // transform length (G periodic, 2G isolated), half length, twiddle table length
   FftShape sh_M, sh_L;
   int dep_RY, dep_RZ, green_TY, c2r_RB, rows_RB, r2c_RB;
+  int dep_chunk_min;  // minimum bodies per deposit work item
   size_t smem_dep, smem_green, smem_c2r, smem_rows, smem_r2c;
+  size_t smem_max;  // the device's opt-in dynamic shared memory per block
   float2 *tw;
   float4 *pos4[2], *vel4[2];
   int cur;
@@ -37,9 +42,11 @@ struct augur_pm_plan {
   size_t dep_items_max;
   unsigned long long *dep_scratch;
   size_t dep_slots;
+  size_t dep_bytes;  // device bytes of the deposit tables (re-sized with the tile shape)
   int64_t cur_n;  // bodies in the sorted state
   float2 *spec, *spec3, *khat;
-  float4 *F4;
+  float4 *F4;      // force grid in use: F4_own, or a caller's buffer bound by augur_pm_plan_bind_force_grid
+  float4 *F4_own;
   float *real_tmp, *phi2d, *rho2d;
   int64_t run_n;
   float run_dt;
@@ -111,13 +118,14 @@ int dalloc(augur_pm_plan *p, T **ptr, size_t count) {
 
 unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-constexpr uint32_t DEP_CHUNK_MIN = 16384;
+constexpr int DEP_CHUNK_MIN = 2048;
 constexpr int DEP_THREADS = 256;
-uint32_t dep_chunk(int64_t n) {
+// bodies per deposit work item: at least the plan's minimum, and at most ~1024 chunks
+uint32_t dep_chunk(const augur_pm_plan *p, int64_t n) {
   int64_t c = (n + 1023) / 1024;
-  return (uint32_t)std::max<int64_t>(DEP_CHUNK_MIN, c);
+  return (uint32_t)std::max<int64_t>(p->dep_chunk_min, c);
 }
-size_t dep_slots_bound(int64_t n) { return (size_t)8 * (size_t)((n + dep_chunk(n) - 1) / dep_chunk(n)) + 1; }
+int64_t dep_nchunks(const augur_pm_plan *p, int64_t n) { return (n + dep_chunk(p, n) - 1) / dep_chunk(p, n); }
 
 cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
@@ -193,7 +201,7 @@ DepositArgs dep_args(const augur_pm_plan *p) {
   a.twmul = p->Lt / p->M;
   a.Lt = p->Lt;
   a.nblk = p->nblk;
-  a.chunk = dep_chunk(p->cur_n);
+  a.chunk = dep_chunk(p, p->cur_n);
   a.fdG = make_fastdiv(p->G);
   a.fdRR = make_fastdiv(a.RY * a.RZ);
   a.fdRY = make_fastdiv(a.RY);
@@ -207,7 +215,7 @@ int launch_deposit(augur_pm_plan *p, float *rho, float2 *spec, cudaStream_t st) 
   deposit_plan_kernel<D><<<1, 1024, 0, st>>>(p->row_start, p->tile_off, a, p->dep_nch, p->dep_item_off,
                                               p->dep_slot_off, p->dep_seg_tab, p->dep_item_blk, p->d_err);
   AUGUR_LAUNCH_CHECK(p);
-  const int64_t items = (int64_t)p->nblk + 4 * ((p->cur_n + a.chunk - 1) / a.chunk) + 1;
+  const int64_t items = (int64_t)p->nblk + 4 * dep_nchunks(p, p->cur_n) + 1;
   if ((size_t)items > p->dep_items_max) return AUGUR_ERANGE;
   deposit_kernel<D, MODE><<<(unsigned)items, DEP_THREADS, p->smem_dep, st>>>(
       p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
@@ -359,6 +367,125 @@ int gather_force(augur_pm_plan *p, const float4 *F4, int64_t n, float *acc, floa
   return AUGUR_OK;
 }
 
+// ---- tile shapes ----------------------------------------------------------------------
+
+augur_pm_tiles default_tiles(const augur_pm_plan *p) {
+  // measured on GB300 over Plummer / clumpy / disk scenes of 1e4..3e6 bodies: single-plane
+  // row blocks, small work items (more CTAs than SM slots even when the bodies concentrate)
+  augur_pm_tiles t;
+  const int G = p->G, L = p->L;
+  t.deposit_rows_y = G <= 64 ? 4 : (G <= 96 ? 8 : (G <= 256 ? 16 : 8));
+  t.deposit_rows_z = 1;
+  t.deposit_chunk = DEP_CHUNK_MIN;
+  t.green_tile_y = (3 * G * 16 * 8 <= 200000) ? 16 : 8;
+  t.c2r_rows = L <= 128 ? 32 : (L <= 512 ? 16 : 8);
+  t.fft_rows = L >= 4096 ? 1 : std::min(4096 / L, L <= 64 ? 16 : 64);
+  return t;
+}
+
+// Validates t against the plan's geometry and the device's shared memory; unless
+// check_only, stores it with the shared-memory sizes that follow from it.
+int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
+  const int G = p->G, M = p->M, L = p->L, Lt = p->Lt;
+  const bool d3 = p->dim == 3;
+  const int RY = t->deposit_rows_y, RZ = t->deposit_rows_z;
+  if (RY < 1 || RY > G || G % RY != 0) return AUGUR_EINVAL;
+  if (d3 ? (RZ < 1 || RZ > 15 || G % RZ != 0) : RZ != 1) return AUGUR_EINVAL;
+  if (t->deposit_chunk < 1024 || t->deposit_chunk > (1 << 24)) return AUGUR_EINVAL;
+  if (!(t->green_tile_y == 8 || t->green_tile_y == 16) || G % t->green_tile_y != 0) return AUGUR_EINVAL;
+  const int RB = t->c2r_rows;
+  if (RB < 1 || RB > 32 || (RB & (RB - 1)) != 0) return AUGUR_EINVAL;
+  if (d3 && ((G * G) % RB) != 0) return AUGUR_EINVAL;
+  if (t->fft_rows < 1 || t->fft_rows > 256) return AUGUR_EINVAL;
+  const size_t s_dep = (size_t)RY * RZ * (G + 2) * 12 + (size_t)Lt * 8;
+  const size_t s_green = (size_t)3 * G * t->green_tile_y * 8 + (size_t)Lt * 8;
+  const size_t s_c2r = (size_t)2 * RB * (M + 1) * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 + (size_t)Lt * 8;
+  const size_t s_rows = (size_t)2 * t->fft_rows * (L + 1) * 8 + (size_t)Lt * 8;
+  const size_t s_r2c = (size_t)3 * 16 * (M + 1) * 8 + (size_t)Lt * 8;
+  const size_t lim = p->smem_max;
+  if (s_dep > lim || s_green > lim || s_c2r > lim || s_rows > lim || s_r2c > lim) return AUGUR_EINVAL;
+  if (check_only) return AUGUR_OK;
+  p->dep_RY = RY;
+  p->dep_RZ = RZ;
+  p->dep_chunk_min = t->deposit_chunk;
+  p->green_TY = t->green_tile_y;
+  p->c2r_RB = RB;
+  p->rows_RB = t->fft_rows;
+  p->r2c_RB = 16;
+  p->smem_dep = s_dep;
+  p->smem_green = s_green;
+  p->smem_c2r = s_c2r;
+  p->smem_rows = s_rows;
+  p->smem_r2c = s_r2c;
+  return AUGUR_OK;
+}
+
+// Deposit work-item tables and partial-tile scratch for the plan's tile shape and body bound.
+int alloc_deposit_tables(augur_pm_plan *p) {
+  void *old[] = {p->dep_nch, p->dep_item_off, p->dep_slot_off, p->dep_counters, p->dep_item_blk, p->dep_seg_tab,
+                 p->dep_scratch};
+  for (void *q : old)
+    if (q) cudaFree(q);
+  p->dep_nch = p->dep_item_off = p->dep_slot_off = p->dep_counters = p->dep_item_blk = nullptr;
+  p->dep_seg_tab = nullptr;
+  p->dep_scratch = nullptr;
+  p->bytes -= p->dep_bytes;
+  const size_t bytes0 = p->bytes;
+  const int G = p->G;
+  p->nblk = (p->dim == 3) ? (G / p->dep_RY) * (G / p->dep_RZ) : G / p->dep_RY;
+  // chunks of any n <= max_n: ceil(n / max(chunk_min, ceil(n / 1024))) <= min(ceil(max_n / chunk_min), 1024)
+  const int64_t nch = std::min<int64_t>((p->max_n + p->dep_chunk_min - 1) / p->dep_chunk_min, 1024);
+  p->dep_slots = (size_t)8 * (size_t)nch + 1;
+  p->dep_items_max = (size_t)p->nblk + 4 * (size_t)nch + 1;
+  int rc = AUGUR_OK;
+  rc |= dalloc(p, &p->dep_nch, (size_t)p->nblk);
+  rc |= dalloc(p, &p->dep_item_off, (size_t)p->nblk + 1);
+  rc |= dalloc(p, &p->dep_slot_off, (size_t)p->nblk);
+  rc |= dalloc(p, &p->dep_counters, (size_t)p->nblk);
+  rc |= dalloc(p, &p->dep_item_blk, p->dep_items_max);
+  rc |= dalloc(p, &p->dep_seg_tab, (size_t)p->nblk * (MAXSEGB + 1));
+  rc |= dalloc(p, &p->dep_scratch, p->dep_slots * (size_t)p->dep_RY * p->dep_RZ * G);
+  p->dep_bytes = p->bytes - bytes0;
+  if (rc != AUGUR_OK) return AUGUR_ENOMEM;
+  if (cudaMemset(p->dep_counters, 0, sizeof(uint32_t) * p->nblk) != cudaSuccess) return AUGUR_ECUDA;
+  return AUGUR_OK;
+}
+
+// The dynamic shared-memory opt-in is a property of the kernel, shared by every plan in the
+// process: it is only ever raised, so that a plan with smaller tiles never lowers the limit
+// another plan's launches rely on.
+template <typename K>
+int raise_smem(K *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cur = done[{dev, (const void *)kernel}];
+  if (bytes <= cur) return AUGUR_OK;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return AUGUR_ECUDA;
+  }
+  cur = bytes;
+  return AUGUR_OK;
+}
+
+int raise_smem_limits(const augur_pm_plan *p) {
+  int rc = AUGUR_OK;
+  rc |= raise_smem(deposit_kernel<3, 0>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 1>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 2>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<2, 0>, p->smem_dep);
+  rc |= raise_smem(fft_z_green_kernel<16>, p->smem_green);
+  rc |= raise_smem(fft_z_green_kernel<8>, p->smem_green);
+  rc |= raise_smem(c2r_rows_kernel<true>, p->smem_c2r);
+  rc |= raise_smem(c2r_rows_kernel<false>, p->smem_c2r);
+  rc |= raise_smem(fft_rows_kernel, p->smem_rows);
+  rc |= raise_smem(r2c_rows_kernel, p->smem_r2c);
+  return rc ? AUGUR_ECUDA : AUGUR_OK;
+}
+
 int check_plan(const augur_pm_plan *p, int64_t n) {
   if (!p) return AUGUR_EINVAL;
   if (n < 0 || n > p->max_n) return AUGUR_EINVAL;
@@ -391,7 +518,7 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
   if (!p) return AUGUR_OK;
   void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
-                  p->F4, p->real_tmp, p->phi2d, p->rho2d, p->dep_nch, p->dep_item_off, p->dep_slot_off,
+                  p->F4_own, p->real_tmp, p->phi2d, p->rho2d, p->dep_nch, p->dep_item_off, p->dep_slot_off,
                   p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -444,31 +571,22 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
     delete p;
     return AUGUR_EINVAL;
   }
-  // tile shapes (the autotuner overrides these through augur_pm_plan_set_tiles)
-  p->dep_RY = 16;
-  if (dim == 3) {
-    int rr = 50000 / (12 * G);  // ~50 KB of shared memory: four 256-thread CTAs per SM
-    int rz = rr / 16;
-    if (rz < 1) {
-      rz = 1;
-      p->dep_RY = 8;
+  // default tile shapes (an autotuner may replace them through augur_pm_plan_set_tiles)
+  {
+    int dev = 0, smax = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+      cudaGetLastError();
+      smax = 232448;
     }
-    while (rz > 1 && (G % rz) != 0) --rz;
-    if (rz > G) rz = G;
-    p->dep_RZ = rz;
-  } else {
-    p->dep_RZ = 1;
+    p->smem_max = (size_t)smax;
   }
-  p->green_TY = (3 * G * 16 * 8 <= 200000) ? 16 : 8;
-  p->c2r_RB = (p->L <= 512) ? 16 : 8;
-  p->rows_RB = p->L >= 4096 ? 1 : 4096 / p->L;
-  p->r2c_RB = 16;
+  augur_pm_tiles t = default_tiles(p);
+  if (apply_tiles(p, &t, /*check_only=*/false) != AUGUR_OK) {
+    delete p;
+    return AUGUR_EINVAL;
+  }
   const int M = p->M, L = p->L, Lt = p->Lt;
-  p->smem_dep = (size_t)p->dep_RY * p->dep_RZ * (G + 2) * 12 + (size_t)Lt * 8;
-  p->smem_green = (size_t)3 * G * p->green_TY * 8 + (size_t)Lt * 8;
-  p->smem_c2r = (size_t)2 * p->c2r_RB * (M + 1) * 8 + (size_t)(g.periodic ? 4 : 1) * p->c2r_RB * L * 4 + (size_t)Lt * 8;
-  p->smem_rows = (size_t)2 * p->rows_RB * (L + 1) * 8 + (size_t)Lt * 8;
-  p->smem_r2c = (size_t)3 * p->r2c_RB * (M + 1) * 8 + (size_t)Lt * 8;
 
   int rc = AUGUR_OK;
   const int64_t N = max_bodies;
@@ -488,17 +606,9 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   rc |= dalloc(p, &p->d_err, 1);
   rc |= dalloc(p, &p->d_mmax, 1);
   rc |= dalloc(p, &p->spec, nspec);
-  rc |= dalloc(p, &p->F4, ncell);
-  p->nblk = (dim == 3) ? (G / p->dep_RY) * (G / p->dep_RZ) : G / p->dep_RY;
-  p->dep_slots = dep_slots_bound(N);
-  rc |= dalloc(p, &p->dep_nch, (size_t)p->nblk);
-  rc |= dalloc(p, &p->dep_item_off, (size_t)p->nblk + 1);
-  rc |= dalloc(p, &p->dep_slot_off, (size_t)p->nblk);
-  rc |= dalloc(p, &p->dep_counters, (size_t)p->nblk);
-  p->dep_items_max = (size_t)p->nblk + 4 * (size_t)((N + dep_chunk(N) - 1) / dep_chunk(N)) + 1;
-  rc |= dalloc(p, &p->dep_item_blk, p->dep_items_max);
-  rc |= dalloc(p, &p->dep_seg_tab, (size_t)p->nblk * (MAXSEGB + 1));
-  rc |= dalloc(p, &p->dep_scratch, p->dep_slots * (size_t)p->dep_RY * p->dep_RZ * G);
+  rc |= dalloc(p, &p->F4_own, ncell);
+  p->F4 = p->F4_own;
+  rc |= alloc_deposit_tables(p);
   if (dim == 3) {
     rc |= dalloc(p, &p->spec3, 4 * nspec);
   } else {
@@ -515,7 +625,6 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   cudaMemset(p->row_start, 0, sizeof(uint32_t) * (size_t)(p->ntiles + 1) * SCAN_TILE);
   cudaMemset(p->d_err, 0, sizeof(unsigned));
   cudaMemset(p->d_mmax, 0, sizeof(unsigned));
-  cudaMemset(p->dep_counters, 0, sizeof(uint32_t) * p->nblk);
   // twiddles exp(-2 pi i t / Lt) in double, rounded once to float
   std::vector<float2> tw(Lt);
   for (int t = 0; t < Lt; ++t) {
@@ -526,18 +635,7 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
     augur_pm_plan_destroy(p);
     return AUGUR_ECUDA;
   }
-  // dynamic shared memory opt-in
-  cudaFuncSetAttribute(deposit_kernel<3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
-  cudaFuncSetAttribute(deposit_kernel<3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
-  cudaFuncSetAttribute(deposit_kernel<3, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
-  cudaFuncSetAttribute(deposit_kernel<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_dep);
-  cudaFuncSetAttribute(fft_z_green_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
-  cudaFuncSetAttribute(fft_z_green_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_green);
-  cudaFuncSetAttribute(c2r_rows_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
-  cudaFuncSetAttribute(c2r_rows_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_c2r);
-  cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_rows);
-  cudaFuncSetAttribute(r2c_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem_r2c);
-  if (cudaGetLastError() != cudaSuccess) {
+  if (raise_smem_limits(p) != AUGUR_OK) {
     augur_pm_plan_destroy(p);
     return AUGUR_ECUDA;
   }
@@ -713,6 +811,40 @@ int augur_pm_run_grid(augur_pm_plan *p, float *rho_out, int with_phi, void *stre
 }
 
 float *augur_pm_force_grid(augur_pm_plan *p) { return p ? reinterpret_cast<float *>(p->F4) : nullptr; }
+
+int augur_pm_plan_get_tiles(const augur_pm_plan *p, augur_pm_tiles *out) {
+  if (!p || !out) return AUGUR_EINVAL;
+  out->deposit_rows_y = p->dep_RY;
+  out->deposit_rows_z = p->dep_RZ;
+  out->deposit_chunk = p->dep_chunk_min;
+  out->green_tile_y = p->green_TY;
+  out->c2r_rows = p->c2r_RB;
+  out->fft_rows = p->rows_RB;
+  return AUGUR_OK;
+}
+
+int augur_pm_plan_set_tiles(augur_pm_plan *p, const augur_pm_tiles *t) {
+  if (!p || !t) return AUGUR_EINVAL;
+  int rc = apply_tiles(p, t, true);
+  if (rc) return rc;
+  const bool realloc_dep = t->deposit_rows_y != p->dep_RY || t->deposit_rows_z != p->dep_RZ ||
+                           t->deposit_chunk != p->dep_chunk_min;
+  if (realloc_dep && cudaDeviceSynchronize() != cudaSuccess) return AUGUR_ECUDA;
+  apply_tiles(p, t, false);
+  if (realloc_dep) {
+    rc = alloc_deposit_tables(p);
+    if (rc) return rc;
+  }
+  return raise_smem_limits(p);
+}
+
+int augur_pm_plan_bind_force_grid(augur_pm_plan *p, float *grid4) {
+  if (!p) return AUGUR_EINVAL;
+  if (p->dim != 3 || p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
+  if (grid4 && (reinterpret_cast<uintptr_t>(grid4) & 15) != 0) return AUGUR_EINVAL;
+  p->F4 = grid4 ? reinterpret_cast<float4 *>(grid4) : p->F4_own;
+  return AUGUR_OK;
+}
 
 int augur_pm_run_kick(augur_pm_plan *p, float kick, int drift, float *acc_out, double *energy_out, float esync,
                       void *stream) {

@@ -59,7 +59,7 @@ class PMPlan:
     """
 
     def __init__(self, dim: int, grid: int, max_bodies: int, mode: str = "periodic", extent: float = 1.0,
-                 eps: float = 0.5, g_newton: float = 1.0, device=None):
+                 eps: float = 0.5, g_newton: float = 1.0, device=None, tiles="cache"):
         self.lib = _lib.load()
         self.dim, self.grid, self.max_bodies = int(dim), int(grid), int(max_bodies)
         self.mode, self.extent, self.eps, self.g_newton = mode, float(extent), float(eps), float(g_newton)
@@ -72,6 +72,14 @@ class PMPlan:
             rc = self.lib.augur_pm_plan_create(C.byref(self._p), self.dim, self.grid, self.max_bodies,
                                                MODES[mode], self.extent, self.eps, self.g_newton)
         _lib.check(rc, "augur_pm_plan_create")
+        # tiles: "cache" = the autotuner's measured shapes for this grid and body count when the
+        # cache has them (periodic 3D), None = the library's defaults, or a dict of shapes
+        if tiles == "cache" and self.dim == 3 and mode == "periodic":
+            from . import autotune
+
+            tiles = autotune.cached_tiles(self.grid, self.max_bodies)
+        if isinstance(tiles, dict) and tiles:
+            self.set_tiles(tiles)
 
     # ---- lifetime --------------------------------------------------------------------
     def close(self) -> None:
@@ -90,6 +98,30 @@ class PMPlan:
     @property
     def workspace_bytes(self) -> int:
         return int(self.lib.augur_pm_plan_workspace_bytes(self._p))
+
+    @property
+    def tiles(self) -> dict:
+        """The kernels' tile shapes (augur_pm_tiles as a dict)."""
+        t = _lib.Tiles()
+        _lib.check(self.lib.augur_pm_plan_get_tiles(self._p, C.byref(t)), "augur_pm_plan_get_tiles")
+        return t.as_dict()
+
+    def set_tiles(self, tiles: dict) -> None:
+        """Apply tile shapes (keys of augur_pm_tiles; missing keys keep their value). Outputs do not
+        depend on them. Synchronises the device when the deposit shape changes."""
+        cur = self.tiles
+        cur.update(tiles)
+        with torch.cuda.device(self.device):
+            rc = self.lib.augur_pm_plan_set_tiles(self._p, C.byref(_lib.Tiles.from_dict(cur)))
+        _lib.check(rc, "augur_pm_plan_set_tiles")
+
+    def bind_force_grid(self, grid4: torch.Tensor | None) -> None:
+        """Use grid4 ((G, G, G, 4) float32 CUDA tensor, e.g. one slice of a batched grid) as the force
+        grid of the run loop; None returns to the plan's own grid."""
+        if grid4 is not None:
+            _need(grid4, "grid4", shape=self.grid_shape + (4,), device=self.device)
+        self._bound = grid4
+        _lib.check(self.lib.augur_pm_plan_bind_force_grid(self._p, _ptr(grid4)), "augur_pm_plan_bind_force_grid")
 
     @property
     def last_launches(self) -> int:

@@ -98,6 +98,46 @@ def wrap(pos, box=1.0):
     return p.astype(np.float32)
 
 
+def plummer_device(pos_out, vel_out, seed: int, a: float = 0.05, rmax: float = 0.45, chunk: int = 1 << 25) -> None:
+    """The plummer() distribution sampled on the GPU into (n, 3) float32 CUDA tensors, chunk by
+    chunk, for scenes too large to build on the host (10^9 bodies). The truncation at rmax is
+    applied by drawing the enclosed-mass fraction from [0, M(rmax)) instead of by rejection, which
+    gives the same truncated distribution; speeds use the same rejection sampler. Seeded with
+    torch's device generator, so the bodies differ from plummer()'s for the same seed. Positions are
+    wrapped into the unit box like wrap()."""
+    import torch
+
+    n, dev = pos_out.shape[0], pos_out.device
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    f64 = dict(dtype=torch.float64, device=dev)
+    fmax = rmax ** 3 / (rmax ** 2 + a * a) ** 1.5
+    vfac = (2.0 / a) ** 0.5
+
+    def iso(m):
+        v = torch.randn(m, 3, generator=gen, **f64)
+        return v / v.norm(dim=1, keepdim=True)
+
+    for s0 in range(0, n, chunk):
+        m = min(chunk, n - s0)
+        u = torch.rand(m, generator=gen, **f64).clamp_(min=1e-300) * fmax
+        r = a / torch.sqrt(u.pow(-2.0 / 3.0) - 1.0)
+        q = torch.empty(m, **f64)
+        todo = torch.arange(m, device=dev)
+        while todo.numel():
+            k = todo.numel()
+            x4 = torch.rand(k, generator=gen, **f64)
+            x5 = torch.rand(k, generator=gen, **f64) * 0.1
+            ok = x5 < x4 * x4 * (1.0 - x4 * x4) ** 3.5
+            q[todo[ok]] = x4[ok]
+            todo = todo[~ok]
+        p = (r[:, None] * iso(m)).float()
+        p = torch.where(p >= 0.5, p - 1.0, p)
+        p = torch.where(p < -0.5, p + 1.0, p)
+        pos_out[s0:s0 + m] = p
+        vel_out[s0:s0 + m] = ((q * vfac * (1.0 + (r / a) ** 2) ** -0.25)[:, None] * iso(m)).float()
+
+
 def make_scene(kind: str, n: int, seed: int, box: float = 1.0):
     """(pos, vel, mass) float32 arrays of n bodies, centred in the periodic box."""
     rng = np.random.default_rng(seed)

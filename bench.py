@@ -155,6 +155,10 @@ def cpu_baseline_run(n, G, dt, budget_s=20.0):
 def run_reference(args, world, rank):
     if rank != 0:
         return
+    if args.workload != "pm":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm times the default 3M-body "
+                                                              "workload only"}), flush=True)
+        return
     n, G = args.bodies, args.grid
     cb = cpu_baseline_run(n, G, args.dt, budget_s=max(5.0, 60.0 / max(1, args.steps)))
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "body-steps/s", "n_gpus": world,
@@ -358,24 +362,243 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """64 independent scenes, N log-uniform in [1e4, 1e6], grids 64/96/128 at ~8 cells per body,
+    stepped together by CUDA-graph replay (two merged steps per replay); plain PM for all and the
+    CNN-corrected form for the 128^3 scenes (trained weights), beside the same scenes run one after
+    another without the graph. Replicas only under torchrun (each rank its own batch)."""
+    from augur_gb300 import PMPlan
+    from augur_gb300.batch import BatchedPM, make_batch
+    from augur_gb300.cnn import GridCNN
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    st = torch.cuda.current_stream(dev)
+    K = args.steps + (args.steps % 2)
+    W = args.warmup + (args.warmup % 2)
+    t0 = time.time()
+    batch = make_batch(64, 1e4, 1e6, seed=9100 + rank)
+    gen_s = time.time() - t0
+
+    def timed(fn):
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        fn()
+        b.record(st)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b)
+
+    # plain PM, all scenes in one graph
+    sim = BatchedPM(batch, dt=args.dt, streams=args.streams)
+    launches_per_step = 0
+    sim.begin()
+    launches_per_step = sum(s["plan"].last_launches for s in sim.scenes)
+    sim.steps(W)
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    ms_total = timed(lambda: sim.steps(K))
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    sim.end()
+    for s in sim.scenes:
+        s["plan"].check()
+    ms = ms_total / K
+    bodies = sim.bodies
+    nbytes = sum(step_bytes(s["n"], s["grid"]) for s in sim.scenes)
+    tiles_cached = sum(1 for s in sim.scenes if s["tuned"])
+    plain_err = sim.force_errors(ntarget=1024) if not args.no_accuracy else None
+    sim.close()
+
+    # the same scenes one after another on one stream, no graph
+    seq_ms = 0.0
+    for sc in batch:
+        plan = PMPlan(3, sc["grid"], sc["n"], "periodic", 1.0, device=dev)
+        from augur_gb300 import autotune
+        tl = autotune.tiles_for(sc["grid"], sc["n"])
+        if tl:
+            plan.set_tiles(tl)
+        p, v, m = (torch.from_numpy(x).to(dev) for x in (sc["pos"], sc["vel"], sc["mass"]))
+        plan.run_begin(p, v, m, dt=args.dt)
+        plan.run_steps(W)
+        seq_ms += timed(lambda: plan.run_steps(K))
+        plan.close()
+    seq_ms /= K
+
+    # CNN-corrected form on the scenes whose grid has trained weights
+    cnn = None
+    ck = ROOT / "augur_gb300" / "weights" / "scatter_cnn_g128.pt"
+    if ck.exists() and not args.no_cnn:
+        d = torch.load(ck, map_location="cpu", weights_only=False)
+        net = GridCNN(dev)
+        net.load_state_dict(d["net"])
+        simc = BatchedPM(batch, dt=args.dt, nets={int(d["grid"]): net}, streams=args.streams, check_every=10)
+        simc.begin()
+        simc.steps(W)
+        cms = timed(lambda: simc.steps(K)) / K
+        simc.end()
+        errs = simc.force_errors(ntarget=1024) if not args.no_accuracy else None
+        ncnn = sum(1 for s in simc.scenes if s["monitor"] is not None)
+        cnn = {"form": "CNN-corrected PM on the 128^3 scenes, plain PM on the others (no weights for 64^3/96^3)",
+               "value": bodies / (cms * 1e-3), "unit": "body-steps/s", "ms_per_step": cms,
+               "cnn_scenes": ncnn, "reverted_to_plain_pm": sum(1 for s in simc.scenes if s["monitor"] is not None
+                                                                and s["monitor"].reverted),
+               "monitor_check_every": 10, "per_scene_error": errs}
+        simc.close()
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+
+    def summary(rows, key):
+        v = [r[key] for r in rows if key in r]
+        return None if not v else {"mean": float(np.mean(v)), "max": float(np.max(v)), "scenes": len(v)}
+
+    line = {
+        "metric": "aggregate body-steps/s of 64 uneven periodic scenes stepped together", "value":
+            world * bodies / (ms * 1e-3), "unit": "body-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "64 scenes (plummer/uniform/clumpy/disk/flyby in turn), N log-uniform in [1e4, 1e6], "
+                               "grid 64/96/128 at >= 8 cells per body, leapfrog dt=%g, CUDA graph of 2 merged steps"
+                               % args.dt, "bodies": bodies, "seed": 9100,
+                   "grids": {str(g): sum(1 for s in batch if s["grid"] == g) for g in (64, 96, 128)},
+                   "streams": args.streams, "scene_generation_s": round(gen_s, 1),
+                   "l2": "per-step traffic %.2f GB > 129 MB L2; no flush" % (nbytes / 1e9)},
+        "form": "plain PM",
+        "step_roofline": {"bound": "hbm", "algorithmic_bytes": nbytes, "achieved": nbytes / (ms * 1e-3) / 1e9,
+                          "peak": peak, "unit": "GB/s", "frac": nbytes / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind},
+        "sequential_no_graph": {"value": bodies / (seq_ms * 1e-3), "ms_per_step": seq_ms,
+                                "what": "the same plans one after another on one stream, run_steps per scene"},
+        "gpu_launches": launches_per_step * K,
+        "tiles": {"autotuned_scenes": tiles_cached, "source": "augur_gb300/tiles_gb300.json"},
+        "clocks": clk,
+        "accuracy_plain_pm": None if plain_err is None else {
+            "vs": "FP64 periodic direct sum (min-image + Ewald), eps=1/256, 1024 sampled bodies per scene, "
+                  "state after the run", "rel_rms": summary(plain_err, "plain_pm"), "per_scene": plain_err},
+        "cnn_corrected": cnn,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_1e9(args, world, rank, local):
+    """One 10^9-body Plummer sphere on a 1024^3 grid, generated on the GPU; 20 merged steps timed;
+    force error at 4096 targets vs the FP64 periodic direct sum over a 10^6-body subsample."""
+    from augur_gb300 import PMPlan, direct_sum_fp64, scenes
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n, G, dt = args.bodies, args.grid, args.dt
+    st = torch.cuda.current_stream(dev)
+    t0 = time.time()
+    pos = torch.empty(n, 3, device=dev)
+    vel = torch.empty(n, 3, device=dev)
+    scenes.plummer_device(pos, vel, seed=9100 + rank)
+    mass = torch.full((n,), 1.0 / n, device=dev)
+    mask = torch.ones(n, device=dev)
+    torch.cuda.synchronize(dev)
+    gen_s = time.time() - t0
+    plan = PMPlan(3, G, n, "periodic", 1.0, device=dev)
+    acc = None
+    if not args.no_accuracy:
+        # the sub-op path (deposit, Poisson solve, gather at the targets) before the run is loaded
+        ns, nt = 1_000_000, 4096
+        g = torch.Generator(device=dev)
+        g.manual_seed(9300)
+        sub = torch.randint(0, n, (ns,), device=dev, generator=g)
+        src = pos[sub].double().contiguous()
+        rho = plan.deposit(pos, mass, mask)
+        F4 = plan.poisson(rho)
+        del rho
+        pm = plan.gather(F4, pos[sub[:nt]].contiguous())[0]
+        del F4
+        torch.cuda.empty_cache()
+        truth = direct_sum_fp64(src[:nt].contiguous(), src, torch.full((ns,), 1.0 / ns, dtype=torch.float64,
+                                device=dev), eps=1.0 / G, box=1.0,
+                                target_index=torch.arange(nt, device=dev, dtype=torch.int64))
+        acc = force_error(pm, truth)
+        acc["vs"] = ("FP64 periodic direct sum (min-image + Ewald), eps=1/%d, over a 10^6-body random subsample "
+                     "(masses scaled to the total), %d targets; the subsample's shot noise is part of the error" % (G, nt))
+        del src, sub
+    plan.run_begin(pos, vel, mass, mask, dt=dt)
+    plan.run_steps(args.warmup)
+    torch.cuda.synchronize(dev)
+    clocks = Clocks(local)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    plan.run_steps(args.steps)
+    b.record(st)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    ms = a.elapsed_time(b) / args.steps
+    launches = plan.last_launches
+    stages = plan.run_profile(2)
+    plan.check()
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    B = step_bytes(n, G)
+    sb = stage_bytes(n, G)
+    dom = max(stages, key=stages.get)
+    ach = sb[dom] / (stages[dom] * 1e-3) / 1e9 if sb[dom] else None
+    line = {
+        "metric": "body-steps/s, one 1e9-body scene", "value": world * n / (ms * 1e-3), "unit": "body-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain PM step, {n}-body Plummer sphere (a=0.05, generated on the GPU) in a unit "
+                               f"periodic box, {G}^3 FP32 grid, leapfrog dt={dt}", "bodies": n, "grid": G,
+                   "scene_generation_s": round(gen_s, 1), "workspace_gb": plan.workspace_bytes / 1e9,
+                   "l2": "per-step traffic %.0f GB >> L2; no flush" % (B / 1e9)},
+        "form": "plain PM",
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": None if ach is None else ach / peak, "peak_kind": peak_kind, "algorithmic_bytes": sb[dom]},
+        "step_roofline": {"bound": "hbm", "algorithmic_bytes": B, "achieved": B / (ms * 1e-3) / 1e9, "peak": peak,
+                          "unit": "GB/s", "frac": B / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind},
+        "stages_ms": stages, "gpu_launches": launches, "clocks": clk, "accuracy": acc,
+        "e2e": None, "e2e_note": "not measured: the 24 GB body state does not round-trip through host memory per step",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--workload", choices=("pm", "batch64", "pm1e9"), default="pm",
+                    help="pm: one 3M-body scene on 256^3 (default); batch64: 64 uneven scenes in one graph; "
+                         "pm1e9: one 1e9-body scene on 1024^3")
+    ap.add_argument("--streams", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--bodies", type=int, default=3_000_000)
-    ap.add_argument("--grid", type=int, default=256)
-    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--bodies", type=int, default=None)
+    ap.add_argument("--grid", type=int, default=None)
+    ap.add_argument("--dt", type=float, default=None)
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-cnn", action="store_true")
     ap.add_argument("--scene", default="plummer", choices=("plummer", "uniform", "clumpy", "disk", "flyby"))
     args = ap.parse_args()
+    defaults = {"pm": (2000, 3_000_000, 256, 5e-4), "batch64": (100, None, None, 5e-4),
+                "pm1e9": (20, 1_000_000_000, 1024, 2.5e-4)}[args.workload]
+    for k, v in zip(("steps", "bodies", "grid", "dt"), defaults):
+        if getattr(args, k) is None:
+            setattr(args, k, v)
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "batch64":
+        run_batch(args, world, rank, local)
+    elif args.workload == "pm1e9":
+        run_1e9(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
 

@@ -68,6 +68,38 @@ int augur_pm_plan_destroy(augur_pm_plan *plan);
 int64_t augur_pm_plan_workspace_bytes(const augur_pm_plan *plan);
 
 /*
+ * Tile shapes of the plan's kernels. They change the launch geometry only: every output
+ * is bit-identical for any valid shape (the deposit sums in fixed point, the transforms
+ * do the same arithmetic per row), so an autotuner may pick them by speed alone.
+ * No counterpart in the reference, whose kernels are cuFFT's and torch's own.
+ */
+typedef struct augur_pm_tiles {
+  int deposit_rows_y; /* y rows per deposit row block; divides grid */
+  int deposit_rows_z; /* z planes per deposit row block; 3D: 1..15 dividing grid, 2D: 1 */
+  int deposit_chunk;  /* minimum bodies per deposit work item, 1024 .. 2^24 */
+  int green_tile_y;   /* y columns per z-transform + Green block: 8 or 16, divides grid */
+  int c2r_rows;       /* x rows per C2R block: power of two <= 32 */
+  int fft_rows;       /* rows per y-transform block: 1..256 */
+} augur_pm_tiles;
+
+int augur_pm_plan_get_tiles(const augur_pm_plan *plan, augur_pm_tiles *out);
+/*
+ * Validates the shapes against the grid and the device's shared memory (AUGUR_EINVAL if
+ * one does not fit) and applies them. A new deposit shape re-sizes the deposit tables:
+ * that synchronises the device, so call it outside stream capture, between runs.
+ */
+int augur_pm_plan_set_tiles(augur_pm_plan *plan, const augur_pm_tiles *tiles);
+
+/*
+ * Periodic 3D plans: use the caller's device buffer (grid^3 float4, 16-byte aligned) as
+ * the force grid that run_grid writes and run_kick reads, so that several plans can fill
+ * the slices of one batched (B, G, G, G, 4) grid that a network then edits in one launch;
+ * NULL returns to the plan's own grid. The caller keeps the buffer alive while bound.
+ * No counterpart in the reference (its batch shares one grid tensor, scatter_field.py:779-794).
+ */
+int augur_pm_plan_bind_force_grid(augur_pm_plan *plan, float *grid4);
+
+/*
  * CIC base cell and fraction, bit-exact with ScatterField._corners
  * (scripts/scatter_field.py:179-182): u = (x + extent/2) / h - 0.5 in IEEE float32
  * (round-to-nearest, true division by float32(h)), i0 = floor(u), w = u - i0.
@@ -138,7 +170,9 @@ int augur_pm_run(augur_pm_plan *plan, float *pos, float *vel, const float *mass,
 /*
  * Split form of augur_pm_run, for callers that time or graph-capture single steps:
  * run_begin loads and sorts the bodies and applies the opening half kick; run_steps
- * advances k merged kick-drift steps (no host synchronisation, capture-safe);
+ * advances k merged kick-drift steps (no host synchronisation, capture-safe; every step
+ * swaps the plan's two body buffers, so a captured graph replays correctly when it holds
+ * an even number of steps);
  * run_end applies the closing half kick and writes pos/vel (and acc_out if not NULL)
  * back in the caller's order.
  */
