@@ -64,7 +64,8 @@ SIGNATURES = {
 class Tiles(C.Structure):
     """augur_pm_tiles: launch geometry of a plan's kernels (results do not depend on it)."""
     _fields_ = [("deposit_rows_y", C.c_int), ("deposit_rows_z", C.c_int), ("deposit_chunk", C.c_int),
-                ("green_tile_y", C.c_int), ("c2r_rows", C.c_int), ("fft_rows", C.c_int)]
+                ("green_tile_y", C.c_int), ("c2r_rows", C.c_int), ("fft_rows", C.c_int),
+                ("deposit_aggregate", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

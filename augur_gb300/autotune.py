@@ -46,6 +46,7 @@ def candidates(grid: int) -> dict:
     return {
         "deposit": [{"deposit_rows_y": ry, "deposit_rows_z": rz} for ry, rz in dep],
         "deposit_chunk": [{"deposit_chunk": c} for c in (1024, 2048, 4096, 8192, 16384, 65536)],
+        "deposit_aggregate": [{"deposit_aggregate": a} for a in (0, 1)],
         "green_tile_y": [{"green_tile_y": t} for t in (8, 16) if G % t == 0],
         "c2r_rows": [{"c2r_rows": r} for r in (2, 4, 8, 16, 32)],
         "fft_rows": [{"fft_rows": r} for r in sorted({max(1, min(256, base * f // 4)) for f in (1, 2, 4, 8)})],

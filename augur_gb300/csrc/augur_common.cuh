@@ -109,6 +109,14 @@ struct FftShape {
   int radix[12];
 };
 
+// Row-mode shared-memory layout of the stages between the first load and the last store:
+// element e of a row sits at fft_pad(e) = e + e/16, so the stride-R stores of a radix-R
+// stage (R = 16: every thread of a row on the same bank) spread over the banks. A row
+// needs fft_row_stride(L) float2 (odd count past the padding, so rows start on different
+// banks too).
+__host__ __device__ constexpr int fft_pad(int e) { return e + (e >> 4); }
+__host__ __device__ constexpr int fft_row_stride(int L) { return L + (L >> 4) + 1; }
+
 template <int R>
 __device__ __forceinline__ void dft(float2 *v, bool inv) {
   if constexpr (R == 2) {
@@ -217,64 +225,6 @@ constexpr int fft_ns(int L, int s) {
   return ns;
 }
 
-// COLS == 0: nb rows of L contiguous elements, row stride bs (batch index slow).
-// COLS > 0 : COLS interleaved columns, element e of column b at buf[e*COLS + b].
-template <int R, int L, int NS, int COLS>
-__device__ __forceinline__ void fft_stage_t(const float2 *__restrict__ in, float2 *__restrict__ out, int nb, int bs,
-                                            const float2 *__restrict__ tw, int twmul, bool inv) {
-  constexpr int nbf = L / R;
-  constexpr int tstride = L / (NS * R);
-  const int total = (COLS > 0 ? COLS : nb) * nbf;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    int b, j;
-    if constexpr (COLS > 0) {
-      j = idx / COLS;
-      b = idx - j * COLS;
-    } else {
-      b = idx / nbf;
-      j = idx - b * nbf;
-    }
-    const float2 *src;
-    float2 *dst;
-    constexpr int es = COLS > 0 ? COLS : 1;
-    if constexpr (COLS > 0) {
-      src = in + b;
-      dst = out + b;
-    } else {
-      src = in + (size_t)b * bs;
-      dst = out + (size_t)b * bs;
-    }
-    float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = src[(j + r * nbf) * es];
-    const int k = j % NS;
-    if constexpr (NS > 1) {
-#pragma unroll
-      for (int r = 1; r < R; ++r) {
-        float2 t = tw[r * k * tstride * twmul];
-        if (inv) t.y = -t.y;
-        v[r] = cmul(v[r], t);
-      }
-    }
-    dft<R>(v, inv);
-    const int base = (j - k) * R + k;
-#pragma unroll
-    for (int r = 0; r < R; ++r) dst[(base + r * NS) * es] = v[r];
-  }
-}
-
-template <int L, int COLS, int S = 0>
-__device__ __forceinline__ float2 *fft_t(float2 *in, float2 *out, int nb, int bs, const float2 *tw, int twmul,
-                                         bool inv) {
-  if constexpr (S < fft_nstages(L)) {
-    fft_stage_t<fft_radix(L, S), L, fft_ns(L, S), COLS>(in, out, nb, bs, tw, twmul, inv);
-    __syncthreads();
-    return fft_t<L, COLS, S + 1>(out, in, nb, bs, tw, twmul, inv);
-  } else {
-    return in;
-  }
-}
-
 // ---------------------------------------------------------------------------------
 // Transform with caller-supplied first load and last store: stage 0 reads element e of
 // transform b through ld(b, e), the last stage writes through st(b, e, value), and the
@@ -324,10 +274,10 @@ __device__ __forceinline__ void fft_io_rec(int nb, LD &ld, ST &st, float2 *in, f
   constexpr int NSTG = fft_nstages(L);
   constexpr int R = fft_radix(L, S);
   constexpr int NS = fft_ns(L, S);
-  auto sld = [&](int b, int e) -> float2 { return COLS > 0 ? in[e * COLS + b] : in[b * bs + e]; };
+  auto sld = [&](int b, int e) -> float2 { return COLS > 0 ? in[e * COLS + b] : in[b * bs + fft_pad(e)]; };
   auto sst = [&](int b, int e, float2 v) {
     if (COLS > 0) out[e * COLS + b] = v;
-    else out[b * bs + e] = v;
+    else out[b * bs + fft_pad(e)] = v;
   };
   if constexpr (NSTG == 1) {
     fft_stage_io<R, L, NS, COLS>(nb, ld, st, tw, twmul, inv);
@@ -384,30 +334,6 @@ inline bool fft_length_supported(int L) {
     AUGUR_FFT_LENGTHS(AUGUR_CASE)
 #undef AUGUR_CASE
     default: return false;
-  }
-}
-
-// Row transforms: nb rows of length L, row stride bs. Returns the result buffer.
-__device__ __forceinline__ float2 *fft_rows(int L, float2 *a, float2 *b, int nb, int bs, const float2 *tw, int twmul,
-                                            bool inv) {
-  switch (L) {
-#define AUGUR_CASE(N) \
-  case N: return fft_t<N, 0>(a, b, nb, bs, tw, twmul, inv);
-    AUGUR_FFT_LENGTHS(AUGUR_CASE)
-#undef AUGUR_CASE
-    default: return nullptr;
-  }
-}
-
-// Column transforms: COLS interleaved columns of length L.
-template <int COLS>
-__device__ __forceinline__ float2 *fft_cols(int L, float2 *a, float2 *b, const float2 *tw, int twmul, bool inv) {
-  switch (L) {
-#define AUGUR_CASE(N) \
-  case N: return fft_t<N, COLS>(a, b, COLS, 0, tw, twmul, inv);
-    AUGUR_FFT_LENGTHS(AUGUR_CASE)
-#undef AUGUR_CASE
-    default: return nullptr;
   }
 }
 

@@ -28,6 +28,7 @@ struct augur_pm_plan {
   FftShape sh_M, sh_L;
   int dep_RY, dep_RZ, green_TY, c2r_RB, rows_RB, r2c_RB;
   int dep_chunk_min;  // minimum bodies per deposit work item
+  int dep_agg;        // warp-aggregated deposit atomics (dense cells)
   size_t smem_dep, smem_green, smem_c2r, smem_rows, smem_r2c;
   size_t smem_max;  // the device's opt-in dynamic shared memory per block
   float2 *tw;
@@ -217,9 +218,14 @@ int launch_deposit(augur_pm_plan *p, float *rho, float2 *spec, cudaStream_t st) 
   AUGUR_LAUNCH_CHECK(p);
   const int64_t items = (int64_t)p->nblk + 4 * dep_nchunks(p, p->cur_n) + 1;
   if ((size_t)items > p->dep_items_max) return AUGUR_ERANGE;
-  deposit_kernel<D, MODE><<<(unsigned)items, DEP_THREADS, p->smem_dep, st>>>(
-      p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
-      p->dep_item_blk, p->dep_scratch, p->dep_counters);
+  if (p->dep_agg)
+    deposit_kernel<D, MODE, true><<<(unsigned)items, DEP_THREADS, p->smem_dep, st>>>(
+        p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
+        p->dep_item_blk, p->dep_scratch, p->dep_counters);
+  else
+    deposit_kernel<D, MODE, false><<<(unsigned)items, DEP_THREADS, p->smem_dep, st>>>(
+        p->pos4[p->cur], p->d_mmax, a, p->tw, rho, spec, p->d_err, p->dep_item_off, p->dep_slot_off, p->dep_seg_tab,
+        p->dep_item_blk, p->dep_scratch, p->dep_counters);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -380,6 +386,7 @@ augur_pm_tiles default_tiles(const augur_pm_plan *p) {
   t.green_tile_y = (3 * G * 16 * 8 <= 200000) ? 16 : 8;
   t.c2r_rows = L <= 128 ? 32 : (L <= 512 ? 16 : 8);
   t.fft_rows = L >= 4096 ? 1 : std::min(4096 / L, L <= 64 ? 16 : 64);
+  t.deposit_aggregate = 0;
   return t;
 }
 
@@ -397,11 +404,14 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   if (RB < 1 || RB > 32 || (RB & (RB - 1)) != 0) return AUGUR_EINVAL;
   if (d3 && ((G * G) % RB) != 0) return AUGUR_EINVAL;
   if (t->fft_rows < 1 || t->fft_rows > 256) return AUGUR_EINVAL;
-  const size_t s_dep = (size_t)RY * RZ * (G + 2) * 12 + (size_t)Lt * 8;
+  if (t->deposit_aggregate != 0 && t->deposit_aggregate != 1) return AUGUR_EINVAL;
+  // shared memory of each kernel (layouts in pm_kernels.cuh; transform rows padded by fft_row_stride)
+  const size_t PM = (size_t)fft_row_stride(M), PL = (size_t)fft_row_stride(L);
+  const size_t s_dep = (size_t)RY * RZ * (2 * PM * 8 + (size_t)(G + 2) * 4) + (size_t)Lt * 8;
   const size_t s_green = (size_t)3 * G * t->green_tile_y * 8 + (size_t)Lt * 8;
-  const size_t s_c2r = (size_t)2 * RB * (M + 1) * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 + (size_t)Lt * 8;
-  const size_t s_rows = (size_t)2 * t->fft_rows * (L + 1) * 8 + (size_t)Lt * 8;
-  const size_t s_r2c = (size_t)3 * 16 * (M + 1) * 8 + (size_t)Lt * 8;
+  const size_t s_c2r = (size_t)2 * RB * PM * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 + (size_t)Lt * 8;
+  const size_t s_rows = (size_t)2 * t->fft_rows * PL * 8 + (size_t)Lt * 8;
+  const size_t s_r2c = (size_t)16 * ((M + 1) + 2 * PM) * 8 + (size_t)Lt * 8;
   const size_t lim = p->smem_max;
   if (s_dep > lim || s_green > lim || s_c2r > lim || s_rows > lim || s_r2c > lim) return AUGUR_EINVAL;
   if (check_only) return AUGUR_OK;
@@ -411,6 +421,7 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   p->green_TY = t->green_tile_y;
   p->c2r_RB = RB;
   p->rows_RB = t->fft_rows;
+  p->dep_agg = t->deposit_aggregate;
   p->r2c_RB = 16;
   p->smem_dep = s_dep;
   p->smem_green = s_green;
@@ -473,10 +484,14 @@ int raise_smem(K *kernel, size_t bytes) {
 
 int raise_smem_limits(const augur_pm_plan *p) {
   int rc = AUGUR_OK;
-  rc |= raise_smem(deposit_kernel<3, 0>, p->smem_dep);
-  rc |= raise_smem(deposit_kernel<3, 1>, p->smem_dep);
-  rc |= raise_smem(deposit_kernel<3, 2>, p->smem_dep);
-  rc |= raise_smem(deposit_kernel<2, 0>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 0, false>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 1, false>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 2, false>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<2, 0, false>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 0, true>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 1, true>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<3, 2, true>, p->smem_dep);
+  rc |= raise_smem(deposit_kernel<2, 0, true>, p->smem_dep);
   rc |= raise_smem(fft_z_green_kernel<16>, p->smem_green);
   rc |= raise_smem(fft_z_green_kernel<8>, p->smem_green);
   rc |= raise_smem(c2r_rows_kernel<true>, p->smem_c2r);
@@ -820,6 +835,7 @@ int augur_pm_plan_get_tiles(const augur_pm_plan *p, augur_pm_tiles *out) {
   out->green_tile_y = p->green_TY;
   out->c2r_rows = p->c2r_RB;
   out->fft_rows = p->rows_RB;
+  out->deposit_aggregate = p->dep_agg;
   return AUGUR_OK;
 }
 

@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
 // writes its fixed-point tile to scratch and the CTA that finishes last (counter +
 // threadfence, no waiting) adds the others' tiles before converting.
 // ---------------------------------------------------------------------------------
-template <int D, int MODE>
+template <int D, int MODE, bool AGG>
 __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restrict__ pos4,
                                                       const unsigned *__restrict__ mmax_bits, DepositArgs a,
                                                       const float2 *__restrict__ twg, float *__restrict__ rho_out,
@@ -436,12 +436,14 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   const int nyb = G / RY;
   const int y0 = (blk % nyb) * RY;
   const int z0 = (D == 3) ? (blk / nyb) * RZ : 0;
-  const int RS = G + 2;  // fp32 row stride (keeps complex rows 8-byte aligned and padded)
+  const int RS = G + 2;                       // fp32 row stride (complex rows 8-byte aligned and padded)
+  const int PS = fft_row_stride(G / 2);       // padded transform rows
+  const size_t region = (size_t)RR * 2 * PS * 8;  // >= RR * G * 8: accumulator, then transform scratch
 
-  // [accumulator / transform scratch: RR*(G+2)*8 bytes][fp32 rows: RR*RS*4][twiddles]
+  // [accumulator / transform scratch: region][fp32 rows: RR*RS*4][twiddles]
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem);
-  float *rows = reinterpret_cast<float *>(smem + (size_t)RR * RS * 8);
-  float2 *tw = reinterpret_cast<float2 *>(smem + (size_t)RR * RS * 8 + (size_t)RR * RS * 4);
+  float *rows = reinterpret_cast<float *>(smem + region);
+  float2 *tw = reinterpret_cast<float2 *>(smem + region + (size_t)RR * RS * 4);
 
   const uint4 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
   if (tid <= MAXSEGB) {
@@ -554,10 +556,16 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
           }
           const int c0 = g.periodic ? rowbase + bx : rowbase + ix;
           const int c1 = g.periodic ? rowbase + bx1 : rowbase + ix + 1;
-          // warp aggregation only when neighbouring lanes share a key
-          const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
-          const bool dup = (lane > 0) && (key != 0xffffffffu) && (prev == key);
-          if (__any_sync(0xffffffffu, dup)) {
+          // AGG: warp aggregation when neighbouring lanes share a key (pays off only for cells
+          // dense enough that many lanes of a warp hit the same one; otherwise the shared-memory
+          // atomics resolve the few collisions faster than the vote and match)
+          bool agg = false;
+          if constexpr (AGG) {
+            const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+            const bool dup = (lane > 0) && (key != 0xffffffffu) && (prev == key);
+            agg = __any_sync(0xffffffffu, dup);
+          }
+          if (agg) {
             const unsigned peers = __match_any_sync(0xffffffffu, key);
             if (key != 0xffffffffu) {
               const uint32_t s0q = __reduce_add_sync(peers, q0);
@@ -616,12 +624,12 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   const int M = G / 2, MS = M + 1;
   float2 *Z = reinterpret_cast<float2 *>(rows);
   float2 *TA = reinterpret_cast<float2 *>(smem);
-  float2 *TB = TA + (size_t)RR * MS;
+  float2 *TB = TA + (size_t)RR * PS;
   {
     const float2 *src = Z;
     auto ld = [&](int b, int e) -> float2 { return src[b * MS + e]; };
     auto st = [&](int b, int e, float2 v) { Z[b * MS + e] = v; };
-    AUGUR_FFT_IO(M, 0, RR, ld, st, TA, TB, MS, tw, a.twmul, false);
+    AUGUR_FFT_IO(M, 0, RR, ld, st, TA, TB, PS, tw, a.twmul, false);
   }
   // post-process X_k = (Z_k + conj Z_{M-k})/2 - i/2 W^k (Z_k - conj Z_{M-k}), k = 0..M
   const int tstep = a.Lt / G;
@@ -656,11 +664,11 @@ struct RowsArgs {
 __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__ in, RowsArgs a,
                                                        const float2 *__restrict__ twg, float2 *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB;
+  const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB, PS = fft_row_stride(M);
   float2 *A = reinterpret_cast<float2 *>(smem);
   float2 *B = A + (size_t)RB * MS;
-  float2 *C = B + (size_t)RB * MS;
-  float2 *tw = C + (size_t)RB * MS;
+  float2 *C = B + (size_t)RB * PS;
+  float2 *tw = C + (size_t)RB * PS;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = blockIdx.x * RB;
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
@@ -677,7 +685,7 @@ __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__
   {
     auto ld = [&](int b, int e) -> float2 { return A[b * MS + e]; };
     auto st = [&](int b, int e, float2 v) { Z[b * MS + e] = v; };
-    AUGUR_FFT_IO(M, 0, RB, ld, st, B, C, MS, tw, a.twmul, false);
+    AUGUR_FFT_IO(M, 0, RB, ld, st, B, C, PS, tw, a.twmul, false);
   }
   const int tstep = a.Lt / L;
   for (int e = tid; e < (M + 1) * RB; e += nt) {
@@ -699,7 +707,7 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data
                                                        FastDiv fdL, int twmul, int Lt,
                                                        const float2 *__restrict__ twg, int inverse) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int LS = L + 1;
+  const int LS = fft_row_stride(L);
   float2 *A = reinterpret_cast<float2 *>(smem);
   float2 *B = A + (size_t)RB * LS;
   float2 *tw = B + (size_t)RB * LS;
@@ -814,7 +822,8 @@ template <bool OUT4>
 __global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
                                                        const float2 *__restrict__ twg, float *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int L = a.L, M = L / 2, MS = M + 1, RB = a.RB;
+  const int L = a.L, M = L / 2, RB = a.RB;
+  const int MS = fft_row_stride(M);  // X holds the loaded rows (M + 1 values), then serves as transform scratch
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = blockIdx.x * RB;
   float2 *X = reinterpret_cast<float2 *>(smem);

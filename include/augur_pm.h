@@ -80,6 +80,7 @@ typedef struct augur_pm_tiles {
   int green_tile_y;   /* y columns per z-transform + Green block: 8 or 16, divides grid */
   int c2r_rows;       /* x rows per C2R block: power of two <= 32 */
   int fft_rows;       /* rows per y-transform block: 1..256 */
+  int deposit_aggregate; /* 1: warp-aggregate deposit atomics (cells dense in bodies), 0: plain */
 } augur_pm_tiles;
 
 int augur_pm_plan_get_tiles(const augur_pm_plan *plan, augur_pm_tiles *out);

@@ -35,11 +35,11 @@ def test_tile_shapes_leave_the_trajectory_bit_identical(G, kind):
     plan = PMPlan(3, G, n, "periodic", 1.0, device=DEV)
     ref = _run(plan, pos, vel, mass, dt, 4)
     shapes = [{"deposit_rows_y": 8, "deposit_rows_z": 1, "deposit_chunk": 2048, "green_tile_y": 8,
-               "c2r_rows": 4, "fft_rows": 8},
+               "c2r_rows": 4, "fft_rows": 8, "deposit_aggregate": 1},
               {"deposit_rows_y": 32, "deposit_rows_z": 2, "deposit_chunk": 65536, "green_tile_y": 16,
-               "c2r_rows": 32, "fft_rows": 64},
+               "c2r_rows": 32, "fft_rows": 64, "deposit_aggregate": 0},
               {"deposit_rows_y": 4, "deposit_rows_z": 4, "deposit_chunk": 4096, "green_tile_y": 16,
-               "c2r_rows": 2, "fft_rows": 1}]
+               "c2r_rows": 2, "fft_rows": 1, "deposit_aggregate": 1}]
     for t in shapes:
         plan.set_tiles(t)
         assert plan.tiles == t
@@ -52,7 +52,7 @@ def test_set_tiles_rejects_shapes_that_do_not_fit():
     plan = PMPlan(3, 96, 1000, "periodic", 1.0, device=DEV)
     before = plan.tiles
     for bad in ({"deposit_rows_y": 5}, {"deposit_rows_z": 16}, {"deposit_rows_z": 5}, {"deposit_chunk": 100},
-                {"green_tile_y": 12}, {"c2r_rows": 3}, {"c2r_rows": 64}, {"fft_rows": 0},
+                {"green_tile_y": 12}, {"c2r_rows": 3}, {"c2r_rows": 64}, {"fft_rows": 0}, {"deposit_aggregate": 2},
                 {"deposit_rows_y": 96, "deposit_rows_z": 12}):
         with pytest.raises(RuntimeError):
             plan.set_tiles(bad)
