@@ -22,6 +22,11 @@
 #include <cmath>
 #include <cstdio>
 
+#include <cuda.h>  // CUtensorMap (the encode entry point is resolved through the runtime)
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "augur_common.cuh"
 #include "tcgen05.cuh"
 
@@ -29,9 +34,17 @@ using bf16 = __nv_bfloat16;
 
 namespace augur {
 
-constexpr int CONV_M = 128;   // voxels per tile (one x segment)
-constexpr int SLAB = CONV_M + 2;
-constexpr int CONV_THREADS = 128;
+constexpr int CONV_M = 128;     // voxels per tile (one x segment)
+constexpr int SLAB = CONV_M + 2;  // voxel rows of an input slab: x0-1 .. x0+128
+constexpr int SLAB_ROWS = 136;    // shared-memory rows per channel block (128-byte aligned TMA boxes)
+constexpr int RING = 6;           // input rows (all three z planes) in flight
+constexpr int NACC = 4;           // TMEM accumulators: tiles between the MMA warp and the epilogue
+// warps 0-7: epilogue (two per TMEM lane quarter, each taking half of the output channels);
+// warp 8: MMA issue; warp 9: TMA loads
+constexpr int EPI_WARPS = 8;
+constexpr int MMA_WARP = EPI_WARPS;
+constexpr int TMA_WARP = EPI_WARPS + 1;
+constexpr int CONV_THREADS = 32 * (EPI_WARPS + 2);
 constexpr uint32_t WAIT_BUDGET = 1u << 20;
 
 enum { EPI_FWD = 0, EPI_OUT = 1, EPI_BWD = 2 };
@@ -43,11 +56,22 @@ __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.f + erff(x * 0.70710678118654752440f)) + x * phi;
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, bool valid) {
-  const int n = valid ? 16 : 0;  // zero-fill when invalid
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+// 5D tiled TMA load (c, x, y, z, b) into shared memory, completing bytes on mbar.
+__device__ __forceinline__ void tma_load5(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z, int b,
+                                          uint64_t *mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(z), "r"(b), "r"(smem_u32(mbar))
+      : "memory");
+}
 
 struct ConvArgs {
   int B, G;
@@ -58,7 +82,23 @@ struct ConvArgs {
   float out_scale;   // EPI_OUT: added field = out_scale * (acc + bias)
 };
 
-constexpr int RING = 5;  // y rows of input slabs kept per z plane (rows y-1 .. y+2 plus one being freed)
+struct ConvUnit {
+  int b, z, x0, ya, ny;
+};
+__device__ __forceinline__ ConvUnit conv_unit(const ConvArgs &a, int unit) {
+  ConvUnit u;
+  int t = unit;
+  const int yc = t % a.nyc;
+  t /= a.nyc;
+  const int xs = t % a.xseg;
+  t /= a.xseg;
+  u.z = t % a.G;
+  u.b = t / a.G;
+  u.x0 = xs * CONV_M;
+  u.ya = yc * a.yc;
+  u.ny = min(a.G, u.ya + a.yc) - u.ya;
+  return u;
+}
 
 // ---------------------------------------------------------------------------------------
 // tcgen05 implicit-GEMM 3x3x3 conv. CIN in {16, 32}, N in {16, 32}.
@@ -66,31 +106,43 @@ constexpr int RING = 5;  // y rows of input slabs kept per z plane (rows y-1 .. 
 //   EPI_OUT: y = out_scale * (acc + b)[0..2]          out0 = F (float4 grid, y added to lanes 0..2)
 //   EPI_BWD: g = acc + resid (fp32, optional)         out0 = g (fp32), out1 = g * gelu'(zprev) (bf16)
 //
-// Work unit = (batch, z, x segment, chunk of yc consecutive y rows). The CTA walks y inside
-// the unit keeping a ring of RING input rows per z plane in shared memory, so each new tile
-// loads one y row for each of the three z planes (prefetched one tile ahead with cp.async);
-// the 54 MMAs of tile y go to TMEM accumulator y & 1 while the epilogue of tile y-1 reads
-// the other one.
+// Work unit = (batch, z, x segment, chunk of yc consecutive y rows); the CTA takes units
+// blockIdx.x, + gridDim.x, ... and walks y inside each. Warp-specialised pipeline, no block
+// barrier per tile:
+//   TMA warp   loads input row y+1 of planes z-1, z, z+1 (one 8-channel x 130-voxel box per
+//              channel block; the tensor map zero-fills outside the grid) into a ring of
+//              RING slots, arming full[slot] with the byte count;
+//   MMA warp   waits for the three rows of tile y, issues its 27 taps x CIN/16 MMAs into
+//              accumulator t % NACC, commits to acc_full, and commits to empty[slot] for the
+//              rows tile y is the last user of;
+//   epilogue   waits for acc_full, reads the accumulator (tcgen05.ld), applies the layer's
+//              epilogue, and arrives on acc_empty.
+// Every wait is bounded: a stall sets the CTA's abort flag, the roles leave their loops,
+// and bit AUGUR_ERRBIT_TIMEOUT is raised in *err.
 // ---------------------------------------------------------------------------------------
 template <int CIN, int N, int EPI>
-__global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const bf16 *__restrict__ in,
+__global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                   const bf16 *__restrict__ wB,
                                                                   const float *__restrict__ bias,
                                                                   const void *__restrict__ resid,
                                                                   const bf16 *__restrict__ zprev,
                                                                   void *__restrict__ out0, bf16 *__restrict__ out1,
                                                                   ConvArgs a, unsigned *__restrict__ err) {
-  constexpr int CB = CIN / 8;                  // 16-byte channel blocks per voxel
-  constexpr int KSTEP_PER_TAP = CIN / 16;      // K = 16 per MMA
-  constexpr int WBYTES = 27 * CIN * N * 2;     // weights, UMMA B layout
-  constexpr int SLAB_BYTES = CB * SLAB * 16;
-  constexpr int SLAB_STRIDE = ((SLAB_BYTES + 127) / 128) * 128;
+  constexpr int CB = CIN / 8;              // 16-byte channel blocks per voxel
+  constexpr int KSTEP_PER_TAP = CIN / 16;  // K = 16 per MMA
+  constexpr int WBYTES = 27 * CIN * N * 2; // weights, UMMA B layout
+  constexpr int WREGION = ((WBYTES + 127) / 128) * 128;
+  constexpr int CBLK = SLAB_ROWS * 16;     // one channel block of a slab
+  constexpr int SLOT_BYTES = 3 * CB * CBLK;
+  constexpr uint32_t ROW_TX = 3u * CB * SLAB * 16;  // bytes the boxes of one ring slot bring
   constexpr uint32_t IDESC = idesc_bf16_f32(CONV_M, N);
+  constexpr int NC = N / 2;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;
-  unsigned char *sSlab = smem + ((WBYTES + 127) / 128) * 128;  // [3 z planes][RING rows]
-  __shared__ __align__(8) uint64_t mbar[2];
+  unsigned char *sSlab = smem + WREGION;  // [RING][3 planes][CB][SLAB_ROWS][16 B]
+  __shared__ __align__(8) uint64_t full[RING], empty[RING], acc_full[NACC], acc_empty[NACC];
   __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int G = a.G;
@@ -100,12 +152,19 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const bf16 *__
     for (int e = tid; e < WBYTES / 16; e += CONV_THREADS) dst[e] = src[e];
   }
   if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int i = 0; i < RING; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < NACC; ++i) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], EPI_WARPS);
+    }
+    s_abort = 0;
     mbar_fence_init();
   }
   if (warp == 0) {
-    tmem_alloc(&s_tmem, 64);  // two 32-column accumulators
+    tmem_alloc(&s_tmem, NACC * 32);
     tmem_relinquish();
   }
   fence_async_smem();
@@ -114,171 +173,190 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const bf16 *__
   tc_fence_after();
   const uint32_t tmem = s_tmem;
   const uint32_t slab0 = smem_u32(sSlab);
-  const uint32_t w_addr = smem_u32(sW);
-  uint32_t commits[2] = {0, 0};
-  bool ok = true;
+  volatile int *abort_flag = &s_abort;
 
-  auto slab_addr = [&](int dz, int row) -> uint32_t {
-    return slab0 + (uint32_t)((dz * RING + ((row + RING) % RING)) * SLAB_STRIDE);
-  };
-  // copy input row (z + dz - 1, row) of x segment x0 into its ring slot (zero outside the grid)
-  auto load_row = [&](size_t bbase, int z, int x0, int row) {
-    for (int c = tid; c < 3 * SLAB * CB; c += CONV_THREADS) {
-      const int dz = c / (SLAB * CB);
-      const int rem = c - dz * SLAB * CB;
-      const int r = rem / CB, cb = rem - r * CB;
-      const int zz = z + dz - 1, xx = x0 - 1 + r;
-      const bool v = zz >= 0 && zz < G && row >= 0 && row < G && xx >= 0 && xx < G;
-      const bf16 *src = v ? in + (bbase + ((size_t)zz * G + row) * G + xx) * CIN + cb * 8 : in;
-      cp_async16(slab_addr(dz, row) + (uint32_t)(cb * SLAB + r) * 16u, src, v);
+  // bounded wait; gives up early once another role has given up
+  auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+    for (uint32_t i = 0; i < WAIT_BUDGET; ++i) {
+      if (mbar_try_wait(bar, parity)) return true;
+      if ((i & 255u) == 255u && *abort_flag) return false;
     }
+    *abort_flag = 1;
+    return false;
   };
-  // epilogue of the tile at (bbase, z, y, x0) from accumulator acc_sel
-  auto epilogue = [&](size_t bbase, int z, int y, int x0, int acc_sel) {
-    tc_fence_after();
-    float acc[32];
-    tmem_ld32(tmem + (uint32_t)(acc_sel * 32) + ((uint32_t)(warp * 32) << 16), acc);
-    const int x = x0 + warp * 32 + lane;
-    if (x < G) {
-      const size_t vox = bbase + ((size_t)z * G + y) * G + x;
-      if constexpr (EPI == EPI_FWD) {
-        const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N;
-        bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N;
-#pragma unroll
-        for (int n = 0; n < N; n += 8) {
-          uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
-          const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
-          __align__(16) __nv_bfloat162 ho[4], zo[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float z0 = acc[n + 2 * q] + bias[n + 2 * q], z1 = acc[n + 2 * q + 1] + bias[n + 2 * q + 1];
-            ho[q] = __floats2bfloat162_rn(__bfloat162float(hp[q].x) + gelu_f(z0),
-                                          __bfloat162float(hp[q].y) + gelu_f(z1));
-            zo[q] = __floats2bfloat162_rn(z0, z1);
+
+  if (warp == TMA_WARP) {
+    // ---- producer: rows ya-1 .. ya+ny of every unit, all three planes ----------------------
+    uint32_t k = 0;
+    if (lane == 0) {
+      bool go = true;
+      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+        const ConvUnit u = conv_unit(a, unit);
+        for (int j = 0; j < u.ny + 2; ++j, ++k) {
+          const uint32_t slot = k % RING, n = k / RING;
+          if (n > 0 && !wait(&empty[slot], (n - 1) & 1u)) {
+            go = false;
+            break;
           }
-          *reinterpret_cast<uint4 *>(hout + n) = *reinterpret_cast<uint4 *>(ho);
-          if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + n) = *reinterpret_cast<uint4 *>(zo);
-        }
-      } else if constexpr (EPI == EPI_OUT) {
-        float4 *F = reinterpret_cast<float4 *>(out0) + vox;
-        float4 f = *F;
-        f.x += a.out_scale * (acc[0] + bias[0]);
-        f.y += a.out_scale * (acc[1] + bias[1]);
-        f.z += a.out_scale * (acc[2] + bias[2]);
-        *F = f;
-      } else {
-        const float *rin = reinterpret_cast<const float *>(resid);
-        float *gout = reinterpret_cast<float *>(out0) + vox * N;
+          mbar_expect_tx(&full[slot], ROW_TX);
+          const uint32_t dst0 = slab0 + slot * SLOT_BYTES;
 #pragma unroll
-        for (int n = 0; n < N; n += 4) {
-          float4 g = make_float4(acc[n], acc[n + 1], acc[n + 2], acc[n + 3]);
-          if (rin) {
-            const float4 r = *reinterpret_cast<const float4 *>(rin + vox * N + n);
-            g.x += r.x;
-            g.y += r.y;
-            g.z += r.z;
-            g.w += r.w;
-          }
-          *reinterpret_cast<float4 *>(gout + n) = g;
-          if (out1) {
-            const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(zprev + vox * N + n);
-            const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(zprev + vox * N + n + 2);
-            __align__(8) __nv_bfloat162 o[2];
-            o[0] = __floats2bfloat162_rn(g.x * gelu_grad(__bfloat162float(z01.x)),
-                                         g.y * gelu_grad(__bfloat162float(z01.y)));
-            o[1] = __floats2bfloat162_rn(g.z * gelu_grad(__bfloat162float(z23.x)),
-                                         g.w * gelu_grad(__bfloat162float(z23.y)));
-            *reinterpret_cast<uint2 *>(out1 + vox * N + n) = *reinterpret_cast<uint2 *>(o);
-          }
+          for (int pz = 0; pz < 3; ++pz)
+#pragma unroll
+            for (int cb = 0; cb < CB; ++cb)
+              tma_load5(dst0 + (uint32_t)((pz * CB + cb) * CBLK), &tmap, cb * 8, u.x0 - 1, u.ya - 1 + j, u.z + pz - 1,
+                        u.b, &full[slot]);
         }
       }
+      // tail: every slot's last fill has been consumed and released (no transfer or MMA
+      // still writes this CTA's shared memory when it exits)
+      const uint32_t last = k;
+      for (uint32_t q = (last > RING ? last - RING : 0); q < last; ++q)
+        if (!wait(&empty[q % RING], (q / RING) & 1u)) {
+          wait(&full[q % RING], (q / RING) & 1u);  // at least let the transfer land
+        }
     }
-  };
-
-  for (int unit = blockIdx.x; unit < a.nunits && ok; unit += gridDim.x) {
-    int t = unit;
-    const int yc = t % a.nyc;
-    t /= a.nyc;
-    const int xs = t % a.xseg;
-    t /= a.xseg;
-    const int z = t % G;
-    const int b = t / G;
-    const int x0 = xs * CONV_M;
-    const size_t bbase = (size_t)b * G * G * G;
-    const int ya = yc * a.yc, yb = min(G, ya + a.yc);
-    // warm-up: rows ya-1, ya, ya+1
-    load_row(bbase, z, x0, ya - 1);
-    load_row(bbase, z, x0, ya);
-    load_row(bbase, z, x0, ya + 1);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    for (int y = ya; y < yb; ++y) {
-      // prefetch the row the next tile adds (its slot last served tile y-2, finished below)
-      load_row(bbase, z, x0, y + 2);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      asm volatile("cp.async.wait_group 1;" ::: "memory");
-      fence_async_smem();
-      __syncthreads();
-      const int sel = y & 1;
-      if (tid == 0) {
+  } else if (warp == MMA_WARP) {
+    // ---- MMA issue ----------------------------------------------------------------------------
+    if (lane == 0) {
+      const uint64_t b_desc0 = smem_desc(smem_u32(sW), N * 16, 128);
+      uint32_t k0 = 0, t = 0;
+      bool go = true;
+      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+        const ConvUnit u = conv_unit(a, unit);
+        for (int i = 0; i < u.ny; ++i, ++t) {
+          uint64_t arow[3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            const uint32_t kr = k0 + i + r;
+            if (!wait(&full[kr % RING], (kr / RING) & 1u)) go = false;
+            arow[r] = smem_desc(slab0 + (kr % RING) * SLOT_BYTES, CBLK, 128);
+          }
+          const uint32_t acc = t % NACC;
+          if (go && t >= NACC && !wait(&acc_empty[acc], ((t / NACC) - 1) & 1u)) go = false;
+          if (!go) break;
+          tc_fence_after();
+          const uint32_t d = tmem + acc * 32;
+#pragma unroll
+          for (int pz = 0; pz < 3; ++pz) {
+#pragma unroll
+            for (int py = 0; py < 3; ++py) {
+#pragma unroll
+              for (int dx = 0; dx < 3; ++dx) {
+                const int tap = (pz * 3 + py) * 3 + dx;
+#pragma unroll
+                for (int kc = 0; kc < KSTEP_PER_TAP; ++kc) {
+                  const int s = tap * KSTEP_PER_TAP + kc;
+                  // plane pz of row y-1+py: + pz * CB blocks; K step kc: + 2 kc blocks; tap dx: + dx voxels
+                  const uint64_t ad = arow[py] + (uint64_t)(((pz * CB + 2 * kc) * CBLK + dx * 16) >> 4);
+                  const uint64_t bd = b_desc0 + (uint64_t)((2 * s * N * 16) >> 4);
+                  umma_bf16(d, ad, bd, IDESC, s ? 1u : 0u);
+                }
+              }
+            }
+          }
+          umma_commit(&acc_full[acc]);
+          // release the rows whose last user is this tile
+          const int nrel = (i < u.ny - 1) ? 1 : 3;
+          for (int r = 0; r < nrel; ++r) umma_commit(&empty[(k0 + i + r) % RING]);
+        }
+        k0 += u.ny + 2;
+      }
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lane quarter w % 4 (voxels x0 + 32 (w % 4) + lane) and
+    // output channels [NC (w / 4), + NC) -------------------------------------------------------
+    const int q = warp & 3, half = warp >> 2;
+    const int c0 = half * NC;
+    const bool active = !(EPI == EPI_OUT && half == 1);  // three output channels: first half only
+    uint32_t t = 0;
+    bool go = true;
+    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+      const ConvUnit u = conv_unit(a, unit);
+      const size_t bbase = (size_t)u.b * G * G * G;
+      for (int i = 0; i < u.ny; ++i, ++t) {
+        const uint32_t acc = t % NACC;
+        if (!wait(&acc_full[acc], (t / NACC) & 1u)) {
+          go = false;
+          break;
+        }
         tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(sel * 32);
-#pragma unroll 1
-        for (int pz = 0; pz < 3; ++pz) {
-#pragma unroll 1
-          for (int py = 0; py < 3; ++py) {
-            const uint32_t sa = slab_addr(pz, y + py - 1);
+        if (active) {
+          float v[NC];
+          const uint32_t taddr = tmem + acc * 32 + (uint32_t)(half * NC) + ((uint32_t)(q * 32) << 16);
+          if constexpr (NC == 16) tmem_ld16(taddr, v);
+          else tmem_ld8(taddr, v);
+          const int y = u.ya + i;
+          const int x = u.x0 + q * 32 + lane;
+          if (x < G) {
+            const size_t vox = bbase + ((size_t)u.z * G + y) * G + x;
+            if constexpr (EPI == EPI_FWD) {
+              const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N + c0;
+              bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N + c0;
 #pragma unroll
-            for (int dx = 0; dx < 3; ++dx) {
-              const int tap = (pz * 3 + py) * 3 + dx;
+              for (int n = 0; n < NC; n += 8) {
+                uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
+                const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
+                __align__(16) __nv_bfloat162 ho[4], zo[4];
 #pragma unroll
-              for (int kc = 0; kc < KSTEP_PER_TAP; ++kc) {
-                const uint64_t ad = smem_desc(sa + (uint32_t)(2 * kc * SLAB * 16 + dx * 16), SLAB * 16, 128);
-                const int s = tap * KSTEP_PER_TAP + kc;
-                const uint64_t bd = smem_desc(w_addr + (uint32_t)(2 * s * N * 16), N * 16, 128);
-                umma_bf16(d, ad, bd, IDESC, (pz | py | dx | kc) ? 1u : 0u);
+                for (int q2 = 0; q2 < 4; ++q2) {
+                  const float z0 = v[n + 2 * q2] + bias[c0 + n + 2 * q2];
+                  const float z1 = v[n + 2 * q2 + 1] + bias[c0 + n + 2 * q2 + 1];
+                  ho[q2] = __floats2bfloat162_rn(__bfloat162float(hp[q2].x) + gelu_f(z0),
+                                                 __bfloat162float(hp[q2].y) + gelu_f(z1));
+                  zo[q2] = __floats2bfloat162_rn(z0, z1);
+                }
+                *reinterpret_cast<uint4 *>(hout + n) = *reinterpret_cast<uint4 *>(ho);
+                if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint4 *>(zo);
+              }
+            } else if constexpr (EPI == EPI_OUT) {
+              float4 *F = reinterpret_cast<float4 *>(out0) + vox;
+              float4 f = *F;
+              f.x += a.out_scale * (v[0] + bias[0]);
+              f.y += a.out_scale * (v[1] + bias[1]);
+              f.z += a.out_scale * (v[2] + bias[2]);
+              *F = f;
+            } else {
+              const float *rin = reinterpret_cast<const float *>(resid);
+              float *gout = reinterpret_cast<float *>(out0) + vox * N + c0;
+#pragma unroll
+              for (int n = 0; n < NC; n += 4) {
+                float4 g = make_float4(v[n], v[n + 1], v[n + 2], v[n + 3]);
+                if (rin) {
+                  const float4 r = *reinterpret_cast<const float4 *>(rin + vox * N + c0 + n);
+                  g.x += r.x;
+                  g.y += r.y;
+                  g.z += r.z;
+                  g.w += r.w;
+                }
+                *reinterpret_cast<float4 *>(gout + n) = g;
+                if (out1) {
+                  const bf16 *zp = zprev + vox * N + c0 + n;
+                  const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(zp);
+                  const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(zp + 2);
+                  __align__(8) __nv_bfloat162 o[2];
+                  o[0] = __floats2bfloat162_rn(g.x * gelu_grad(__bfloat162float(z01.x)),
+                                               g.y * gelu_grad(__bfloat162float(z01.y)));
+                  o[1] = __floats2bfloat162_rn(g.z * gelu_grad(__bfloat162float(z23.x)),
+                                               g.w * gelu_grad(__bfloat162float(z23.y)));
+                  *reinterpret_cast<uint2 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint2 *>(o);
+                }
               }
             }
           }
         }
-        umma_commit(&mbar[sel]);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[acc]);
       }
-      commits[sel]++;
-      if (y > ya) {  // epilogue of the previous tile while this tile's MMAs run
-        const int ps = sel ^ 1;
-        const bool got = mbar_wait_bounded(&mbar[ps], (commits[ps] - 1) & 1, WAIT_BUDGET);
-        if (__syncthreads_or(!got)) {  // the give-up decision is the same in every thread
-          ok = false;
-          break;
-        }
-        epilogue(bbase, z, y - 1, x0, ps);
-      }
-      tc_fence_before();
-      __syncthreads();
     }
-    if (!ok) break;
-    // last tile of the unit
-    const int ls = (yb - 1) & 1;
-    const bool got = mbar_wait_bounded(&mbar[ls], (commits[ls] - 1) & 1, WAIT_BUDGET);
-    if (__syncthreads_or(!got)) {
-      ok = false;
-      break;
-    }
-    epilogue(bbase, z, yb - 1, x0, ls);
-    asm volatile("cp.async.wait_all;" ::: "memory");  // the unit's last prefetch (beyond the chunk)
-    tc_fence_before();
-    __syncthreads();
-  }
-  if (!ok) {
-    if (tid == 0) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
-    for (int bb = 0; bb < 2; ++bb)
-      if (commits[bb] > 0) mbar_wait_bounded(&mbar[bb], (commits[bb] - 1) & 1, WAIT_BUDGET);
-    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
+  if (tid == 0 && *abort_flag) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, 64);
+    tmem_dealloc(tmem, NACC * 32);
   }
 }
 
@@ -496,6 +574,37 @@ using namespace augur;
 
 namespace {
 
+// cuTensorMapEncodeTiled through the runtime's driver entry-point query (no link against
+// libcuda); resolved once.
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+template <int CIN>
+int make_act_map(CUtensorMap *map, const void *in, int B, int G) {
+  auto fn = encode_fn();
+  if (!fn || (reinterpret_cast<uintptr_t>(in) & 15) != 0) return AUGUR_EINVAL;
+  const cuuint64_t dim[5] = {(cuuint64_t)CIN, (cuuint64_t)G, (cuuint64_t)G, (cuuint64_t)G, (cuuint64_t)B};
+  const cuuint64_t stride[4] = {(cuuint64_t)CIN * 2, (cuuint64_t)G * CIN * 2, (cuuint64_t)G * G * CIN * 2,
+                                (cuuint64_t)G * G * G * CIN * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)SLAB, 1, 1, 1};
+  const cuuint32_t estride[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(in), dim, stride, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? AUGUR_OK : AUGUR_EINVAL;
+}
+
 template <int CIN, int N, int EPI>
 int launch_conv_tc(const void *in, const void *wB, const float *bias, const void *resid, const void *zprev,
                    void *out0, void *out1, int B, int G, float out_scale, unsigned *err, cudaStream_t st) {
@@ -506,7 +615,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // y chunk: long enough to amortise the 3-row warm-up, short enough to fill every SM
+  // y chunk: long enough to amortise the two halo rows, short enough to fill every SM
   const int columns = B * G * a.xseg;
   int yc = G;
   while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
@@ -514,17 +623,22 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   a.nyc = (G + yc - 1) / yc;
   a.nunits = columns * a.nyc;
   a.out_scale = out_scale;
+  // input activations [B][G][G][G][CIN] bf16 as a 5D tensor (c, x, y, z, b); box = 8 channels x
+  // SLAB voxels of one row; outside the grid the box reads zeros (the convolution's padding)
+  CUtensorMap map;
+  if (make_act_map<CIN>(&map, in, B, G) != AUGUR_OK) return AUGUR_ECUDA;
   constexpr int WBYTES = 27 * CIN * N * 2;
-  constexpr int SLAB_STRIDE = ((((CIN / 8) * SLAB * 16) + 127) / 128) * 128;
-  const size_t smem = ((WBYTES + 127) / 128) * 128 + (size_t)3 * RING * SLAB_STRIDE;
+  const size_t smem = ((WBYTES + 127) / 128) * 128 + (size_t)RING * 3 * (CIN / 8) * SLAB_ROWS * 16;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(conv_tc_kernel<CIN, N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaFuncSetAttribute(conv_tc_kernel<CIN, N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return AUGUR_ECUDA;
     attr = true;
   }
   const int grid = std::min(a.nunits, nsm);
-  conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(
-      (const bf16 *)in, (const bf16 *)wB, bias, resid, (const bf16 *)zprev, out0, (bf16 *)out1, a, err);
+  conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(map, (const bf16 *)wB, bias, resid,
+                                                                (const bf16 *)zprev, out0, (bf16 *)out1, a, err);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
 }
 
