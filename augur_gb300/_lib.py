@@ -50,6 +50,7 @@ SIGNATURES = {
     # include/augur_cnn.h
     "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp]),
     "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
+    "augur_cnn_conv_in_tc": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "augur_cnn_wgrad": (_i32, [_i32, _vp, _vp, _i32, _i32, _vp, _i32, _vp, _vp]),
     "augur_cnn_prep_weights": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
     "augur_cnn_input": (_i32, [_vp, _vp, _i64, _f32, _f32, _vp, _vp]),

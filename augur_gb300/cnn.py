@@ -52,6 +52,7 @@ class GridCNN:
         self.op_fwd_mid = [torch.empty(27 * W * W, **bf) for _ in range(3)]
         self.op_bwd_mid = [torch.empty(27 * W * W, **bf) for _ in range(3)]
         self.op_fwd_out = torch.empty(27 * W * 16, **bf)
+        self.op_in = torch.zeros(64 * W, **bf)  # input layer: K = 27 x 2 padded to 64
         self.op_bwd_out = torch.empty(27 * 16 * W, **bf)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.adam_step = 0
@@ -106,6 +107,7 @@ class GridCNN:
             w = self.view[f"w_mid{i}"]
             self._call("augur_cnn_prep_weights", w.data_ptr(), W, W, W, W, 0, self.op_fwd_mid[i].data_ptr())
             self._call("augur_cnn_prep_weights", w.data_ptr(), W, W, W, W, 1, self.op_bwd_mid[i].data_ptr())
+        self._call("augur_cnn_prep_weights", self.view["w_in"].data_ptr(), W, 2, 2, W, 0, self.op_in.data_ptr())
         wo = self.view["w_out"]
         self._call("augur_cnn_prep_weights", wo.data_ptr(), 3, W, W, 16, 0, self.op_fwd_out.data_ptr())
         self._call("augur_cnn_prep_weights", wo.data_ptr(), 3, W, 16, W, 1, self.op_bwd_out.data_ptr())
@@ -151,9 +153,8 @@ class GridCNN:
         """field4 (B*G^3*4 floats) lanes 0..2 += out_scale * net(x)."""
         ws = self._workspace(B, G, train)
         h, z = ws["h"], ws.get("z")
-        tmp_z = z[0] if train else None
-        self._call("augur_cnn_conv_in", x.data_ptr(), self.view["w_in"].data_ptr(), self.view["b_in"].data_ptr(),
-                   B, G, (z[0] if train else h[1]).data_ptr(), h[0].data_ptr())
+        self._call("augur_cnn_conv_in_tc", x.data_ptr(), self.op_in.data_ptr(), self.view["b_in"].data_ptr(),
+                   B, G, _p(z[0]) if train else None, h[0].data_ptr(), self.err.data_ptr())
         for i in range(3):
             self._call("augur_cnn_conv_tc", 0, h[i].data_ptr(), self.op_fwd_mid[i].data_ptr(),
                        self.view[f"b_mid{i}"].data_ptr(), h[i].data_ptr(), None, h[i + 1].data_ptr(),
@@ -162,7 +163,6 @@ class GridCNN:
                    self.view["b_out"].data_ptr(), None, None, field4.data_ptr(), None, B, G, self.out_scale,
                    self.err.data_ptr())
         self._x = x
-        del tmp_z
 
     def backward(self, dfield4: torch.Tensor, B: int, G: int) -> None:
         """Gradients of all parameters given dL/d(field4 lanes 0..2) (lane 3 must be zero).

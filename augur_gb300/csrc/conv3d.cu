@@ -361,6 +361,192 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
 }
 
 // ---------------------------------------------------------------------------------------
+// Input layer on tcgen05: x (B, G^3, 2) bf16 -> z0 (optional), h0 = gelu(z0), 32 channels.
+// K = 27 taps x 2 channels = 54, padded to 64 (four K = 16 MMAs per tile); the A operand is
+// built in shared memory by four producer warps (im2col: thread r gathers the 27 neighbours of
+// voxel x0 + r, two channels each, into 16-byte K blocks), published to the MMA warp through
+// full/empty mbarriers; the epilogue is the forward layers' (eight warps, two per TMEM lane
+// quarter). Weights: augur_cnn_prep_weights(w_in, 32, 2, 2, 32, 0) into a zeroed 64 x 32 buffer.
+// ---------------------------------------------------------------------------------------
+constexpr int IN_PROD_WARPS = 4;                        // 128 producer threads: one per voxel row
+constexpr int IN_STAGES = 4;                            // A buffers in flight
+constexpr int IN_KB = 8;                                // 16-byte K blocks (64 K values)
+constexpr int IN_ABYTES = IN_KB * CONV_M * 16;          // 16 KB per A buffer
+constexpr int IN_THREADS = 32 * (EPI_WARPS + 1 + IN_PROD_WARPS);
+
+__global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *__restrict__ x,
+                                                                   const bf16 *__restrict__ wB,
+                                                                   const float *__restrict__ bias,
+                                                                   bf16 *__restrict__ z0, bf16 *__restrict__ h0,
+                                                                   ConvArgs a, unsigned *__restrict__ err) {
+  constexpr int N = 32, NC = 16;
+  constexpr uint32_t IDESC = idesc_bf16_f32(CONV_M, N);
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sW = smem;                   // [8 kb][32 n][16 B]
+  unsigned char *sA = smem + IN_KB * N * 16;  // [IN_STAGES][8 kb][128 r][16 B]
+  __shared__ __align__(8) uint64_t full[IN_STAGES], empty[IN_STAGES], acc_full[NACC], acc_empty[NACC];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int G = a.G;
+  {
+    const uint4 *src = reinterpret_cast<const uint4 *>(wB);
+    uint4 *dst = reinterpret_cast<uint4 *>(sW);
+    for (int e = tid; e < IN_KB * N; e += IN_THREADS) dst[e] = src[e];
+    // K blocks 6 (upper half) and 7 of every A buffer are padding: zero once
+    uint4 *A = reinterpret_cast<uint4 *>(sA);
+    for (int e = tid; e < IN_STAGES * IN_KB * CONV_M; e += IN_THREADS) A[e] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  if (tid == 0) {
+    for (int i = 0; i < IN_STAGES; ++i) {
+      mbar_init(&full[i], 32 * IN_PROD_WARPS);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < NACC; ++i) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], EPI_WARPS);
+    }
+    s_abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, NACC * 32);
+    tmem_relinquish();
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t a0 = smem_u32(sA);
+  volatile int *abort_flag = &s_abort;
+  auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+    for (uint32_t i = 0; i < WAIT_BUDGET; ++i) {
+      if (mbar_try_wait(bar, parity)) return true;
+      if ((i & 255u) == 255u && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    return false;
+  };
+
+  if (warp > MMA_WARP) {
+    // ---- producers: thread r builds row r of the tile's A operand ---------------------------
+    const int r = tid - 32 * (MMA_WARP + 1);
+    const uint32_t *x32 = reinterpret_cast<const uint32_t *>(x);  // two bf16 channels per voxel
+    uint32_t t = 0;
+    bool go = true;
+    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+      const ConvUnit u = conv_unit(a, unit);
+      const size_t bbase = (size_t)u.b * G * G * G;
+      const int xx = u.x0 + r;
+      for (int i = 0; i < u.ny; ++i, ++t) {
+        const uint32_t st = t % IN_STAGES, n = t / IN_STAGES;
+        if (n > 0 && !wait(&empty[st], (n - 1) & 1u)) {
+          go = false;
+          break;
+        }
+        const int y = u.ya + i;
+        uint32_t v[28];
+#pragma unroll
+        for (int tap = 0; tap < 27; ++tap) {
+          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+          const int zz = u.z + dz, yy = y + dy, xq = xx + dx;
+          const bool in = zz >= 0 && zz < G && yy >= 0 && yy < G && xq >= 0 && xq < G;
+          v[tap] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
+        }
+        v[27] = 0u;
+        unsigned char *A = sA + (size_t)st * IN_ABYTES;
+#pragma unroll
+        for (int kb = 0; kb < 7; ++kb)
+          *reinterpret_cast<uint4 *>(A + ((size_t)kb * CONV_M + r) * 16) =
+              make_uint4(v[4 * kb], v[4 * kb + 1], v[4 * kb + 2], v[4 * kb + 3]);
+        fence_async_smem();  // generic-proxy stores -> visible to the tensor core
+        mbar_arrive(&full[st]);
+      }
+    }
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      const uint64_t b_desc0 = smem_desc(smem_u32(sW), N * 16, 128);
+      uint32_t t = 0;
+      bool go = true;
+      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+        const ConvUnit u = conv_unit(a, unit);
+        for (int i = 0; i < u.ny; ++i, ++t) {
+          const uint32_t st = t % IN_STAGES, acc = t % NACC;
+          if (!wait(&full[st], (t / IN_STAGES) & 1u)) go = false;
+          if (go && t >= NACC && !wait(&acc_empty[acc], ((t / NACC) - 1) & 1u)) go = false;
+          if (!go) break;
+          tc_fence_after();
+          const uint64_t ad0 = smem_desc(a0 + st * IN_ABYTES, CONV_M * 16, 128);
+#pragma unroll
+          for (int kc = 0; kc < 4; ++kc)
+            umma_bf16(tmem + acc * 32, ad0 + (uint64_t)((2 * kc * CONV_M * 16) >> 4),
+                      b_desc0 + (uint64_t)((2 * kc * N * 16) >> 4), IDESC, kc ? 1u : 0u);
+          umma_commit(&acc_full[acc]);
+          umma_commit(&empty[st]);
+        }
+      }
+    }
+  } else {
+    // ---- epilogue ------------------------------------------------------------------------------
+    const int q = warp & 3, half = warp >> 2;
+    const int c0 = half * NC;
+    uint32_t t = 0;
+    bool go = true;
+    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
+      const ConvUnit u = conv_unit(a, unit);
+      const size_t bbase = (size_t)u.b * G * G * G;
+      for (int i = 0; i < u.ny; ++i, ++t) {
+        const uint32_t acc = t % NACC;
+        if (!wait(&acc_full[acc], (t / NACC) & 1u)) {
+          go = false;
+          break;
+        }
+        tc_fence_after();
+        float v[NC];
+        tmem_ld16(tmem + acc * 32 + (uint32_t)c0 + ((uint32_t)(q * 32) << 16), v);
+        const int xq = u.x0 + q * 32 + lane;
+        if (xq < G) {
+          const size_t vox = bbase + ((size_t)u.z * G + u.ya + i) * G + xq;
+#pragma unroll
+          for (int nn = 0; nn < NC; nn += 8) {
+            __align__(16) __nv_bfloat162 ho[4], zo[4];
+#pragma unroll
+            for (int q2 = 0; q2 < 4; ++q2) {
+              const float za = v[nn + 2 * q2] + bias[c0 + nn + 2 * q2];
+              const float zb = v[nn + 2 * q2 + 1] + bias[c0 + nn + 2 * q2 + 1];
+              ho[q2] = __floats2bfloat162_rn(gelu_f(za), gelu_f(zb));
+              zo[q2] = __floats2bfloat162_rn(za, zb);
+            }
+            *reinterpret_cast<uint4 *>(h0 + vox * N + c0 + nn) = *reinterpret_cast<uint4 *>(ho);
+            if (z0) *reinterpret_cast<uint4 *>(z0 + vox * N + c0 + nn) = *reinterpret_cast<uint4 *>(zo);
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[acc]);
+      }
+    }
+  }
+  // drain: every issued MMA has been waited for by the epilogue (acc_full); the empty commits
+  // of the last stages are waited here so no arrival targets this CTA after it exits
+  if (tid == 32 * (MMA_WARP + 1)) {
+    uint32_t total = 0;
+    for (int unit = blockIdx.x; unit < a.nunits; unit += gridDim.x) total += conv_unit(a, unit).ny;
+    for (uint32_t q = (total > IN_STAGES ? total - IN_STAGES : 0); q < total; ++q)
+      wait(&empty[q % IN_STAGES], (q / IN_STAGES) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && *abort_flag) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, NACC * 32);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Input layer on the CUDA cores: x (B, G^3, 2) bf16 -> z0 (bf16), h0 = gelu(z0) (bf16), 32 ch.
 // Weights w[n][tap][c] fp32 (27 * 2 * 32) + bias[32].
 // ---------------------------------------------------------------------------------------
@@ -642,6 +828,35 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
 }
 
+int launch_conv_in_tc(const void *x, const void *wB, const float *bias, void *z0, void *h0, int B, int G,
+                      unsigned *err, cudaStream_t st) {
+  ConvArgs a;
+  a.B = B;
+  a.G = G;
+  a.xseg = (G + CONV_M - 1) / CONV_M;
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int columns = B * G * a.xseg;
+  int yc = G;
+  while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
+  a.yc = yc;
+  a.nyc = (G + yc - 1) / yc;
+  a.nunits = columns * a.nyc;
+  a.out_scale = 1.f;
+  const size_t smem = (size_t)IN_KB * 32 * 16 + (size_t)IN_STAGES * IN_ABYTES;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(conv_in_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return AUGUR_ECUDA;
+    attr = true;
+  }
+  const int grid = std::min(a.nunits, nsm);
+  conv_in_tc_kernel<<<grid, IN_THREADS, smem, st>>>((const bf16 *)x, (const bf16 *)wB, bias, (bf16 *)z0, (bf16 *)h0,
+                                                    a, err);
+  return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
+}
+
 template <int CIN, int N, int DZF>
 int launch_wgrad(const void *h, const void *dz, int B, int G, float *partial, int max_parts, float *out,
                  cudaStream_t st) {
@@ -690,6 +905,13 @@ int augur_cnn_conv_in(const void *x, const float *w, const float *bias, int batc
   conv_in_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>((const bf16 *)x, w, bias, batch, grid, (bf16 *)z0,
                                                           (bf16 *)h0);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
+}
+
+int augur_cnn_conv_in_tc(const void *x, const void *w_umma, const float *bias, int batch, int grid, void *z0,
+                         void *h0, unsigned *err, void *stream) {
+  if (!x || !w_umma || !bias || !h0 || !err || batch < 1 || grid < 3) return AUGUR_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(x) & 3) != 0) return AUGUR_EINVAL;
+  return launch_conv_in_tc(x, w_umma, bias, z0, h0, batch, grid, err, (cudaStream_t)stream);
 }
 
 // kind: 0 = 32 -> 32 (dz bf16), 1 = output layer 32 -> 3 (dz = output gradient, fp32 float4

@@ -42,6 +42,15 @@ int augur_cnn_conv_in(const void *x, const float *w, const float *bias, int batc
                       void *stream);
 
 /*
+ * Input layer 2 -> 32 on tcgen05 (K = 54 padded to 64, A operand built in shared memory):
+ * h0 = gelu(conv(x) + bias) bf16; z0 (may be NULL) = conv(x) + bias bf16. w_umma: a zeroed
+ * 64 x 32 bf16 buffer filled by augur_cnn_prep_weights(w, 32, 2, 2, 32, 0, w_umma) (weights
+ * rounded to bf16, unlike augur_cnn_conv_in's fp32 weights).
+ */
+int augur_cnn_conv_in_tc(const void *x, const void *w_umma, const float *bias, int batch, int grid, void *z0,
+                         void *h0, unsigned *err, void *stream);
+
+/*
  * Weight and bias gradients (fixed-order reduction of per-CTA partial sums):
  *   kind 0: 32 -> 32 layer, h (bf16, 32 ch) and dz (bf16, 32 ch)
  *   kind 1: output layer, h3 (bf16, 32 ch) and the output gradient as a float4 grid (4 channels,

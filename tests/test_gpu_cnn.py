@@ -37,7 +37,8 @@ def torch_weights(net: GridCNN):
 
 def ref_forward(x, tw, out_scale, round_bf16=True):
     r = bf if round_bf16 else (lambda t: t)
-    z0 = F.conv3d(x, tw["in"][0], tw["in"][1], padding=1)
+    win = bf(tw["in"][0]) if round_bf16 else tw["in"][0]
+    z0 = F.conv3d(x, win, tw["in"][1], padding=1)
     h = r(F.gelu(z0))
     for i in range(3):
         wmid = bf(tw[f"mid{i}"][0]) if round_bf16 else tw[f"mid{i}"][0]
@@ -146,3 +147,30 @@ def test_gather_transpose_is_the_adjoint_of_the_gather():
     lhs = float((a.double() * v.double()).sum())
     rhs = float((Fg.view(-1).double() * out.double()).sum())
     assert abs(lhs - rhs) < 1e-4 * abs(lhs)
+
+
+@pytest.mark.parametrize("B,G", [(1, 20), (2, 130)])
+def test_tensor_core_input_layer_matches_cuda_core_layer(B, G):
+    """The tcgen05 input layer (bf16 weights, K padded to 64) against the CUDA-core one
+    (fp32 weights) and against torch with bf16-rounded weights."""
+    net = make_net(seed=3)
+    x, xd = inputs(B, G, seed=4)
+    nv = B * G ** 3
+    bf16 = dict(dtype=torch.bfloat16, device=DEV)
+    z_tc, h_tc = torch.empty(nv * 32, **bf16), torch.empty(nv * 32, **bf16)
+    z_cc, h_cc = torch.empty(nv * 32, **bf16), torch.empty(nv * 32, **bf16)
+    net._call("augur_cnn_conv_in_tc", xd.data_ptr(), net.op_in.data_ptr(), net.view["b_in"].data_ptr(), B, G,
+              z_tc.data_ptr(), h_tc.data_ptr(), net.err.data_ptr())
+    net._call("augur_cnn_conv_in", xd.data_ptr(), net.view["w_in"].data_ptr(), net.view["b_in"].data_ptr(), B, G,
+              z_cc.data_ptr(), h_cc.data_ptr())
+    net.check()
+    tw = torch_weights(net)
+    ref = F.conv3d(x, bf(tw["in"][0]), tw["in"][1], padding=1).permute(0, 2, 3, 4, 1).reshape(-1)
+    assert rel_rms(z_tc.float().cpu(), ref) < 5e-3
+    assert rel_rms(z_tc.float(), z_cc.float()) < 1e-2
+    assert rel_rms(h_tc.float(), h_cc.float()) < 1e-2
+    # without z0 the layer writes h0 only
+    h2 = torch.empty_like(h_tc)
+    net._call("augur_cnn_conv_in_tc", xd.data_ptr(), net.op_in.data_ptr(), net.view["b_in"].data_ptr(), B, G,
+              None, h2.data_ptr(), net.err.data_ptr())
+    assert torch.equal(h2, h_tc)
