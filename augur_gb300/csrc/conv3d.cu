@@ -101,25 +101,37 @@ __device__ __forceinline__ ConvUnit conv_unit(const ConvArgs &a, int unit) {
 }
 
 // ---------------------------------------------------------------------------------------
-// tcgen05 implicit-GEMM 3x3x3 conv. CIN in {16, 32}, N in {16, 32}.
+// tcgen05 implicit-GEMM 3x3x3 conv. CIN in {16, 32}, N (output channels) in {16, 32}.
 //   EPI_FWD: z = acc + b ; h = h_in + gelu(z)         out0 = h (bf16), out1 = z (bf16, optional)
 //   EPI_OUT: y = out_scale * (acc + b)[0..2]          out0 = F (float4 grid, y added to lanes 0..2)
 //   EPI_BWD: g = acc + resid (fp32, optional)         out0 = g (fp32), out1 = g * gelu'(zprev) (bf16)
 //
+// GEMM shape. A 128-voxel input row (x0-1 .. x0+128) of the three planes z-1, z, z+1 is one
+// K = 3 * CIN operand; for each dx it multiplies a [3 CIN] x [3 N] weight block whose N axis
+// is (dy, output channel). So one input row y' feeds output rows y'+1, y', y'-1 (dy = 0, 1, 2)
+// at once, with MMAs of N up to 96 instead of 27 narrow N = 32 ones per output row (a
+// 128 x N x 16 MMA costs ~46 cycles for any N <= 64 on this part, 64 at N = 128).
+// Output rows accumulate in a ring of RACC TMEM slots ordered so that the three targets of an
+// input row are adjacent columns (slot(T) = RACC-1 - T mod RACC for output row T); at the ring's
+// wrap, or at a unit's first and last rows, the MMA is split or narrowed to the rows that exist.
+// Accumulators start from zero and every MMA accumulates: the epilogue zeroes a slot after
+// reading it.
+//
 // Work unit = (batch, z, x segment, chunk of yc consecutive y rows); the CTA takes units
-// blockIdx.x, + gridDim.x, ... and walks y inside each. Warp-specialised pipeline, no block
-// barrier per tile:
-//   TMA warp   loads input row y+1 of planes z-1, z, z+1 (one 8-channel x 130-voxel box per
-//              channel block; the tensor map zero-fills outside the grid) into a ring of
-//              RING slots, arming full[slot] with the byte count;
-//   MMA warp   waits for the three rows of tile y, issues its 27 taps x CIN/16 MMAs into
-//              accumulator t % NACC, commits to acc_full, and commits to empty[slot] for the
-//              rows tile y is the last user of;
-//   epilogue   waits for acc_full, reads the accumulator (tcgen05.ld), applies the layer's
-//              epilogue, and arrives on acc_empty.
+// blockIdx.x, + gridDim.x, ... Warp-specialised pipeline, no block barrier per row:
+//   TMA warp   loads input row y' of planes z-1, z, z+1 (one 8-channel x 130-voxel box per
+//              channel block; the tensor map zero-fills outside the grid) into a ring of RING
+//              slots, arming full[slot] with the byte count;
+//   MMA warp   per input row: 3 dx x 3 CIN/16 MMAs (or two narrower ones at the wrap), then
+//              commits empty[slot] (the row is used once) and slot_full of the output row the
+//              row completed;
+//   epilogue   per output row: waits for slot_full, reads (tcgen05.ld), zeroes (tcgen05.st) the
+//              slot, applies the layer's epilogue, and arrives on slot_empty.
 // Every wait is bounded: a stall sets the CTA's abort flag, the roles leave their loops,
 // and bit AUGUR_ERRBIT_TIMEOUT is raised in *err.
 // ---------------------------------------------------------------------------------------
+constexpr int RACC = 8;  // output-row accumulator slots in TMEM
+
 template <int CIN, int N, int EPI>
 __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                   const bf16 *__restrict__ wB,
@@ -129,18 +141,20 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
                                                                   void *__restrict__ out0, bf16 *__restrict__ out1,
                                                                   ConvArgs a, unsigned *__restrict__ err) {
   constexpr int CB = CIN / 8;              // 16-byte channel blocks per voxel
-  constexpr int KSTEP_PER_TAP = CIN / 16;  // K = 16 per MMA
-  constexpr int WBYTES = 27 * CIN * N * 2; // weights, UMMA B layout
+  constexpr int KB = 3 * CB;               // K blocks of an input row (three planes)
+  constexpr int KSTEPS = KB / 2;           // K = 16 per MMA
+  constexpr int NR = 3 * N;                // (dy, output channel)
+  constexpr int WBYTES = 27 * CIN * N * 2; // weights [dx][KB][NR][16 B]
   constexpr int WREGION = ((WBYTES + 127) / 128) * 128;
   constexpr int CBLK = SLAB_ROWS * 16;     // one channel block of a slab
   constexpr int SLOT_BYTES = 3 * CB * CBLK;
   constexpr uint32_t ROW_TX = 3u * CB * SLAB * 16;  // bytes the boxes of one ring slot bring
-  constexpr uint32_t IDESC = idesc_bf16_f32(CONV_M, N);
   constexpr int NC = N / 2;
+  constexpr int TMEM_COLS = RACC * N;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;
   unsigned char *sSlab = smem + WREGION;  // [RING][3 planes][CB][SLAB_ROWS][16 B]
-  __shared__ __align__(8) uint64_t full[RING], empty[RING], acc_full[NACC], acc_empty[NACC];
+  __shared__ __align__(8) uint64_t full[RING], empty[RING], slot_full[RACC], slot_empty[RACC];
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
 
@@ -156,15 +170,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], 1);
     }
-    for (int i = 0; i < NACC; ++i) {
-      mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], EPI_WARPS);
+    for (int i = 0; i < RACC; ++i) {
+      mbar_init(&slot_full[i], 1);
+      mbar_init(&slot_empty[i], EPI_WARPS);
     }
     s_abort = 0;
     mbar_fence_init();
   }
   if (warp == 0) {
-    tmem_alloc(&s_tmem, NACC * 32);
+    tmem_alloc(&s_tmem, TMEM_COLS);
     tmem_relinquish();
   }
   fence_async_smem();
@@ -172,8 +186,21 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
+  const int q = warp & 3, half = warp >> 2;  // epilogue warps: lane quarter, column half
+  if (warp < EPI_WARPS) {  // every accumulator slot starts at zero
+    for (int sl = 0; sl < RACC; ++sl) {
+      const uint32_t ta = tmem + (uint32_t)(sl * N + half * NC) + ((uint32_t)(q * 32) << 16);
+      if constexpr (NC == 16) tmem_zero16(ta);
+      else tmem_zero8(ta);
+    }
+    tmem_wait_st();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
   const uint32_t slab0 = smem_u32(sSlab);
   volatile int *abort_flag = &s_abort;
+  auto slot_of = [](uint32_t T) -> uint32_t { return RACC - 1 - (T % RACC); };
 
   // bounded wait; gives up early once another role has given up
   auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
@@ -211,143 +238,147 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
       // tail: every slot's last fill has been consumed and released (no transfer or MMA
       // still writes this CTA's shared memory when it exits)
       const uint32_t last = k;
-      for (uint32_t q = (last > RING ? last - RING : 0); q < last; ++q)
-        if (!wait(&empty[q % RING], (q / RING) & 1u)) {
-          wait(&full[q % RING], (q / RING) & 1u);  // at least let the transfer land
-        }
+      for (uint32_t r = (last > RING ? last - RING : 0); r < last; ++r)
+        if (!wait(&empty[r % RING], (r / RING) & 1u)) wait(&full[r % RING], (r / RING) & 1u);
     }
   } else if (warp == MMA_WARP) {
-    // ---- MMA issue ----------------------------------------------------------------------------
+    // ---- MMA issue, one input row at a time ---------------------------------------------------
     if (lane == 0) {
-      const uint64_t b_desc0 = smem_desc(smem_u32(sW), N * 16, 128);
-      uint32_t k0 = 0, t = 0;
+      const uint32_t w0 = smem_u32(sW);
+      uint32_t k0 = 0, T0 = 0;
       bool go = true;
       for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
         const ConvUnit u = conv_unit(a, unit);
-        for (int i = 0; i < u.ny; ++i, ++t) {
-          uint64_t arow[3];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            const uint32_t kr = k0 + i + r;
-            if (!wait(&full[kr % RING], (kr / RING) & 1u)) go = false;
-            arow[r] = smem_desc(slab0 + (kr % RING) * SLOT_BYTES, CBLK, 128);
+        for (int j = 0; j < u.ny + 2 && go; ++j) {
+          const uint32_t kr = k0 + j;
+          if (!wait(&full[kr % RING], (kr / RING) & 1u)) {
+            go = false;
+            break;
           }
-          const uint32_t acc = t % NACC;
-          if (go && t >= NACC && !wait(&acc_empty[acc], ((t / NACC) - 1) & 1u)) go = false;
-          if (!go) break;
-          tc_fence_after();
-          const uint32_t d = tmem + acc * 32;
-#pragma unroll
-          for (int pz = 0; pz < 3; ++pz) {
-#pragma unroll
-            for (int py = 0; py < 3; ++py) {
-#pragma unroll
-              for (int dx = 0; dx < 3; ++dx) {
-                const int tap = (pz * 3 + py) * 3 + dx;
-#pragma unroll
-                for (int kc = 0; kc < KSTEP_PER_TAP; ++kc) {
-                  const int s = tap * KSTEP_PER_TAP + kc;
-                  // plane pz of row y-1+py: + pz * CB blocks; K step kc: + 2 kc blocks; tap dx: + dx voxels
-                  const uint64_t ad = arow[py] + (uint64_t)(((pz * CB + 2 * kc) * CBLK + dx * 16) >> 4);
-                  const uint64_t bd = b_desc0 + (uint64_t)((2 * s * N * 16) >> 4);
-                  umma_bf16(d, ad, bd, IDESC, s ? 1u : 0u);
-                }
-              }
+          if (j <= u.ny - 1) {  // first contribution to output row T0 + j: its slot must be free
+            const uint32_t Tn = T0 + j;
+            if (Tn >= RACC && !wait(&slot_empty[slot_of(Tn)], ((Tn / RACC) - 1) & 1u)) {
+              go = false;
+              break;
             }
           }
-          umma_commit(&acc_full[acc]);
-          // release the rows whose last user is this tile
-          const int nrel = (i < u.ny - 1) ? 1 : 3;
-          for (int r = 0; r < nrel; ++r) umma_commit(&empty[(k0 + i + r) % RING]);
+          tc_fence_after();
+          const uint64_t arow = smem_desc(slab0 + (kr % RING) * SLOT_BYTES, CBLK, 128);
+          const int dlo = max(0, j - u.ny + 1), dhi = min(2, j);
+          // runs of adjacent accumulator slots: split where the ring wraps
+          int s0 = dlo;
+          for (int dy = dlo; dy <= dhi; ++dy) {
+            const uint32_t sl = slot_of(T0 + j - dy);
+            if (dy < dhi && sl != RACC - 1) continue;
+            const int nrun = dy - s0 + 1;
+            const uint32_t d = tmem + slot_of(T0 + j - s0) * N;
+            const uint32_t idesc = idesc_bf16_f32(CONV_M, nrun * N);
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx) {
+#pragma unroll
+              for (int kc = 0; kc < KSTEPS; ++kc) {
+                const uint64_t ad = arow + (uint64_t)(((2 * kc) * CBLK + dx * 16) >> 4);
+                const uint64_t bd = smem_desc(w0 + (uint32_t)(((dx * KB + 2 * kc) * NR + s0 * N) * 16), NR * 16, 128);
+                umma_bf16(d, ad, bd, idesc, 1u);
+              }
+            }
+            s0 = dy + 1;
+          }
+          umma_commit(&empty[kr % RING]);                                     // the input row is used once
+          if (j >= 2) umma_commit(&slot_full[slot_of(T0 + j - 2)]);            // output row j - 2 is complete
         }
         k0 += u.ny + 2;
+        T0 += u.ny;
       }
     }
   } else {
     // ---- epilogue: warp w reads TMEM lane quarter w % 4 (voxels x0 + 32 (w % 4) + lane) and
-    // output channels [NC (w / 4), + NC) -------------------------------------------------------
-    const int q = warp & 3, half = warp >> 2;
+    // output channels [NC (w / 4), + NC) of the output row's slot ---------------------------------
     const int c0 = half * NC;
     const bool active = !(EPI == EPI_OUT && half == 1);  // three output channels: first half only
-    uint32_t t = 0;
+    uint32_t T = 0;
     bool go = true;
     for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
       const ConvUnit u = conv_unit(a, unit);
       const size_t bbase = (size_t)u.b * G * G * G;
-      for (int i = 0; i < u.ny; ++i, ++t) {
-        const uint32_t acc = t % NACC;
-        if (!wait(&acc_full[acc], (t / NACC) & 1u)) {
+      for (int i = 0; i < u.ny; ++i, ++T) {
+        const uint32_t sl = slot_of(T);
+        if (!wait(&slot_full[sl], (T / RACC) & 1u)) {
           go = false;
           break;
         }
         tc_fence_after();
-        if (active) {
-          float v[NC];
-          const uint32_t taddr = tmem + acc * 32 + (uint32_t)(half * NC) + ((uint32_t)(q * 32) << 16);
-          if constexpr (NC == 16) tmem_ld16(taddr, v);
-          else tmem_ld8(taddr, v);
-          const int y = u.ya + i;
-          const int x = u.x0 + q * 32 + lane;
-          if (x < G) {
-            const size_t vox = bbase + ((size_t)u.z * G + y) * G + x;
-            if constexpr (EPI == EPI_FWD) {
-              const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N + c0;
-              bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N + c0;
+        float v[NC];
+        const uint32_t taddr = tmem + sl * N + (uint32_t)c0 + ((uint32_t)(q * 32) << 16);
+        if constexpr (NC == 16) {
+          tmem_ld16(taddr, v);
+          tmem_zero16(taddr);
+        } else {
+          tmem_ld8(taddr, v);
+          tmem_zero8(taddr);
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&slot_empty[sl]);
+        const int y = u.ya + i;
+        const int x = u.x0 + q * 32 + lane;
+        if (active && x < G) {
+          const size_t vox = bbase + ((size_t)u.z * G + y) * G + x;
+          if constexpr (EPI == EPI_FWD) {
+            const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N + c0;
+            bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N + c0;
 #pragma unroll
-              for (int n = 0; n < NC; n += 8) {
-                uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
-                const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
-                __align__(16) __nv_bfloat162 ho[4], zo[4];
+            for (int n = 0; n < NC; n += 8) {
+              uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
+              const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
+              __align__(16) __nv_bfloat162 ho[4], zo[4];
 #pragma unroll
-                for (int q2 = 0; q2 < 4; ++q2) {
-                  const float z0 = v[n + 2 * q2] + bias[c0 + n + 2 * q2];
-                  const float z1 = v[n + 2 * q2 + 1] + bias[c0 + n + 2 * q2 + 1];
-                  ho[q2] = __floats2bfloat162_rn(__bfloat162float(hp[q2].x) + gelu_f(z0),
-                                                 __bfloat162float(hp[q2].y) + gelu_f(z1));
-                  zo[q2] = __floats2bfloat162_rn(z0, z1);
-                }
-                *reinterpret_cast<uint4 *>(hout + n) = *reinterpret_cast<uint4 *>(ho);
-                if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint4 *>(zo);
+              for (int q2 = 0; q2 < 4; ++q2) {
+                const float z0 = v[n + 2 * q2] + bias[c0 + n + 2 * q2];
+                const float z1 = v[n + 2 * q2 + 1] + bias[c0 + n + 2 * q2 + 1];
+                ho[q2] = __floats2bfloat162_rn(__bfloat162float(hp[q2].x) + gelu_f(z0),
+                                               __bfloat162float(hp[q2].y) + gelu_f(z1));
+                zo[q2] = __floats2bfloat162_rn(z0, z1);
               }
-            } else if constexpr (EPI == EPI_OUT) {
-              float4 *F = reinterpret_cast<float4 *>(out0) + vox;
-              float4 f = *F;
-              f.x += a.out_scale * (v[0] + bias[0]);
-              f.y += a.out_scale * (v[1] + bias[1]);
-              f.z += a.out_scale * (v[2] + bias[2]);
-              *F = f;
-            } else {
-              const float *rin = reinterpret_cast<const float *>(resid);
-              float *gout = reinterpret_cast<float *>(out0) + vox * N + c0;
+              *reinterpret_cast<uint4 *>(hout + n) = *reinterpret_cast<uint4 *>(ho);
+              if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint4 *>(zo);
+            }
+          } else if constexpr (EPI == EPI_OUT) {
+            float4 *F = reinterpret_cast<float4 *>(out0) + vox;
+            float4 f = *F;
+            f.x += a.out_scale * (v[0] + bias[0]);
+            f.y += a.out_scale * (v[1] + bias[1]);
+            f.z += a.out_scale * (v[2] + bias[2]);
+            *F = f;
+          } else {
+            const float *rin = reinterpret_cast<const float *>(resid);
+            float *gout = reinterpret_cast<float *>(out0) + vox * N + c0;
 #pragma unroll
-              for (int n = 0; n < NC; n += 4) {
-                float4 g = make_float4(v[n], v[n + 1], v[n + 2], v[n + 3]);
-                if (rin) {
-                  const float4 r = *reinterpret_cast<const float4 *>(rin + vox * N + c0 + n);
-                  g.x += r.x;
-                  g.y += r.y;
-                  g.z += r.z;
-                  g.w += r.w;
-                }
-                *reinterpret_cast<float4 *>(gout + n) = g;
-                if (out1) {
-                  const bf16 *zp = zprev + vox * N + c0 + n;
-                  const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(zp);
-                  const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(zp + 2);
-                  __align__(8) __nv_bfloat162 o[2];
-                  o[0] = __floats2bfloat162_rn(g.x * gelu_grad(__bfloat162float(z01.x)),
-                                               g.y * gelu_grad(__bfloat162float(z01.y)));
-                  o[1] = __floats2bfloat162_rn(g.z * gelu_grad(__bfloat162float(z23.x)),
-                                               g.w * gelu_grad(__bfloat162float(z23.y)));
-                  *reinterpret_cast<uint2 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint2 *>(o);
-                }
+            for (int n = 0; n < NC; n += 4) {
+              float4 g = make_float4(v[n], v[n + 1], v[n + 2], v[n + 3]);
+              if (rin) {
+                const float4 r = *reinterpret_cast<const float4 *>(rin + vox * N + c0 + n);
+                g.x += r.x;
+                g.y += r.y;
+                g.z += r.z;
+                g.w += r.w;
+              }
+              *reinterpret_cast<float4 *>(gout + n) = g;
+              if (out1) {
+                const bf16 *zp = zprev + vox * N + c0 + n;
+                const __nv_bfloat162 z01 = *reinterpret_cast<const __nv_bfloat162 *>(zp);
+                const __nv_bfloat162 z23 = *reinterpret_cast<const __nv_bfloat162 *>(zp + 2);
+                __align__(8) __nv_bfloat162 o[2];
+                o[0] = __floats2bfloat162_rn(g.x * gelu_grad(__bfloat162float(z01.x)),
+                                             g.y * gelu_grad(__bfloat162float(z01.y)));
+                o[1] = __floats2bfloat162_rn(g.z * gelu_grad(__bfloat162float(z23.x)),
+                                             g.w * gelu_grad(__bfloat162float(z23.y)));
+                *reinterpret_cast<uint2 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint2 *>(o);
               }
             }
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&acc_empty[acc]);
       }
     }
   }
@@ -356,7 +387,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
   if (tid == 0 && *abort_flag) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, NACC * 32);
+    tmem_dealloc(tmem, TMEM_COLS);
   }
 }
 
@@ -661,13 +692,35 @@ __global__ void reduce_partials_kernel(const float *__restrict__ partial, int np
 // [k/8][N][8] with k = tap * CIN + c (zero padded to CIN x N). flip = 1 builds the data-
 // gradient operand: B'[c][k' = tap * Nreal_in + n] = w[n][26 - tap][c] (roles swapped).
 // ---------------------------------------------------------------------------------------
+// fp32 w[n][tap][c] -> bf16 tensor-core B operand. 3-channel-padded layers (CIN >= 16) use the
+// row layout of conv_tc_kernel: for each dx a K x NR block, K = (dz, c) = 3 CIN, NR = (dy, n) =
+// 3 N, stored [dx][K / 8][NR][8]. The input layer (CIN = 2) uses the flat layout K = (tap, c)
+// of conv_in_tc_kernel, [K / 8][N][8]. flip builds the data-gradient operand (taps mirrored,
+// input and output channels exchanged).
 __global__ void prep_weights_kernel(const float *__restrict__ w, int Nreal, int Creal, int CIN, int N, int flip,
                                     bf16 *__restrict__ out) {
-  const int K = 27 * CIN;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= K * N) return;
-  const int n = e / K, k = e % K;
-  const int tap = k / CIN, c = k % CIN;
+  if (e >= 27 * CIN * N) return;
+  int tap, c, n;
+  size_t idx;
+  if (CIN < 8) {  // flat K = tap * CIN + c
+    const int K = 27 * CIN;
+    n = e / K;
+    const int k = e % K;
+    tap = k / CIN;
+    c = k % CIN;
+    idx = ((size_t)(k / 8) * N + n) * 8 + (k % 8);
+  } else {  // rows: e = ((dx * K) + k) * NR + nr
+    const int K = 3 * CIN, NR = 3 * N;
+    const int dx = e / (K * NR);
+    const int rem = e % (K * NR);
+    const int k = rem / NR, nr = rem % NR;
+    const int dz = k / CIN, dy = nr / N;
+    c = k % CIN;
+    n = nr % N;
+    tap = (dz * 3 + dy) * 3 + dx;
+    idx = (((size_t)dx * (K / 8) + k / 8) * NR + nr) * 8 + (k % 8);
+  }
   float v = 0.f;
   if (!flip) {
     if (n < Nreal && c < Creal) v = w[(n * 27 + tap) * Creal + c];
@@ -676,7 +729,7 @@ __global__ void prep_weights_kernel(const float *__restrict__ w, int Nreal, int 
     // reduction channel c is forward output channel c
     if (c < Nreal && n < Creal) v = w[(c * 27 + (26 - tap)) * Creal + n];
   }
-  out[((size_t)(k / 8) * N + n) * 8 + (k % 8)] = __float2bfloat16_rn(v);
+  out[idx] = __float2bfloat16_rn(v);
 }
 
 // x (B, G^3, 2) bf16 from the density and potential grids: x0 = log(1 + rho_scale * rho)

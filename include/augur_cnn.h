@@ -65,7 +65,9 @@ int augur_cnn_wgrad(int kind, const void *h, const void *dz, int batch, int grid
 /*
  * fp32 w[n][tap][c] (n < n_out, c < c_in) -> bf16 tensor-core operand with cin_pad
  * reduction channels and n_pad output channels; flip = 1 builds the data-gradient operand
- * (taps mirrored, input and output channels exchanged).
+ * (taps mirrored, input and output channels exchanged). cin_pad >= 16: the layout of
+ * augur_cnn_conv_tc (per dx, K = (dz, channel), N = (dy, output channel)); cin_pad = 2: the
+ * input layer's (K = (tap, channel) padded to 64, into a zeroed 64 x n_pad buffer).
  */
 int augur_cnn_prep_weights(const float *w, int n_out, int c_in, int cin_pad, int n_pad, int flip, void *out,
                            void *stream);
