@@ -303,6 +303,23 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
       const size_t bbase = (size_t)u.b * G * G * G;
       for (int i = 0; i < u.ny; ++i, ++T) {
         const uint32_t sl = slot_of(T);
+        const int y = u.ya + i;
+        const int x = u.x0 + q * 32 + lane;
+        const bool mine = active && x < G;
+        const size_t vox = bbase + ((size_t)u.z * G + y) * G + x;
+        // the residual / force-grid values this thread adds to are loaded before the wait, so
+        // their latency overlaps the row's MMAs
+        uint4 hpre[EPI == EPI_FWD ? NC / 8 : 1];
+        float4 fpre = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (EPI == EPI_FWD) {
+          if (mine) {
+#pragma unroll
+            for (int n = 0; n < NC; n += 8)
+              hpre[n / 8] = *reinterpret_cast<const uint4 *>(reinterpret_cast<const bf16 *>(resid) + vox * N + c0 + n);
+          }
+        } else if constexpr (EPI == EPI_OUT) {
+          if (mine) fpre = reinterpret_cast<const float4 *>(out0)[vox];
+        }
         if (!wait(&slot_full[sl], (T / RACC) & 1u)) {
           go = false;
           break;
@@ -321,16 +338,12 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&slot_empty[sl]);
-        const int y = u.ya + i;
-        const int x = u.x0 + q * 32 + lane;
-        if (active && x < G) {
-          const size_t vox = bbase + ((size_t)u.z * G + y) * G + x;
+        if (mine) {
           if constexpr (EPI == EPI_FWD) {
-            const bf16 *hin = reinterpret_cast<const bf16 *>(resid) + vox * N + c0;
             bf16 *hout = reinterpret_cast<bf16 *>(out0) + vox * N + c0;
 #pragma unroll
             for (int n = 0; n < NC; n += 8) {
-              uint4 hv = *reinterpret_cast<const uint4 *>(hin + n);
+              uint4 hv = hpre[n / 8];
               const __nv_bfloat162 *hp = reinterpret_cast<const __nv_bfloat162 *>(&hv);
               __align__(16) __nv_bfloat162 ho[4], zo[4];
 #pragma unroll
@@ -345,12 +358,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
               if (out1) *reinterpret_cast<uint4 *>(out1 + vox * N + c0 + n) = *reinterpret_cast<uint4 *>(zo);
             }
           } else if constexpr (EPI == EPI_OUT) {
-            float4 *F = reinterpret_cast<float4 *>(out0) + vox;
-            float4 f = *F;
+            float4 f = fpre;
             f.x += a.out_scale * (v[0] + bias[0]);
             f.y += a.out_scale * (v[1] + bias[1]);
             f.z += a.out_scale * (v[2] + bias[2]);
-            *F = f;
+            reinterpret_cast<float4 *>(out0)[vox] = f;
           } else {
             const float *rin = reinterpret_cast<const float *>(resid);
             float *gout = reinterpret_cast<float *>(out0) + vox * N + c0;
