@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
 // full/empty mbarriers; the epilogue is the forward layers' (eight warps, two per TMEM lane
 // quarter). Weights: augur_cnn_prep_weights(w_in, 32, 2, 2, 32, 0) into a zeroed 64 x 32 buffer.
 // ---------------------------------------------------------------------------------------
-constexpr int IN_PROD_WARPS = 4;                        // 128 producer threads: one per voxel row
+constexpr int IN_PROD_WARPS = 8;                        // 256 producer threads: two per voxel row
 constexpr int IN_STAGES = 4;                            // A buffers in flight
 constexpr int IN_KB = 8;                                // 16-byte K blocks (64 K values)
 constexpr int IN_ABYTES = IN_KB * CONV_M * 16;          // 16 KB per A buffer
@@ -474,8 +474,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
   };
 
   if (warp > MMA_WARP) {
-    // ---- producers: thread r builds row r of the tile's A operand ---------------------------
-    const int r = tid - 32 * (MMA_WARP + 1);
+    // ---- producers: threads r and r + 128 build row r of the tile's A operand (K blocks 0-3
+    // and 4-6 respectively) ---------------------------------------------------------------------
+    const int pr = tid - 32 * (MMA_WARP + 1);
+    const int r = pr & (CONV_M - 1), kh = pr >> 7;
     const uint32_t *x32 = reinterpret_cast<const uint32_t *>(x);  // two bf16 channels per voxel
     uint32_t t = 0;
     bool go = true;
@@ -490,20 +492,22 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
           break;
         }
         const int y = u.ya + i;
-        uint32_t v[28];
+        const int t0 = kh * 16;  // taps t0 .. t0 + 15 (K blocks 4 kh .. 4 kh + 3; tap 27 is padding)
+        uint32_t v[16];
 #pragma unroll
-        for (int tap = 0; tap < 27; ++tap) {
+        for (int tt = 0; tt < 16; ++tt) {
+          const int tap = t0 + tt;
           const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
           const int zz = u.z + dz, yy = y + dy, xq = xx + dx;
-          const bool in = zz >= 0 && zz < G && yy >= 0 && yy < G && xq >= 0 && xq < G;
-          v[tap] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
+          const bool in = tap < 27 && zz >= 0 && zz < G && yy >= 0 && yy < G && xq >= 0 && xq < G;
+          v[tt] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
         }
-        v[27] = 0u;
         unsigned char *A = sA + (size_t)st * IN_ABYTES;
 #pragma unroll
-        for (int kb = 0; kb < 7; ++kb)
-          *reinterpret_cast<uint4 *>(A + ((size_t)kb * CONV_M + r) * 16) =
-              make_uint4(v[4 * kb], v[4 * kb + 1], v[4 * kb + 2], v[4 * kb + 3]);
+        for (int kb = 0; kb < 4; ++kb)
+          if (4 * kh + kb < 7)
+            *reinterpret_cast<uint4 *>(A + ((size_t)(4 * kh + kb) * CONV_M + r) * 16) =
+                make_uint4(v[4 * kb], v[4 * kb + 1], v[4 * kb + 2], v[4 * kb + 3]);
         fence_async_smem();  // generic-proxy stores -> visible to the tensor core
         mbar_arrive(&full[st]);
       }
