@@ -48,7 +48,7 @@ SIGNATURES = {
     "augur_energy_fp64": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp]),
     "augur_direct_sum_fp64_noalloc": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _vp, _vp]),
     # include/augur_cnn.h
-    "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp]),
+    "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp, _vp]),
     "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     "augur_cnn_conv_in_tc": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "augur_cnn_wgrad": (_i32, [_i32, _vp, _vp, _i32, _i32, _vp, _i32, _vp, _vp]),

@@ -149,8 +149,10 @@ class GridCNN:
         return x
 
     # ---- forward / backward -------------------------------------------------------------------
-    def forward(self, x: torch.Tensor, B: int, G: int, field4: torch.Tensor, train: bool = False) -> None:
-        """field4 (B*G^3*4 floats) lanes 0..2 += out_scale * net(x)."""
+    def forward(self, x: torch.Tensor, B: int, G: int, field4: torch.Tensor, train: bool = False,
+                stats: torch.Tensor | None = None) -> None:
+        """field4 (B*G^3*4 floats) lanes 0..2 += out_scale * net(x). stats (float64 (2,), device):
+        += (sum |correction|^2, sum |field4 lanes 0..2 before the correction|^2)."""
         ws = self._workspace(B, G, train)
         h, z = ws["h"], ws.get("z")
         self._call("augur_cnn_conv_in_tc", x.data_ptr(), self.op_in.data_ptr(), self.view["b_in"].data_ptr(),
@@ -158,10 +160,10 @@ class GridCNN:
         for i in range(3):
             self._call("augur_cnn_conv_tc", 0, h[i].data_ptr(), self.op_fwd_mid[i].data_ptr(),
                        self.view[f"b_mid{i}"].data_ptr(), h[i].data_ptr(), None, h[i + 1].data_ptr(),
-                       _p(z[i + 1]) if train else None, B, G, 1.0, self.err.data_ptr())
+                       _p(z[i + 1]) if train else None, B, G, 1.0, self.err.data_ptr(), None)
         self._call("augur_cnn_conv_tc", 1, h[3].data_ptr(), self.op_fwd_out.data_ptr(),
                    self.view["b_out"].data_ptr(), None, None, field4.data_ptr(), None, B, G, self.out_scale,
-                   self.err.data_ptr())
+                   self.err.data_ptr(), _p(stats))
         self._x = x
 
     def backward(self, dfield4: torch.Tensor, B: int, G: int) -> None:
@@ -182,7 +184,7 @@ class GridCNN:
         self.gview["b_out"].copy_(gw[4 * 27 * W:4 * 27 * W + 3] * s)
         self._call("augur_cnn_pack_dout", dfield4.data_ptr(), nv, s, ws["dout16"].data_ptr())
         self._call("augur_cnn_conv_tc", 3, ws["dout16"].data_ptr(), self.op_bwd_out.data_ptr(), None, None,
-                   z[3].data_ptr(), dh[1].data_ptr(), dz[1].data_ptr(), B, G, 1.0, self.err.data_ptr())
+                   z[3].data_ptr(), dh[1].data_ptr(), dz[1].data_ptr(), B, G, 1.0, self.err.data_ptr(), None)
         cur = 1
         for i in (2, 1, 0):  # middle layer i maps h[i] -> h[i+1]
             gm = torch.empty(W * 27 * W + W, dtype=torch.float32, device=self.device)
@@ -193,7 +195,7 @@ class GridCNN:
             nxt = 1 - cur
             self._call("augur_cnn_conv_tc", 2, dz[cur].data_ptr(), self.op_bwd_mid[i].data_ptr(), None,
                        dh[cur].data_ptr(), z[i].data_ptr(), dh[nxt].data_ptr(), dz[nxt].data_ptr(), B, G, 1.0,
-                       self.err.data_ptr())
+                       self.err.data_ptr(), None)
             cur = nxt
         gi = torch.empty(W * 27 * 2 + W, dtype=torch.float32, device=self.device)
         self._call("augur_cnn_wgrad", 2, self._x.data_ptr(), dz[cur].data_ptr(), B, G, self._partial.data_ptr(),

@@ -139,7 +139,8 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
                                                                   const void *__restrict__ resid,
                                                                   const bf16 *__restrict__ zprev,
                                                                   void *__restrict__ out0, bf16 *__restrict__ out1,
-                                                                  ConvArgs a, unsigned *__restrict__ err) {
+                                                                  ConvArgs a, unsigned *__restrict__ err,
+                                                                  double *__restrict__ stats) {
   constexpr int CB = CIN / 8;              // 16-byte channel blocks per voxel
   constexpr int KB = 3 * CB;               // K blocks of an input row (three planes)
   constexpr int KSTEPS = KB / 2;           // K = 16 per MMA
@@ -212,6 +213,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
     return false;
   };
 
+  double s_corr_out = 0.0, s_pm_out = 0.0;  // EPI_OUT with stats: sums over this thread's voxels
   if (warp == TMA_WARP) {
     // ---- producer: rows ya-1 .. ya+ny of every unit, all three planes ----------------------
     uint32_t k = 0;
@@ -359,9 +361,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
             }
           } else if constexpr (EPI == EPI_OUT) {
             float4 f = fpre;
-            f.x += a.out_scale * (v[0] + bias[0]);
-            f.y += a.out_scale * (v[1] + bias[1]);
-            f.z += a.out_scale * (v[2] + bias[2]);
+            const float cx = a.out_scale * (v[0] + bias[0]), cy = a.out_scale * (v[1] + bias[1]),
+                        cz = a.out_scale * (v[2] + bias[2]);
+            if (stats) {  // |correction|^2 and |PM force|^2 of this voxel, summed below
+              s_corr_out += (double)(cx * cx + cy * cy + cz * cz);
+              s_pm_out += (double)(f.x * f.x + f.y * f.y + f.z * f.z);
+            }
+            f.x += cx;
+            f.y += cy;
+            f.z += cz;
             reinterpret_cast<float4 *>(out0)[vox] = f;
           } else {
             const float *rin = reinterpret_cast<const float *>(resid);
@@ -391,6 +399,20 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
             }
           }
         }
+      }
+    }
+  }
+  if constexpr (EPI == EPI_OUT) {
+    if (stats && warp < EPI_WARPS) {
+      double c = s_corr_out, m = s_pm_out;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+      }
+      if (lane == 0) {
+        atomicAdd(&stats[0], c);
+        atomicAdd(&stats[1], m);
       }
     }
   }
@@ -862,7 +884,8 @@ int make_act_map(CUtensorMap *map, const void *in, int B, int G) {
 
 template <int CIN, int N, int EPI>
 int launch_conv_tc(const void *in, const void *wB, const float *bias, const void *resid, const void *zprev,
-                   void *out0, void *out1, int B, int G, float out_scale, unsigned *err, cudaStream_t st) {
+                   void *out0, void *out1, int B, int G, float out_scale, unsigned *err, double *stats,
+                   cudaStream_t st) {
   ConvArgs a;
   a.B = B;
   a.G = G;
@@ -893,7 +916,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   }
   const int grid = std::min(a.nunits, nsm);
   conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(map, (const bf16 *)wB, bias, resid,
-                                                                (const bf16 *)zprev, out0, (bf16 *)out1, a, err);
+                                                                (const bf16 *)zprev, out0, (bf16 *)out1, a, err, stats);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
 }
 
@@ -954,14 +977,14 @@ extern "C" {
 // output layer (input: 16-channel padded output gradient).
 int augur_cnn_conv_tc(int layer, const void *in, const void *w_umma, const float *bias, const void *resid,
                       const void *zprev, void *out0, void *out1, int batch, int grid, float out_scale,
-                      unsigned *err, void *stream) {
+                      unsigned *err, double *stats, void *stream) {
   if (!in || !w_umma || !out0 || batch < 1 || grid < 3 || !err) return AUGUR_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
   switch (layer) {
-    case 0: return launch_conv_tc<32, 32, EPI_FWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, st);
-    case 1: return launch_conv_tc<32, 16, EPI_OUT>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, out_scale, err, st);
-    case 2: return launch_conv_tc<32, 32, EPI_BWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, st);
-    case 3: return launch_conv_tc<16, 32, EPI_BWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, st);
+    case 0: return launch_conv_tc<32, 32, EPI_FWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, nullptr, st);
+    case 1: return launch_conv_tc<32, 16, EPI_OUT>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, out_scale, err, stats, st);
+    case 2: return launch_conv_tc<32, 32, EPI_BWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, nullptr, st);
+    case 3: return launch_conv_tc<16, 32, EPI_BWD>(in, w_umma, bias, resid, zprev, out0, out1, batch, grid, 1.f, err, nullptr, st);
     default: return AUGUR_EINVAL;
   }
 }

@@ -231,25 +231,43 @@ __global__ void __launch_bounds__(EN_THREADS) energy_partial_kernel(const float 
   }
 }
 
+// Fixed-order fold of the per-block partials: thread t sums a contiguous chunk of blocks
+// (Neumaier-compensated), then a fixed shared-memory tree -- deterministic and parallel (a
+// serial FP64 chain over ~10^4 partials takes milliseconds on this part).
+constexpr int EN_FOLD = 256;
 template <int D>
-__global__ void energy_final_kernel(const double *__restrict__ partial, int nblk, double *__restrict__ out) {
-  // one thread per quantity, fixed order, Neumaier-compensated
-  const int q = threadIdx.x;
-  if (q >= EN_Q) return;
-  double s = 0.0, c = 0.0;
-  for (int b = 0; b < nblk; ++b) {
-    double v = partial[(size_t)b * EN_Q + q];
-    double t = s + v;
-    c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
-    s = t;
+__global__ void __launch_bounds__(EN_FOLD) energy_final_kernel(const double *__restrict__ partial, int nblk,
+                                                              double *__restrict__ out) {
+  __shared__ double sh[EN_Q][EN_FOLD];
+  const int t = threadIdx.x;
+  const int per = (nblk + EN_FOLD - 1) / EN_FOLD;
+  const int b0 = min(nblk, t * per), b1 = min(nblk, b0 + per);
+  for (int q = 0; q < EN_Q; ++q) {
+    double s = 0.0, c = 0.0;
+    for (int b = b0; b < b1; ++b) {
+      const double v = partial[(size_t)b * EN_Q + q];
+      const double u = s + v;
+      c += (fabs(s) >= fabs(v)) ? (s - u) + v : (v - u) + s;
+      s = u;
+    }
+    sh[q][t] = s + c;
   }
-  s += c;
-  // out layout: ke, p[0..D-1], mass, pe
-  if (q == 0) out[0] = s;
-  else if (q <= 3) {
-    if (q - 1 < D) out[q] = s;
-  } else if (q == 4) out[D + 1] = s;
-  else out[D + 2] = s;
+  __syncthreads();
+  for (int w = EN_FOLD / 2; w > 0; w >>= 1) {
+    if (t < w)
+      for (int q = 0; q < EN_Q; ++q) sh[q][t] += sh[q][t + w];
+    __syncthreads();
+  }
+  if (t < EN_Q) {
+    const int q = t;
+    const double s = sh[q][0];
+    // out layout: ke, p[0..D-1], mass, pe
+    if (q == 0) out[0] = s;
+    else if (q <= 3) {
+      if (q - 1 < D) out[q] = s;
+    } else if (q == 4) out[D + 1] = s;
+    else out[D + 2] = s;
+  }
 }
 
 // ---- allocation-free variant ------------------------------------------------------------
@@ -366,10 +384,10 @@ int augur_energy_fp64(const float *vel, const float *mass, const float *mask, co
   if (cudaMallocAsync(&partial, sizeof(double) * EN_Q * nblk, st) != cudaSuccess) return AUGUR_ENOMEM;
   if (dim == 3) {
     energy_partial_kernel<3><<<nblk, EN_THREADS, 0, st>>>(vel, mass, mask, phi, n, partial);
-    energy_final_kernel<3><<<1, 32, 0, st>>>(partial, nblk, out);
+    energy_final_kernel<3><<<1, EN_FOLD, 0, st>>>(partial, nblk, out);
   } else {
     energy_partial_kernel<2><<<nblk, EN_THREADS, 0, st>>>(vel, mass, mask, phi, n, partial);
-    energy_final_kernel<2><<<1, 32, 0, st>>>(partial, nblk, out);
+    energy_final_kernel<2><<<1, EN_FOLD, 0, st>>>(partial, nblk, out);
   }
   cudaError_t e = cudaGetLastError();
   cudaFreeAsync(partial, st);

@@ -792,7 +792,7 @@ static int run_gather(augur_pm_plan *p, float kick, int drift, float *acc_out, c
                                                  nullptr, p->key, p->slot, p->row_count, p->d_err);
   AUGUR_LAUNCH_CHECK(p);
   if (energy_out) {
-    energy_fold_kernel<<<1, 32, 0, st>>>(p->epart, (int)nb, energy_out);
+    energy_fold_kernel<<<1, FOLD_THREADS, 0, st>>>(p->epart, (int)nb, energy_out);
     AUGUR_LAUNCH_CHECK(p);
   }
   return AUGUR_OK;

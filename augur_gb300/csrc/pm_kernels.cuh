@@ -1083,17 +1083,36 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
 }
 
 // Fixed-order sum of the gather's per-block energy partials: out[0] kinetic, out[1] potential.
-__global__ void energy_fold_kernel(const double *__restrict__ epart, int nblk, double *__restrict__ out) {
-  const int q = threadIdx.x;
-  if (q >= 2) return;
-  double s = 0.0, c = 0.0;
-  for (int b = 0; b < nblk; ++b) {
-    const double v = epart[(size_t)b * 2 + q];
-    const double t = s + v;
-    c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
-    s = t;
+// Fixed-order fold of the per-block energy partials: thread t sums a contiguous chunk
+// (compensated), then a shared-memory tree in a fixed pattern -- deterministic, and parallel
+// (a serial FP64 chain over ~10^4 partials takes milliseconds on this part).
+constexpr int FOLD_THREADS = 1024;
+__global__ void __launch_bounds__(FOLD_THREADS) energy_fold_kernel(const double *__restrict__ epart, int nblk,
+                                                                   double *__restrict__ out) {
+  __shared__ double sh[2][FOLD_THREADS];
+  const int t = threadIdx.x;
+  const int per = (nblk + FOLD_THREADS - 1) / FOLD_THREADS;
+  const int b0 = min(nblk, t * per), b1 = min(nblk, b0 + per);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    double s = 0.0, c = 0.0;
+    for (int b = b0; b < b1; ++b) {
+      const double v = epart[(size_t)b * 2 + q];
+      const double u = s + v;
+      c += (fabs(s) >= fabs(v)) ? (s - u) + v : (v - u) + s;
+      s = u;
+    }
+    sh[q][t] = s + c;
   }
-  out[q] = s + c;
+  __syncthreads();
+  for (int w = FOLD_THREADS / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      sh[0][t] += sh[0][t + w];
+      sh[1][t] += sh[1][t + w];
+    }
+    __syncthreads();
+  }
+  if (t < 2) out[t] = sh[t][0];
 }
 
 // Write the sorted state back to the caller's order (end of a run).

@@ -197,30 +197,30 @@ class CorrectedPM:
         self.check_every = check_every
         G = plan.grid
         self.rho = torch.empty((G,) * 3, device=plan.device)
-        self.energy = torch.zeros(2, dtype=torch.float64, device=plan.device)
+        # (kinetic, potential, sum |correction|^2, sum |PM force|^2): read back together, once per check
+        self.energy = torch.zeros(4, dtype=torch.float64, device=plan.device)
         self.nstep = 0
         self.last_energy = None
+        self._stats_due = False
 
     def _grid(self, check: bool):
         use = self.net is not None and not self.monitor.reverted
         F4 = self.plan.run_grid(self.rho if use else None, with_phi=use or check)
         if use:
-            pm_rms = None
+            stats = None
             if check:
-                pm_rms = float(F4[..., :3].pow(2).sum(-1).mean().sqrt())
-                before = F4[..., :3].clone()
+                stats = self.energy[2:]
+                stats.zero_()
+                self._stats_due = True
             x = self.net.input(self.rho, F4)
-            self.net.forward(x, 1, self.plan.grid, F4.view(-1))
-            if check:
-                corr = float((F4[..., :3] - before).pow(2).sum(-1).mean().sqrt())
-                self.monitor.observe(corr_ratio=corr / max(pm_rms, 1e-30))
+            self.net.forward(x, 1, self.plan.grid, F4.view(-1), stats=stats)
         return F4
 
     def begin(self, pos, vel, mass=None, mask=None, dt: float = 5e-4):
         self.dt = dt
         self.plan.run_load(pos, vel, mass, mask, dt=dt)
         self._grid(True)
-        self.plan.run_kick(0.5 * dt, True, energy_out=self.energy, esync=0.0)
+        self.plan.run_kick(0.5 * dt, True, energy_out=self.energy[:2], esync=0.0)
         self._record()
 
     def steps(self, k: int):
@@ -229,18 +229,24 @@ class CorrectedPM:
             check = self.check_every > 0 and self.nstep % self.check_every == 0
             self._grid(check)
             if check:
-                self.plan.run_kick(self.dt, True, energy_out=self.energy, esync=0.5 * self.dt)
+                self.plan.run_kick(self.dt, True, energy_out=self.energy[:2], esync=0.5 * self.dt)
                 self._record()
             else:
                 self.plan.run_kick(self.dt, True)
 
     def end(self, pos, vel):
         self._grid(True)
-        self.plan.run_kick(0.5 * self.dt, False, energy_out=self.energy, esync=0.5 * self.dt)
+        self.plan.run_kick(0.5 * self.dt, False, energy_out=self.energy[:2], esync=0.5 * self.dt)
         self._record()
         self.plan.run_unload(pos, vel)
 
     def _record(self):
-        ke, pe = self.energy.tolist()
+        """One host read per check: the energy taps and, when the network ran, the correction
+        and PM-force norms accumulated by its output layer."""
+        ke, pe, c2, f2 = self.energy.tolist()
         self.last_energy = ke + pe
-        self.monitor.observe(energy=self.last_energy)
+        corr = None
+        if self._stats_due:
+            corr = math.sqrt(c2 / max(f2, 1e-300))
+            self._stats_due = False
+        self.monitor.observe(energy=self.last_energy, corr_ratio=corr)

@@ -31,11 +31,14 @@ extern "C" {
  *            out1 = out0 * gelu'(zprev) (bf16)
  *   layer 3: data gradient of the output layer (in: 16-channel padded output gradient), as layer 2
  * w_umma: weights prepared by augur_cnn_prep_weights for that layer.
+ * stats (layer 1 only, may be NULL): stats[0] += sum |correction|^2, stats[1] += sum |force|^2
+ * of the grid before the correction, over all voxels (doubles; the fallback monitor's
+ * correction-size check without another pass over the grid).
  * Replaces the nn.Conv3d calls of LocalNet.forward / autograd backward.
  */
 int augur_cnn_conv_tc(int layer, const void *in, const void *w_umma, const float *bias, const void *resid,
                       const void *zprev, void *out0, void *out1, int batch, int grid, float out_scale,
-                      unsigned *err, void *stream);
+                      unsigned *err, double *stats, void *stream);
 
 /* Input layer 2 -> 32 on the CUDA cores: z0 = conv(x) + bias, h0 = gelu(z0), both bf16. */
 int augur_cnn_conv_in(const void *x, const float *w, const float *bias, int batch, int grid, void *z0, void *h0,
