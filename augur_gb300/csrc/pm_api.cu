@@ -49,6 +49,9 @@ struct augur_pm_plan {
   float4 *F4;      // force grid in use: F4_own, or a caller's buffer bound by augur_pm_plan_bind_force_grid
   float4 *F4_own;
   float *real_tmp, *phi2d, *rho2d;
+  float *phi_ext;  // isolated, kpad = "ext": potential at rows/columns -1 .. G, (G+2)^2
+  float *kparams;  // learned kernel MLP parameters (device copy)
+  int kpad_ext;
   int64_t run_n;
   float run_dt;
   int run_active;
@@ -263,7 +266,7 @@ int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   AUGUR_LAUNCH_CHECK(p);
   rc = fft_rows(p, p->spec3, (int64_t)ncomp * (M + 1) * G, true, st);
   if (rc) return rc;
-  C2RArgs ca;
+  C2RArgs ca{};
   ca.L = G;
   ca.nrows = G * G;
   ca.RB = p->c2r_RB;
@@ -312,7 +315,7 @@ int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream
   AUGUR_LAUNCH_CHECK(p);
   rc = fft_rows(p, p->spec, (int64_t)(p->M + 1), true, st);
   if (rc) return rc;
-  C2RArgs ca;
+  C2RArgs ca{};
   ca.L = L;
   ca.nrows = L;
   ca.RB = p->c2r_RB;
@@ -327,6 +330,16 @@ int isolated_from_rho(augur_pm_plan *p, const float *rho, float4 *F4, cudaStream
   ca.fdRB = make_fastdiv(ca.RB);
   ca.fdM = make_fastdiv(ca.L / 2);
   ca.fdL = make_fastdiv(ca.L);
+  ca.ext = p->kpad_ext;
+  if (p->kpad_ext) {
+    // rows 0..G and 2G-1 are needed: transform every row (the others are not stored)
+    c2r_rows_kernel<false><<<(unsigned)((L + p->c2r_RB - 1) / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec, ca, p->tw,
+                                                                                                 p->phi_ext);
+    AUGUR_LAUNCH_CHECK(p);
+    fd_grad2d_ext_kernel<<<blocks_for((int64_t)G * G, 256), 256, 0, st>>>(p->phi_ext, G, (float)(2.0 * h), F4);
+    AUGUR_LAUNCH_CHECK(p);
+    return AUGUR_OK;
+  }
   c2r_rows_kernel<false><<<(unsigned)((G + p->c2r_RB - 1) / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec, ca, p->tw,
                                                                                                p->phi2d);
   AUGUR_LAUNCH_CHECK(p);
@@ -501,6 +514,24 @@ int raise_smem_limits(const augur_pm_plan *p) {
   return rc ? AUGUR_ECUDA : AUGUR_OK;
 }
 
+// the isolated plan's kernel spectrum from the lattice in real_tmp
+int lattice_to_khat(augur_pm_plan *p, cudaStream_t st) {
+  const int L = p->L;
+  int rc = r2c_rows(p, p->real_tmp, L, L, L, p->khat, st);
+  if (!rc) rc = fft_rows(p, p->khat, (int64_t)(p->M + 1), false, st);
+  return rc;
+}
+
+// the reference's plain-PM kernel K = -1/sqrt(d^2 + eps^2) (pm_baseline_force_error.py:70-73)
+int softened_kernel(augur_pm_plan *p, cudaStream_t st) {
+  const int L = p->L;
+  kernel_lattice_kernel<<<blocks_for((int64_t)L * L, 256), 256, 0, st>>>(p->real_tmp, L, (float)(p->extent / p->G),
+                                                                         (float)(p->eps * p->eps));
+  AUGUR_LAUNCH_CHECK(p);
+  p->kpad_ext = 0;
+  return lattice_to_khat(p, st);
+}
+
 int check_plan(const augur_pm_plan *p, int64_t n) {
   if (!p) return AUGUR_EINVAL;
   if (n < 0 || n > p->max_n) return AUGUR_EINVAL;
@@ -533,7 +564,7 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
   if (!p) return AUGUR_OK;
   void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
-                  p->F4_own, p->real_tmp, p->phi2d, p->rho2d, p->dep_nch, p->dep_item_off, p->dep_slot_off,
+                  p->F4_own, p->real_tmp, p->phi2d, p->rho2d, p->phi_ext, p->kparams, p->dep_nch, p->dep_item_off, p->dep_slot_off,
                   p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -630,6 +661,8 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
     rc |= dalloc(p, &p->khat, nspec);
     rc |= dalloc(p, &p->real_tmp, (size_t)L * L);
     rc |= dalloc(p, &p->phi2d, ncell);
+    rc |= dalloc(p, &p->phi_ext, (size_t)(G + 2) * (G + 2));
+    rc |= dalloc(p, &p->kparams, (size_t)KMLP_H * KMLP_MAXCOL + KMLP_H * KMLP_H + 3 * KMLP_H + 1);
     rc |= dalloc(p, &p->rho2d, ncell);
   }
   if (rc != AUGUR_OK) {
@@ -656,10 +689,7 @@ int augur_pm_plan_create(augur_pm_plan **out, int dim, int grid, int64_t max_bod
   }
   if (mode == AUGUR_MODE_ISOLATED_SOFTENED) {
     // kernel spectrum rfft2(K) of the 2G min-image lattice, once per plan
-    kernel_lattice_kernel<<<blocks_for((int64_t)L * L, 256), 256>>>(p->real_tmp, L, (float)h,
-                                                                    (float)(eps * eps));
-    rc = r2c_rows(p, p->real_tmp, L, L, L, p->khat, 0);
-    if (!rc) rc = fft_rows(p, p->khat, (int64_t)(M + 1), false, 0);
+    rc = softened_kernel(p, 0);
     if (!rc) rc = cuda_status(cudaDeviceSynchronize());
     if (rc) {
       augur_pm_plan_destroy(p);
@@ -854,6 +884,44 @@ int augur_pm_plan_set_tiles(augur_pm_plan *p, const augur_pm_tiles *t) {
   return raise_smem_limits(p);
 }
 
+int augur_pm_set_kernel_mlp(augur_pm_plan *p, const float *params, int ncol, const float *extra, int n_extra,
+                            int flags, double split_radius, double eps, void *stream) {
+  if (!p || !params) return AUGUR_EINVAL;
+  if (p->mode != AUGUR_MODE_ISOLATED_SOFTENED) return AUGUR_EINVAL;
+  const int nbase = (flags & AUGUR_KERNEL_CELL_UNITS) ? 3 : 2;
+  if (n_extra < 0 || ncol != nbase + n_extra || ncol > KMLP_MAXCOL || (n_extra > 0 && !extra)) return AUGUR_EINVAL;
+  if ((flags & AUGUR_KERNEL_SPLIT) && !(split_radius > 0.0)) return AUGUR_EINVAL;
+  if ((flags & AUGUR_KERNEL_PRIOR) && !(eps >= 0.0)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  const size_t np = (size_t)KMLP_H * ncol + KMLP_H * KMLP_H + 3 * KMLP_H + 1;
+  if (cudaMemcpyAsync(p->kparams, params, np * sizeof(float), cudaMemcpyDefault, st) != cudaSuccess)
+    return AUGUR_ECUDA;
+  KmlpArgs a;
+  a.L = p->L;
+  a.ncol = ncol;
+  a.nbase = nbase;
+  a.flags = ((flags & AUGUR_KERNEL_CELL_UNITS) ? 1 : 0) | ((flags & AUGUR_KERNEL_PRIOR) ? 2 : 0) |
+            ((flags & AUGUR_KERNEL_SPLIT) ? 4 : 0);
+  a.h = (float)(p->extent / p->G);
+  a.split_r = (float)split_radius;
+  a.eps2 = (float)(eps * eps);
+  for (int j = 0; j < KMLP_MAXCOL; ++j) a.extra[j] = j < n_extra ? extra[j] : 0.f;
+  const int L = p->L;
+  kmlp_lattice_kernel<<<blocks_for((int64_t)L * L, 256), 256, np * sizeof(float), st>>>(p->kparams, a, p->real_tmp);
+  AUGUR_LAUNCH_CHECK(p);
+  int rc = lattice_to_khat(p, st);
+  if (rc) return rc;
+  p->kpad_ext = (flags & AUGUR_KERNEL_PAD_EXT) ? 1 : 0;
+  return AUGUR_OK;
+}
+
+int augur_pm_reset_kernel(augur_pm_plan *p, void *stream) {
+  if (!p || p->mode != AUGUR_MODE_ISOLATED_SOFTENED) return AUGUR_EINVAL;
+  p->launches = 0;
+  return softened_kernel(p, S(stream));
+}
+
 int augur_pm_plan_bind_force_grid(augur_pm_plan *p, float *grid4) {
   if (!p) return AUGUR_EINVAL;
   if (p->dim != 3 || p->mode != AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
@@ -958,7 +1026,7 @@ int augur_pm_run_profile(augur_pm_plan *p, int k, float *stage_ms, int nstage, v
     if (!rc) rc = fft_rows(p, p->spec3, (int64_t)3 * (M + 1) * G, true, st);
     cudaEventRecord(ev[5], st);
     if (!rc) {
-      C2RArgs ca;
+      C2RArgs ca{};
       ca.L = G;
       ca.nrows = G * G;
       ca.RB = p->c2r_RB;

@@ -733,6 +733,79 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data
   AUGUR_FFT_IO(L, 0, nr, ld, st, A, B, LS, tw, twmul, inverse != 0);
 }
 
+// 2D isolated, kpad = "ext" (scripts/scatter_field.py:286-288): the central difference reads the
+// potential's wrapped neighbours, E = phi at rows/columns -1 .. G of the 2G transform.
+__global__ void fd_grad2d_ext_kernel(const float *__restrict__ E, int G, float two_h, float4 *__restrict__ F4) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= G * G) return;
+  int y = e / G, x = e - y * G;
+  const int W = G + 2;
+  const float *c = E + (size_t)(y + 1) * W + (x + 1);
+  float gx = __fdiv_rn(__fsub_rn(c[1], c[-1]), two_h);
+  float gy = __fdiv_rn(__fsub_rn(c[W], c[-W]), two_h);
+  F4[e] = make_float4(-gx, -gy, 0.f, c[0]);
+}
+
+// Learned radial kernel on the 2G x 2G minimum-image lattice (ScatterField._kernel_fft,
+// scripts/scatter_field.py:263-272): K = kmlp(features(r)), kmlp = Linear(ncol, 64), GELU,
+// Linear(64, 64), GELU, Linear(64, 1) (torch layouts, exact erf GELU); features [r, log(r + h)]
+// or in cell units [r/h, log(r/h + 1), log(0.5/h)] (:141-151), then the constant extras; prior
+// K = -(1 + K)/sqrt(r^2 + eps^2); split K *= 1 - (1 - min(r/rs, 1)^2)^2.
+constexpr int KMLP_H = 64;
+constexpr int KMLP_MAXCOL = 8;
+struct KmlpArgs {
+  int L, ncol, nbase, flags;
+  float h, split_r, eps2;
+  float extra[KMLP_MAXCOL];
+};
+__global__ void __launch_bounds__(256) kmlp_lattice_kernel(const float *__restrict__ params, KmlpArgs a,
+                                                           float *__restrict__ K) {
+  extern __shared__ float sp[];  // W1 (64 x ncol), b1, W2 (64 x 64), b2, W3 (64), b3
+  const int np = KMLP_H * a.ncol + KMLP_H + KMLP_H * KMLP_H + KMLP_H + KMLP_H + 1;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) sp[i] = params[i];
+  __syncthreads();
+  const float *W1 = sp, *b1 = W1 + KMLP_H * a.ncol, *W2 = b1 + KMLP_H, *b2 = W2 + KMLP_H * KMLP_H;
+  const float *W3 = b2 + KMLP_H, *b3 = W3 + KMLP_H;
+  const int L = a.L;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= L * L) return;
+  const int iy = e / L, ix = e - iy * L;
+  const float dy = (float)min(iy, L - iy) * a.h, dx = (float)min(ix, L - ix) * a.h;
+  const float r = sqrtf(dy * dy + dx * dx);
+  float f[KMLP_MAXCOL];
+  if (a.flags & 1) {  // cell units
+    f[0] = r / a.h;
+    f[1] = logf(r / a.h + 1.0f);
+    f[2] = logf(0.5f / a.h);
+  } else {
+    f[0] = r;
+    f[1] = logf(r + a.h);
+  }
+  for (int j = a.nbase; j < a.ncol; ++j) f[j] = a.extra[j - a.nbase];
+  float h1[KMLP_H];
+#pragma unroll 4
+  for (int o = 0; o < KMLP_H; ++o) {
+    float t = b1[o];
+    for (int j = 0; j < a.ncol; ++j) t += W1[o * a.ncol + j] * f[j];
+    h1[o] = 0.5f * t * (1.f + erff(t * 0.70710678118654752440f));
+  }
+  float out = b3[0];
+  for (int o = 0; o < KMLP_H; ++o) {
+    float t = b2[o];
+#pragma unroll 8
+    for (int j = 0; j < KMLP_H; ++j) t += W2[o * KMLP_H + j] * h1[j];
+    out += W3[o] * (0.5f * t * (1.f + erff(t * 0.70710678118654752440f)));
+  }
+  float k = out;
+  if (a.flags & 2) k = -(1.f + k) / sqrtf(r * r + a.eps2);
+  if (a.flags & 4) {
+    const float u = fminf(r / a.split_r, 1.f);
+    const float w = 1.f - u * u;
+    k *= 1.f - w * w;
+  }
+  K[e] = k;
+}
+
 // ---------------------------------------------------------------------------------
 // K3b: z transform + Green's function + spectral gradient + inverse z transform, for
 // one kx plane and a strip of TY ky columns, all z. spec is [kx][z][ky] (after the
@@ -816,6 +889,7 @@ struct C2RArgs {
   FftShape fsh;  // complex length L/2
   int twmul;
   FastDiv fdRB, fdM, fdL;
+  int ext;  // single component: keep rows/columns 0..Lkeep and L-1 into a (Lkeep+2)^2 array, index +1 (L-1 -> 0)
 };
 
 template <bool OUT4>
@@ -871,6 +945,17 @@ __global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict_
       v.z = (a.ncomp > 2) ? res[(size_t)2 * RB * L + rr * L + x] : 0.f;
       v.w = (a.ncomp > 3) ? res[(size_t)3 * RB * L + rr * L + x] : 0.f;
       o4[(size_t)r * L + x] = v;
+    }
+  } else if (a.ext) {
+    // rows and columns -1 .. Lkeep of the zero-padded transform (index -1 is L - 1)
+    const int W = a.Lkeep + 2;
+    for (int e = tid; e < RB * L; e += nt) {
+      int rr = (int)fdiv(e, a.fdL), x = e - rr * L;
+      int r = r0 + rr;
+      if (r >= a.nrows) continue;
+      const int er = (r == L - 1) ? 0 : r + 1, ex = (x == L - 1) ? 0 : x + 1;
+      if (er > a.Lkeep + 1 || ex > a.Lkeep + 1) continue;
+      out[(size_t)er * W + ex] = res[rr * L + x];
     }
   } else {
     for (int e = tid; e < RB * L; e += nt) {

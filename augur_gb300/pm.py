@@ -123,6 +123,31 @@ class PMPlan:
         self._bound = grid4
         _lib.check(self.lib.augur_pm_plan_bind_force_grid(self._p, _ptr(grid4)), "augur_pm_plan_bind_force_grid")
 
+    def set_kernel_mlp(self, params, ncol: int, extra=(), cell_units: bool = False, prior: bool = False,
+                       split: bool = False, split_radius: float = 0.0, eps: float = 0.0, pad_ext: bool = False) -> None:
+        """Isolated 2D plans: use the learned radial kernel of ScatterField.kernel_acc
+        (scripts/scatter_field.py:263-289) in the Poisson solve. params: the kmlp's parameters
+        flattened in order W1 (64 x ncol), b1, W2 (64 x 64), b2, W3 (1 x 64), b3 (fp32, any device);
+        extra: the constant feature values after the two (three in cell units) distance features."""
+        p = torch.as_tensor(params, dtype=torch.float32).reshape(-1).contiguous()
+        if p.numel() != 64 * ncol + 64 * 64 + 3 * 64 + 1:
+            raise ValueError(f"params must hold {64 * ncol + 64 * 64 + 3 * 64 + 1} values for ncol={ncol}")
+        if p.is_cuda and p.device != self.device:
+            raise ValueError(f"params are on {p.device}, the plan is on {self.device}")
+        ex = (C.c_float * max(1, len(extra)))(*[float(e) for e in extra])
+        flags = (1 if cell_units else 0) | (2 if prior else 0) | (4 if split else 0) | (8 if pad_ext else 0)
+        self._kparams = p
+        with torch.cuda.device(self.device):
+            rc = self.lib.augur_pm_set_kernel_mlp(self._p, p.data_ptr(), int(ncol), ex, len(extra), flags,
+                                                  float(split_radius), float(eps), _stream(self.device))
+            if not p.is_cuda:
+                torch.cuda.synchronize(self.device)  # the host copy is read asynchronously
+        _lib.check(rc, "augur_pm_set_kernel_mlp")
+
+    def reset_kernel(self) -> None:
+        """Back to the plan's softened -1/sqrt(d^2 + eps^2) kernel with zero-padded gradient."""
+        self._call("augur_pm_reset_kernel")
+
     @property
     def last_launches(self) -> int:
         """Kernel launches issued by the last plan call."""

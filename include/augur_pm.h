@@ -101,6 +101,29 @@ int augur_pm_plan_set_tiles(augur_pm_plan *plan, const augur_pm_tiles *tiles);
 int augur_pm_plan_bind_force_grid(augur_pm_plan *plan, float *grid4);
 
 /*
+ * Learned kernel term of the isolated 2D plan: ScatterField._kernel_fft / kernel_acc
+ * (scripts/scatter_field.py:263-289). Replaces the plan's kernel spectrum with rfft2 of K on
+ * the 2G x 2G minimum-image lattice (distance r per lattice point), where
+ *   K(r) = kmlp(features(r)),  kmlp = Linear(ncol, 64), GELU, Linear(64, 64), GELU, Linear(64, 1)
+ * with torch's layouts and exact (erf) GELU; params: device or host fp32, W1 (64 x ncol), b1 (64),
+ * W2 (64 x 64), b2 (64), W3 (64), b3 (1). features = [r, log(r + h)], or with
+ * AUGUR_KERNEL_CELL_UNITS [r/h, log(r/h + 1), log(0.5/h)] (:141-151), followed by the n_extra
+ * constant features `extra` (host array; the reference's log(eps/0.5) and dt features); ncol is
+ * the total. AUGUR_KERNEL_PRIOR: K = -(1 + K)/sqrt(r^2 + eps^2); AUGUR_KERNEL_SPLIT:
+ * K *= 1 - (1 - min(r/split_radius, 1)^2)^2; AUGUR_KERNEL_PAD_EXT: the gradient reads the
+ * potential's wrapped neighbours (kpad = "ext", :286-288) instead of zero padding.
+ * augur_pm_poisson / augur_pm_force then use this kernel; augur_pm_reset_kernel restores the
+ * softened -1/sqrt(d^2 + eps^2) kernel with zero padding.
+ */
+#define AUGUR_KERNEL_CELL_UNITS 1
+#define AUGUR_KERNEL_PRIOR      2
+#define AUGUR_KERNEL_SPLIT      4
+#define AUGUR_KERNEL_PAD_EXT    8
+int augur_pm_set_kernel_mlp(augur_pm_plan *plan, const float *params, int ncol, const float *extra,
+                            int n_extra, int flags, double split_radius, double eps, void *stream);
+int augur_pm_reset_kernel(augur_pm_plan *plan, void *stream);
+
+/*
  * CIC base cell and fraction, bit-exact with ScatterField._corners
  * (scripts/scatter_field.py:179-182): u = (x + extent/2) / h - 0.5 in IEEE float32
  * (round-to-nearest, true division by float32(h)), i0 = floor(u), w = u - i0.

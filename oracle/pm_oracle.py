@@ -185,6 +185,68 @@ def neg_grad_2d(phi, h: float):
     return out
 
 
+def _gelu(x):
+    from math import erf
+    v = np.vectorize(erf)
+    return 0.5 * x * (1.0 + v(x / np.sqrt(2.0)))
+
+
+def kernel_lattice_mlp_2d(params, ncol: int, extra, flags: int, split_radius: float, eps: float, G: int, h: float):
+    """Learned radial kernel on the 2G min-image lattice (ScatterField._kernel_fft,
+    scatter_field.py:263-272), float64: K = kmlp(features(r)) with kmlp = Linear(ncol, 64), GELU,
+    Linear(64, 64), GELU, Linear(64, 1); features [r, log(r + h)] or (flags & 1, cell units)
+    [r/h, log(r/h + 1), log(0.5/h)] (:141-151) plus the constant extras; flags & 2: prior
+    K = -(1 + K)/sqrt(r^2 + eps^2); flags & 4: split window 1 - (1 - min(r/rs, 1)^2)^2."""
+    p = np.asarray(params, np.float64)
+    H = 64
+    o = 0
+    W1 = p[o:o + H * ncol].reshape(H, ncol); o += H * ncol
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    W3 = p[o:o + H]; o += H
+    b3 = p[o]
+    L = 2 * G
+    idx = np.arange(L, dtype=np.float64)
+    d = np.minimum(idx, L - idx) * h
+    r = np.sqrt(d[:, None] ** 2 + d[None, :] ** 2)
+    if flags & 1:
+        feats = [r / h, np.log(r / h + 1.0), np.full_like(r, np.log(0.5 / h))]
+    else:
+        feats = [r, np.log(r + h)]
+    feats += [np.full_like(r, float(e)) for e in extra]
+    f = np.stack(feats, -1)
+    h1 = _gelu(f @ W1.T + b1)
+    h2 = _gelu(h1 @ W2.T + b2)
+    K = h2 @ W3 + b3
+    if flags & 2:
+        K = -(1.0 + K) / np.sqrt(r ** 2 + eps ** 2)
+    if flags & 4:
+        u = np.minimum(r / split_radius, 1.0) ** 2
+        K = K * (1.0 - (1.0 - u) ** 2)
+    return K
+
+
+def kernel_acc_2d(rho, params, ncol: int, extra, flags: int, split_radius: float, eps: float, E: float):
+    """ScatterField.kernel_acc (scatter_field.py:274-289) for one (G, G) density, float64:
+    phi = h^2 irfft2(rfft2(rho, 2G) rfft2(K)); kpad "zero" (flags & 8 == 0): zero-padded central
+    difference of phi[:G, :G]; kpad "ext": the difference reads phi at rows/columns -1 .. G of
+    the 2G transform. Returns (G, G, 2) = (a_x, a_y)."""
+    rho = np.asarray(rho, np.float64)
+    G = rho.shape[0]
+    h = E / G
+    K = kernel_lattice_mlp_2d(params, ncol, extra, flags, split_radius, eps, G, h)
+    full = np.fft.irfft2(np.fft.rfft2(rho, s=(2 * G, 2 * G)) * np.fft.rfft2(K), s=(2 * G, 2 * G)) * h ** 2
+    if flags & 8:
+        idx = [2 * G - 1] + list(range(G + 1))
+        p = full[np.ix_(idx, idx)]
+    else:
+        p = np.pad(full[:G, :G], 1)
+    gx = (p[1:-1, 2:] - p[1:-1, :-2]) / (2 * h)
+    gy = (p[2:, 1:-1] - p[:-2, 1:-1]) / (2 * h)
+    return np.stack([-gx, -gy], -1)
+
+
 # ----------------------------------------------------------------------------------
 # gather (scripts/scatter_field.py:252-261)
 # ----------------------------------------------------------------------------------

@@ -110,10 +110,56 @@ def exact_acc_cases():
     np.savez_compressed(OUT / "exact_acc.npz", **out)
 
 
+def kernel_acc_cases():
+    """ScatterField.kernel_acc (learned radial kernel, scripts/scatter_field.py:263-289) with seeded
+    kmlp weights: plain kernel with zero padding; split window with kpad = "ext"; cell-unit
+    features with the prior, split and an eps feature."""
+    import math
+
+    cases = [
+        dict(name="plain", grid=32, extent=64.0, cu=False, prior=False, split=False, pp=0.0, epsin=False, kpad="zero"),
+        dict(name="split_ext", grid=32, extent=64.0, cu=False, prior=False, split=True, pp=3.0, epsin=False,
+             kpad="ext"),
+        dict(name="cu_prior", grid=64, extent=64.0, cu=True, prior=True, split=True, pp=2.0, epsin=True, kpad="ext"),
+    ]
+    out = {}
+    for i, c in enumerate(cases):
+        torch.manual_seed(4738 + i)
+        m = sf.ScatterField(grid=c["grid"], extent=c["extent"], kernel=True, pp=c["pp"], split=c["split"],
+                            prior=c["prior"], eps=0.5, cu=c["cu"], epsin=c["epsin"])
+        m.kpad = c["kpad"]
+        m.eps_cur = 0.8
+        g = torch.Generator().manual_seed(9100 + i)
+        with torch.no_grad():  # the output layer starts at zero: give it seeded values
+            m.kmlp[-1].weight.copy_(torch.randn(m.kmlp[-1].weight.shape, generator=g) * 0.3)
+            m.kmlp[-1].bias.copy_(torch.randn(1, generator=g) * 0.3)
+        G = c["grid"]
+        rho = (torch.rand(1, 1, G, G, generator=g) * (torch.rand(1, 1, G, G, generator=g) < 0.2)).float()
+        with torch.no_grad():
+            acc = m.kernel_acc(rho)
+        params = torch.cat([t.detach().reshape(-1) for t in (m.kmlp[0].weight, m.kmlp[0].bias, m.kmlp[2].weight,
+                                                             m.kmlp[2].bias, m.kmlp[4].weight, m.kmlp[4].bias)])
+        extra = [math.log(m.eps_cur / sf.EPS0)] if c["epsin"] else []
+        k = c["name"]
+        out[f"{k}_params"] = params.numpy().astype(np.float32)
+        out[f"{k}_extra"] = np.array(extra, np.float32)
+        out[f"{k}_ncol"] = np.int32(m.kmlp[0].in_features)
+        out[f"{k}_flags"] = np.int32((1 if c["cu"] else 0) | (2 if c["prior"] else 0) | (4 if c["split"] else 0) |
+                                     (8 if c["kpad"] == "ext" else 0))
+        out[f"{k}_split_radius"] = np.float64(m.ppe()) if c["split"] else np.float64(0.0)
+        out[f"{k}_eps"] = np.float64(m.eps)
+        out[f"{k}_grid"] = np.int32(G)
+        out[f"{k}_extent"] = np.float64(c["extent"])
+        out[f"{k}_rho"] = rho[0, 0].numpy()
+        out[f"{k}_acc"] = acc[0].permute(1, 2, 0).numpy()  # (G, G, 2): (a_x, a_y)
+    np.savez_compressed(OUT / "kernel_acc.npz", **out)
+
+
+CASES = {"cell_index": cell_index_cases, "scatter_gather": scatter_gather_cases, "pm_acc": pm_acc_cases,
+         "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases}
+
 if __name__ == "__main__":
-    cell_index_cases()
-    scatter_gather_cases()
-    pm_acc_cases()
-    exact_acc_cases()
+    for name in (sys.argv[1:] or list(CASES)):
+        CASES[name]()
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
