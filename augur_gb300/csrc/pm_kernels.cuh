@@ -893,7 +893,7 @@ struct C2RArgs {
 };
 
 template <bool OUT4>
-__global__ void __launch_bounds__(512) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
+__global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
                                                        const float2 *__restrict__ twg, float *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int L = a.L, M = L / 2, RB = a.RB;
