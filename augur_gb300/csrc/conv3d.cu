@@ -665,28 +665,38 @@ __global__ void __launch_bounds__(256) conv_in_kernel(const bf16 *__restrict__ x
 // Weight gradient on the CUDA cores: dW[n][tap][c] = sum_v dz[v][n] * h[v + tap][c]
 // (zero padding), partial sums per CTA over x rows, reduced in a fixed order afterwards.
 // h: (B, G^3, CIN) bf16 ; dz: (B, G^3, N) as bf16 (DZ_F32 = 0) or fp32 (DZ_F32 = 1).
-// One thread per (n, c) pair keeps 27 tap sums in registers. Also accumulates the bias
+// One thread per (n, c, x range): XS threads share an (n, c) pair, each keeping 27 tap sums
+// over a contiguous range of x in registers (a sliding window loads each input value once);
+// the XS partial sums are added in a fixed order at the end. Also accumulates the bias
 // gradient sum_v dz[v][n] (threads with c == 0).
 // ---------------------------------------------------------------------------------------
-template <int CIN, int N, int DZ_F32>
-__global__ void __launch_bounds__(CIN * N) wgrad_kernel(const bf16 *__restrict__ h, const void *__restrict__ dz,
-                                                        int B, int G, int rows_per_cta,
-                                                        float *__restrict__ partial) {
+template <int CIN, int N, int DZ_F32, int XS, int NB>
+__global__ void __launch_bounds__(CIN * (N / NB) * XS) wgrad_kernel(const bf16 *__restrict__ h,
+                                                                    const void *__restrict__ dz, int B, int G,
+                                                                    int rows_per_cta, float *__restrict__ partial) {
   extern __shared__ __align__(16) unsigned char smem[];
   float *sh = reinterpret_cast<float *>(smem);            // [9][G + 2][CIN]
   float *sd = sh + (size_t)9 * (G + 2) * CIN;             // [G][N]
+  constexpr int NP = CIN * (N / NB);                      // (output-channel group, c) pairs
+  constexpr int NT = NP * XS;
   const int tid = threadIdx.x;
-  const int n = tid / CIN, c = tid % CIN;
-  float acc[27];
+  const int pair = tid % NP, xs = tid / NP;
+  const int n0 = (pair / CIN) * NB, c = pair % CIN;
+  const int xa = (G * xs) / XS, xb = (G * (xs + 1)) / XS;
+  float acc[NB][27];
 #pragma unroll
-  for (int t = 0; t < 27; ++t) acc[t] = 0.f;
-  float bacc = 0.f;
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int t = 0; t < 27; ++t) acc[i][t] = 0.f;
+  float bacc[NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i) bacc[i] = 0.f;
   const int nrows = B * G * G;
   const int r0 = blockIdx.x * rows_per_cta, r1 = min(nrows, r0 + rows_per_cta);
   for (int row = r0; row < r1; ++row) {
     const int y = row % G, z = (row / G) % G, b = row / (G * G);
     __syncthreads();
-    for (int e = tid; e < 9 * (G + 2) * CIN; e += blockDim.x) {
+    for (int e = tid; e < 9 * (G + 2) * CIN; e += NT) {
       const int cc = e % CIN, xr = (e / CIN) % (G + 2), p = e / (CIN * (G + 2));
       const int zz = z + p / 3 - 1, yy = y + p % 3 - 1, xx = xr - 1;
       float v = 0.f;
@@ -694,26 +704,65 @@ __global__ void __launch_bounds__(CIN * N) wgrad_kernel(const bf16 *__restrict__
         v = __bfloat162float(h[((((size_t)b * G + zz) * G + yy) * G + xx) * CIN + cc]);
       sh[e] = v;
     }
-    for (int e = tid; e < G * N; e += blockDim.x) {
+    for (int e = tid; e < G * N; e += NT) {
       const size_t idx = (((size_t)b * G + z) * G + y) * G * N + e;
       sd[e] = DZ_F32 ? reinterpret_cast<const float *>(dz)[idx]
                      : __bfloat162float(reinterpret_cast<const bf16 *>(dz)[idx]);
     }
     __syncthreads();
-    for (int x = 0; x < G; ++x) {
-      const float g = sd[x * N + n];
-      if (c == 0) bacc += g;
+    // sliding window: voxel x + dx of plane-row p is loaded once (at x' = x + 2) and reused for
+    // the three dx taps and the NB output channels that read it
+    float win[9][3];
+#pragma unroll
+    for (int p = 0; p < 9; ++p) {
+      win[p][0] = sh[(p * (G + 2) + xa) * CIN + c];
+      win[p][1] = sh[(p * (G + 2) + xa + 1) * CIN + c];
+    }
+    for (int x = xa; x < xb; ++x) {
+      float g[NB];
+#pragma unroll
+      for (int i = 0; i < NB; ++i) g[i] = sd[x * N + n0 + i];
+      if (c == 0)
+#pragma unroll
+        for (int i = 0; i < NB; ++i) bacc[i] += g[i];
 #pragma unroll
       for (int p = 0; p < 9; ++p) {
+        win[p][2] = sh[(p * (G + 2) + x + 2) * CIN + c];
 #pragma unroll
-        for (int dx = 0; dx < 3; ++dx) acc[p * 3 + dx] += g * sh[(p * (G + 2) + x + dx) * CIN + c];
+        for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+          for (int i = 0; i < NB; ++i) acc[i][p * 3 + dx] += g[i] * win[p][dx];
+        win[p][0] = win[p][1];
+        win[p][1] = win[p][2];
       }
     }
   }
   float *out = partial + (size_t)blockIdx.x * (N * 27 * CIN + N);
+  if constexpr (XS == 1) {
 #pragma unroll
-  for (int t = 0; t < 27; ++t) out[(n * 27 + t) * CIN + c] = acc[t];
-  if (c == 0) out[N * 27 * CIN + n] = bacc;
+    for (int i = 0; i < NB; ++i) {
+#pragma unroll
+      for (int t = 0; t < 27; ++t) out[((n0 + i) * 27 + t) * CIN + c] = acc[i][t];
+      if (c == 0) out[N * 27 * CIN + n0 + i] = bacc[i];
+    }
+  } else {
+    static_assert(NB == 1, "x ranges are only used with one output channel per thread");
+    // fixed-order sum of the XS ranges through shared memory (reusing the row buffers)
+    __syncthreads();
+    float *red = sh;  // [XS][CIN * N][28]
+#pragma unroll
+    for (int t = 0; t < 27; ++t) red[((size_t)xs * NP + pair) * 28 + t] = acc[0][t];
+    red[((size_t)xs * NP + pair) * 28 + 27] = bacc[0];
+    __syncthreads();
+    for (int e = tid; e < NP * 28; e += NT) {
+      const int pr = e / 28, t = e % 28;
+      float v = 0.f;
+      for (int k = 0; k < XS; ++k) v += red[((size_t)k * NP + pr) * 28 + t];
+      const int nn = pr / CIN, cc = pr % CIN;
+      if (t < 27) out[(nn * 27 + t) * CIN + cc] = v;
+      else if (cc == 0) out[N * 27 * CIN + nn] = v;
+    }
+  }
 }
 
 __global__ void reduce_partials_kernel(const float *__restrict__ partial, int nparts, int len,
@@ -725,11 +774,6 @@ __global__ void reduce_partials_kernel(const float *__restrict__ partial, int np
   out[e] = s;
 }
 
-// ---------------------------------------------------------------------------------------
-// Weight preparation: fp32 w[n][tap][c] (n < Nreal, c < Creal) -> bf16 UMMA B operand
-// [k/8][N][8] with k = tap * CIN + c (zero padded to CIN x N). flip = 1 builds the data-
-// gradient operand: B'[c][k' = tap * Nreal_in + n] = w[n][26 - tap][c] (roles swapped).
-// ---------------------------------------------------------------------------------------
 // fp32 w[n][tap][c] -> bf16 tensor-core B operand. 3-channel-padded layers (CIN >= 16) use the
 // row layout of conv_tc_kernel: for each dx a K x NR block, K = (dz, c) = 3 CIN, NR = (dy, n) =
 // 3 N, stored [dx][K / 8][NR][8]. The input layer (CIN = 2) uses the flat layout K = (tap, c)
@@ -959,10 +1003,17 @@ int launch_wgrad(const void *h, const void *dz, int B, int G, float *partial, in
   int nparts = std::min(max_parts, std::min(nrows, nsm * 4));
   const int rows_per = (nrows + nparts - 1) / nparts;
   nparts = (nrows + rows_per - 1) / rows_per;
-  const size_t smem = ((size_t)9 * (G + 2) * CIN + (size_t)G * N) * 4;
+  // narrower layers get x ranges so that a CTA has 1024 threads (ranges may be short or empty
+  // for small G); measured on GB300, two output channels per thread (NB = 2, 512 threads) is
+  // slower for the 32 x 32 layers (21.9 -> 24.9 ms at batch 4, 128^3)
+  constexpr int NB = 1;
+  constexpr int XS = (CIN * N >= 1024) ? 1 : 1024 / (CIN * N);
+  const size_t smem = std::max(((size_t)9 * (G + 2) * CIN + (size_t)G * N) * 4,
+                               XS > 1 ? (size_t)XS * CIN * N * 28 * 4 : 0);
   if (smem > 227 * 1024) return AUGUR_EINVAL;
-  cudaFuncSetAttribute(wgrad_kernel<CIN, N, DZF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  wgrad_kernel<CIN, N, DZF><<<nparts, CIN * N, smem, st>>>((const bf16 *)h, dz, B, G, rows_per, partial);
+  cudaFuncSetAttribute(wgrad_kernel<CIN, N, DZF, XS, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  wgrad_kernel<CIN, N, DZF, XS, NB><<<nparts, CIN * (N / NB) * XS, smem, st>>>((const bf16 *)h, dz, B, G, rows_per,
+                                                                              partial);
   const int len = N * 27 * CIN + N;
   reduce_partials_kernel<<<(len + 255) / 256, 256, 0, st>>>(partial, nparts, len, out);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
