@@ -216,6 +216,9 @@ DepositArgs dep_args(const augur_pm_plan *p) {
 template <int D, int MODE>
 int launch_deposit(augur_pm_plan *p, float *rho, float2 *spec, cudaStream_t st) {
   DepositArgs a = dep_args(p);
+  deposit_count_kernel<D><<<blocks_for(p->nblk, 256), 256, 0, st>>>(p->row_start, p->tile_off, a, p->dep_nch,
+                                                                      p->dep_seg_tab, p->d_err);
+  AUGUR_LAUNCH_CHECK(p);
   deposit_plan_kernel<D><<<1, 1024, 0, st>>>(p->row_start, p->tile_off, a, p->dep_nch, p->dep_item_off,
                                               p->dep_slot_off, p->dep_seg_tab, p->dep_item_blk, p->d_err);
   AUGUR_LAUNCH_CHECK(p);

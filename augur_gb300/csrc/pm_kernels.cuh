@@ -318,6 +318,31 @@ __device__ __forceinline__ void block_segments(const DepositArgs &a, int b, cons
 // split over more than one item), and lists the block of every item in item_blk.
 constexpr int MAXSEGB = 32;  // segments per row block: 2 * (RZ + 1) with RZ <= 15
 
+// One thread per row block (many CTAs): the block's body segments and its item count.
+template <int D>
+__global__ void __launch_bounds__(256) deposit_count_kernel(const uint32_t *__restrict__ start,
+                                                            const uint32_t *__restrict__ tile_off, DepositArgs a,
+                                                            uint32_t *__restrict__ nch, uint4 *__restrict__ seg_tab,
+                                                            unsigned *__restrict__ err) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nblk) return;
+  uint32_t cnt = 0;
+  int ns = 0;
+  uint4 *tab = seg_tab + (size_t)b * (MAXSEGB + 1);
+  block_segments<D>(a, b, start, tile_off, [&](uint32_t lo, uint32_t hi, uint32_t row0) {
+    if (ns < MAXSEGB) {
+      tab[1 + ns] = make_uint4(lo, cnt, row0, 0u);
+      ++ns;
+      cnt += hi - lo;
+    } else {
+      set_err(err, AUGUR_ERRBIT_RANGE);
+    }
+  });
+  tab[0] = make_uint4((uint32_t)ns, cnt, 0u, 0u);
+  nch[b] = cnt == 0 ? 1u : (cnt + a.chunk - 1) / a.chunk;
+}
+
+// One CTA: scan of the item counts into item_off and slot_off, and the block of every item.
 template <int D>
 __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__restrict__ start,
                                                             const uint32_t *__restrict__ tile_off, DepositArgs a,
@@ -327,23 +352,6 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
                                                             unsigned *__restrict__ err) {
   __shared__ uint32_t wsum[2][32];
   const int nb = a.nblk, tid = threadIdx.x, nt = blockDim.x;
-  for (int b = tid; b < nb; b += nt) {
-    uint32_t cnt = 0;
-    int ns = 0;
-    uint4 *tab = seg_tab + (size_t)b * (MAXSEGB + 1);
-    block_segments<D>(a, b, start, tile_off, [&](uint32_t lo, uint32_t hi, uint32_t row0) {
-      if (ns < MAXSEGB) {
-        tab[1 + ns] = make_uint4(lo, cnt, row0, 0u);
-        ++ns;
-        cnt += hi - lo;
-      } else {
-        set_err(err, AUGUR_ERRBIT_RANGE);
-      }
-    });
-    tab[0] = make_uint4((uint32_t)ns, cnt, 0u, 0u);
-    nch[b] = cnt == 0 ? 1u : (cnt + a.chunk - 1) / a.chunk;
-  }
-  __syncthreads();
   const int per = (nb + nt - 1) / nt;
   const int b0 = min(nb, tid * per), b1 = min(nb, b0 + per);
   uint32_t si = 0, ss = 0;
@@ -608,7 +616,11 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
   for (int e = tid; e < RR * G; e += nt) {
     int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
-    float v = __fmul_rn(__ull2float_rn(acc[e]), qs.outscale);
+    // u64 -> f32 rounds correctly either way; the 32-bit conversion is a fast FP32-pipe
+    // instruction, the 64-bit one is not on this part and is only needed for sums >= 2^32
+    const unsigned long long q = acc[e];
+    const float fq = (q >> 32) ? __ull2float_rn(q) : __uint2float_rn((unsigned)q);
+    float v = __fmul_rn(fq, qs.outscale);
     if (MODE != 1) {
       int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
       size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
