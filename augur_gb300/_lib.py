@@ -28,6 +28,7 @@ SIGNATURES = {
     "augur_pm_plan_bind_force_grid": (_i32, [_vp, _vp]),
     "augur_pm_set_kernel_mlp": (_i32, [_vp, _vp, _i32, _vp, _i32, _i32, _f64, _f64, _vp]),
     "augur_pm_reset_kernel": (_i32, [_vp, _vp]),
+    "augur_pm_pair_acc": (_i32, [_vp, _vp, _vp, _vp, _i64, _f64, _i32, _vp, _i32, _vp, _i32, _i32, _f64, _vp, _vp]),
     "augur_pm_cell_index": (_i32, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "augur_pm_deposit": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp]),
     "augur_pm_poisson": (_i32, [_vp, _vp, _vp, _vp]),

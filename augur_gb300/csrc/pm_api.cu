@@ -52,6 +52,10 @@ struct augur_pm_plan {
   float *phi_ext;  // isolated, kpad = "ext": potential at rows/columns -1 .. G, (G+2)^2
   float *kparams;  // learned kernel MLP parameters (device copy)
   int kpad_ext;
+  // pair term: cell keys and body order (max_n each), cell counts / starts / fill cursors
+  uint32_t *pair_key, *pair_order, *pair_cnt, *pair_start, *pair_fill;
+  size_t pair_cells_cap;
+  float *pair_params;
   int64_t run_n;
   float run_dt;
   int run_active;
@@ -570,7 +574,8 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
   void *ptrs[] = {p->tw, p->pos4[0], p->pos4[1], p->vel4[0], p->vel4[1], p->key, p->slot, p->row_count,
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
                   p->F4_own, p->real_tmp, p->phi2d, p->rho2d, p->phi_ext, p->kparams, p->dep_nch, p->dep_item_off, p->dep_slot_off,
-                  p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart};
+                  p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart,
+                  p->pair_key, p->pair_order, p->pair_cnt, p->pair_start, p->pair_fill, p->pair_params};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -925,6 +930,78 @@ int augur_pm_reset_kernel(augur_pm_plan *p, void *stream) {
   if (!p || p->mode != AUGUR_MODE_ISOLATED_SOFTENED) return AUGUR_EINVAL;
   p->launches = 0;
   return softened_kernel(p, S(stream));
+}
+
+int augur_pm_pair_acc(augur_pm_plan *p, const float *pos, const float *mass, const float *mask, int64_t n,
+                      double ppe, int knn, const float *params, int ncol, const float *extra, int n_extra, int flags,
+                      double eps, float *acc, void *stream) {
+  if (!p || p->dim != 2 || p->mode == AUGUR_MODE_PERIODIC) return AUGUR_EINVAL;
+  if (n < 0 || n > p->max_n) return AUGUR_EINVAL;
+  if (n > 0 && (!pos || !mass || !mask || !acc)) return AUGUR_EINVAL;
+  if (!(ppe > 0.0) || !std::isfinite(ppe) || knn < 1 || knn > PAIR_KMAX) return AUGUR_EINVAL;
+  const int nbase = (flags & AUGUR_KERNEL_CELL_UNITS) ? 3 : 2;
+  if (params && (n_extra < 0 || ncol != nbase + n_extra || ncol > KMLP_MAXCOL || (n_extra > 0 && !extra)))
+    return AUGUR_EINVAL;
+  if ((flags & AUGUR_KERNEL_PRIOR) && !(eps >= 0.0)) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  cudaStream_t st = S(stream);
+  p->launches = 0;
+  PairArgs a{};
+  const double E = p->extent;
+  const double cells = std::ceil(E / ppe);
+  a.C = cells > PAIR_CMAX ? PAIR_CMAX : (int)std::max(1.0, cells);
+  a.cs = cells > PAIR_CMAX ? (float)(E / PAIR_CMAX) : (float)ppe;  // a coarser side still holds every pair < ppe
+  a.knn = knn;
+  a.half_ext = (float)(E / 2);
+  a.inv_ppe = (float)(1.0 / ppe);
+  a.eps2 = (float)(eps * eps);
+  a.h = (float)(E / p->G);
+  a.flags = ((flags & AUGUR_KERNEL_CELL_UNITS) ? 1 : 0) | ((flags & AUGUR_KERNEL_PRIOR) ? 2 : 0);
+  a.nbase = nbase;
+  a.ncol = params ? ncol : nbase;
+  for (int j = 0; j < KMLP_MAXCOL; ++j) a.extra[j] = (params && j < n_extra) ? extra[j] : 0.f;
+  const size_t ncells = (size_t)a.C * a.C + 1;
+  int rc = AUGUR_OK;
+  if (!p->pair_key) {
+    rc |= dalloc(p, &p->pair_key, (size_t)p->max_n);
+    rc |= dalloc(p, &p->pair_order, (size_t)p->max_n);
+    rc |= dalloc(p, &p->pair_params, (size_t)KMLP_H * KMLP_MAXCOL + KMLP_H * KMLP_H + 3 * KMLP_H + 1);
+    if (rc) return AUGUR_ENOMEM;
+  }
+  if (ncells > p->pair_cells_cap) {
+    for (uint32_t **q : {&p->pair_cnt, &p->pair_start, &p->pair_fill}) {
+      if (*q) {
+        cudaFree(*q);
+        p->bytes -= p->pair_cells_cap * sizeof(uint32_t);
+        *q = nullptr;
+      }
+      rc |= dalloc(p, q, ncells);
+    }
+    if (rc) {
+      p->pair_cells_cap = 0;
+      return AUGUR_ENOMEM;
+    }
+    p->pair_cells_cap = ncells;
+  }
+  size_t np = 0;
+  if (params) {
+    np = (size_t)KMLP_H * ncol + KMLP_H * KMLP_H + 3 * KMLP_H + 1;
+    if (cudaMemcpyAsync(p->pair_params, params, np * sizeof(float), cudaMemcpyDefault, st) != cudaSuccess)
+      return AUGUR_ECUDA;
+  }
+  if (cudaMemsetAsync(p->pair_cnt, 0, ncells * sizeof(uint32_t), st) != cudaSuccess) return AUGUR_ECUDA;
+  const unsigned nb = blocks_for(n, 256);
+  pair_keys_kernel<<<nb, 256, 0, st>>>(pos, mask, n, a, p->pair_key, p->pair_cnt);
+  AUGUR_LAUNCH_CHECK(p);
+  pair_scan_kernel<<<1, 1024, 0, st>>>(p->pair_cnt, (int)(ncells - 1), p->pair_start, p->pair_fill);
+  AUGUR_LAUNCH_CHECK(p);
+  pair_scatter_kernel<<<nb, 256, 0, st>>>(p->pair_key, n, p->pair_fill, p->pair_order);
+  AUGUR_LAUNCH_CHECK(p);
+  pair_acc_kernel<<<blocks_for(n, 128), 128, np * sizeof(float), st>>>(pos, mass, mask, n, p->pair_start,
+                                                                        p->pair_order, params ? p->pair_params : nullptr,
+                                                                        a, acc);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
 }
 
 int augur_pm_plan_bind_force_grid(augur_pm_plan *p, float *grid4) {

@@ -144,6 +144,27 @@ class PMPlan:
                 torch.cuda.synchronize(self.device)  # the host copy is read asynchronously
         _lib.check(rc, "augur_pm_set_kernel_mlp")
 
+    def pair_acc(self, pos, mass=None, mask=None, ppe: float = 2.0, knn: int = 16, params=None, ncol: int = 2,
+                 extra=(), cell_units: bool = False, prior: bool = False, eps: float = 0.0) -> torch.Tensor:
+        """Isolated 2D plans: the pair term of ScatterField.pp_acc (scripts/scatter_field.py:291-300,
+        324-364, 500-521) -- the knn nearest bodies within ppe weighted by the ppmlp (params in the
+        kmlp layout of set_kernel_mlp, or None for the prior alone) and the prior's near-field
+        difference. ppe is the pair radius in length units (ScatterField.ppe())."""
+        n = self._n(pos)
+        mass, mask = self._mm(n, mass, mask)
+        p = None
+        if params is not None:
+            p = torch.as_tensor(params, dtype=torch.float32).reshape(-1).contiguous()
+            if p.numel() != 64 * ncol + 64 * 64 + 3 * 64 + 1:
+                raise ValueError(f"params must hold {64 * ncol + 64 * 64 + 3 * 64 + 1} values for ncol={ncol}")
+            p = p.to(self.device)
+        ex = (C.c_float * max(1, len(extra)))(*[float(e) for e in extra])
+        flags = (1 if cell_units else 0) | (2 if prior else 0)
+        acc = torch.empty((n, 2), dtype=torch.float32, device=self.device)
+        self._call("augur_pm_pair_acc", pos.data_ptr(), mass.data_ptr(), mask.data_ptr(), n, float(ppe), int(knn),
+                   _ptr(p), int(ncol), ex, len(extra), flags, float(eps), acc.data_ptr())
+        return acc
+
     def reset_kernel(self) -> None:
         """Back to the plan's softened -1/sqrt(d^2 + eps^2) kernel with zero-padded gradient."""
         self._call("augur_pm_reset_kernel")

@@ -124,6 +124,27 @@ int augur_pm_set_kernel_mlp(augur_pm_plan *plan, const float *params, int ncol, 
 int augur_pm_reset_kernel(augur_pm_plan *plan, void *stream);
 
 /*
+ * Pair term of the isolated 2D plan: ScatterField.pp_acc / pp_acc_cell / _pair_w
+ * (scripts/scatter_field.py:291-300, 302-311, 324-364, 500-521). Bodies with mask > 0 are
+ * sorted by cells of side ppe (clamped into ceil(extent/ppe)^2 cells, as _cell_keys); for every
+ * such body the knn (1..32) nearest other such bodies in the 3 x 3 cells around its own, with
+ * r = sqrt(|d|^2 + 1e-8), give
+ *   acc_out_i = sum_j w(r) m_j mask_j d / r,   w = g(r) (1 - u)^2 (+ prior),   u = min(r/ppe, 1)^2,
+ * g = ppmlp(features(r)) in the kmlp layout of augur_pm_set_kernel_mlp (params NULL: g = 0),
+ * features [r, log(r + 0.05)], or with AUGUR_KERNEL_CELL_UNITS [r/h, log(r/h + 0.1), log(0.5/h)]
+ * (h = extent/grid), then the n_extra constants; AUGUR_KERNEL_PRIOR adds
+ * r/q^3 - a_mesh, q = sqrt(r^2 + eps^2), a_mesh = -4 (1 - u) r / (ppe^2 q) + (1 - (1 - u)^2) r / q^3.
+ * Bodies with mask <= 0 get 0. The weight vanishes at r >= ppe, so the 3 x 3 search equals the
+ * reference's dense top-knn; equal distances rank the lower index first. Deterministic. The
+ * first call (and one that needs more cells than before) allocates scratch: make it before
+ * any stream capture. pos (N, 2), mass, mask (N,), acc_out (N, 2): device float32.
+ */
+int augur_pm_pair_acc(augur_pm_plan *plan, const float *pos, const float *mass, const float *mask,
+                      int64_t n, double ppe, int knn, const float *params, int ncol,
+                      const float *extra, int n_extra, int flags, double eps, float *acc_out,
+                      void *stream);
+
+/*
  * CIC base cell and fraction, bit-exact with ScatterField._corners
  * (scripts/scatter_field.py:179-182): u = (x + extent/2) / h - 0.5 in IEEE float32
  * (round-to-nearest, true division by float32(h)), i0 = floor(u), w = u - i0.

@@ -247,6 +247,62 @@ def kernel_acc_2d(rho, params, ncol: int, extra, flags: int, split_radius: float
     return np.stack([-gx, -gy], -1)
 
 
+def _mlp64(params, ncol, f):
+    """Linear(ncol, 64), GELU, Linear(64, 64), GELU, Linear(64, 1) on features f (..., ncol), float64."""
+    p = np.asarray(params, np.float64)
+    H = 64
+    o = 0
+    W1 = p[o:o + H * ncol].reshape(H, ncol); o += H * ncol
+    b1 = p[o:o + H]; o += H
+    W2 = p[o:o + H * H].reshape(H, H); o += H * H
+    b2 = p[o:o + H]; o += H
+    W3 = p[o:o + H]; o += H
+    return _gelu(_gelu(f @ W1.T + b1) @ W2.T + b2) @ W3 + p[o]
+
+
+def pair_acc_2d(pos, mass, mask, params, ncol: int, extra, flags: int, ppe: float, eps: float, h: float,
+                knn: int = 16, queries=None):
+    """ScatterField.pp_acc (scripts/scatter_field.py:291-300, 500-521), float64 brute force: for every
+    body with mask > 0, the knn nearest other bodies with mask > 0 (r = sqrt(d^2 + 1e-8)); weight
+    w = g(r) (1 - u)^2 with g = ppmlp(features(r)), u = min(r/ppe, 1)^2, features [r, log(r + 0.05)]
+    or (flags & 1) [r/h, log(r/h + 0.1), log(0.5/h)] plus the extras; flags & 2 adds the prior
+    r/q^3 - a_mesh, q = sqrt(r^2 + eps^2), a_mesh = -4 (1 - u) r / (ppe^2 q) + (1 - (1 - u)^2) r / q^3.
+    acc_i = sum_j w m_j (x_j - x_i) / r. (The reference's cell-list mode searches the 3 x 3 cells of
+    side ppe, which hold every body closer than ppe; weights vanish beyond ppe, so it agrees.)
+    params None: g = 0 (the prior alone). queries: body indices to evaluate (default all); the
+    other rows stay 0."""
+    pos = np.asarray(pos, np.float64)
+    mass = np.asarray(mass, np.float64)
+    mask = np.asarray(mask, np.float64)
+    n = pos.shape[0]
+    out = np.zeros((n, 2))
+    valid = mask > 0
+    rows = np.nonzero(valid)[0] if queries is None else [int(q) for q in queries if valid[int(q)]]
+    for i in rows:
+        d = pos - pos[i]
+        r = np.sqrt((d ** 2).sum(1) + 1e-8)
+        cand = valid.copy()
+        cand[i] = False
+        idx = np.nonzero(cand)[0]
+        sel = idx[np.argsort(r[idx], kind="stable")[:knn]]
+        rs = r[sel]
+        if flags & 1:
+            f = [rs / h, np.log(rs / h + 0.1), np.full_like(rs, np.log(0.5 / h))]
+        else:
+            f = [rs, np.log(rs + 0.05)]
+        f += [np.full_like(rs, float(e)) for e in extra]
+        g = _mlp64(params, ncol, np.stack(f, -1)) if params is not None else np.zeros_like(rs)
+        u = np.minimum(rs / ppe, 1.0) ** 2
+        win = (1 - u) ** 2
+        w = g * win
+        if flags & 2:
+            q = np.sqrt(rs ** 2 + eps ** 2)
+            a_mesh = -4 * (1 - u) * rs / ppe ** 2 / q + (1 - win) * rs / q ** 3
+            w = w + (rs / q ** 3 - a_mesh)
+        out[i] = ((w * mass[sel])[:, None] * d[sel] / rs[:, None]).sum(0)
+    return out
+
+
 # ----------------------------------------------------------------------------------
 # gather (scripts/scatter_field.py:252-261)
 # ----------------------------------------------------------------------------------

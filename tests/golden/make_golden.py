@@ -11,6 +11,7 @@ results/pm_baseline_force_error.json. Nothing at test time reads the reference.
 from __future__ import annotations
 
 import json
+import math
 import os
 import sys
 from pathlib import Path
@@ -114,8 +115,6 @@ def kernel_acc_cases():
     """ScatterField.kernel_acc (learned radial kernel, scripts/scatter_field.py:263-289) with seeded
     kmlp weights: plain kernel with zero padding; split window with kpad = "ext"; cell-unit
     features with the prior, split and an eps feature."""
-    import math
-
     cases = [
         dict(name="plain", grid=32, extent=64.0, cu=False, prior=False, split=False, pp=0.0, epsin=False, kpad="zero"),
         dict(name="split_ext", grid=32, extent=64.0, cu=False, prior=False, split=True, pp=3.0, epsin=False,
@@ -155,8 +154,59 @@ def kernel_acc_cases():
     np.savez_compressed(OUT / "kernel_acc.npz", **out)
 
 
+def pair_acc_cases():
+    """ScatterField.pp_acc (pair term: k nearest neighbours, windowed learned weight and prior,
+    scripts/scatter_field.py:291-300, 324-364, 500-521) with seeded ppmlp weights: dense mode
+    (N <= 512) and the cell-list mode, plain and cell-unit features."""
+    cases = [
+        dict(name="dense", n=300, cu=False, cell=False, prior=True, epsin=False),
+        dict(name="cell", n=3000, cu=False, cell=True, prior=True, epsin=False),
+        dict(name="cell_cu", n=3000, cu=True, cell=True, prior=False, epsin=True),
+    ]
+    out = {}
+    for i, c in enumerate(cases):
+        torch.manual_seed(4738 + i)
+        m = sf.ScatterField(grid=64, extent=64.0, kernel=True, pp=2.0, split=True, prior=c["prior"], eps=0.5,
+                            cu=c["cu"], epsin=c["epsin"])
+        if c["cell"]:
+            m.opt = {"cell"}
+        m.eps_cur = 0.8
+        g = torch.Generator().manual_seed(9200 + i)
+        with torch.no_grad():  # the output layer starts at zero: give it seeded values
+            m.ppmlp[-1].weight.copy_(torch.randn(m.ppmlp[-1].weight.shape, generator=g) * 0.3)
+            m.ppmlp[-1].bias.copy_(torch.randn(1, generator=g) * 0.3)
+        n = c["n"]
+        # clustered bodies (many pairs inside ppe) plus a uniform background, a few off the grid
+        cen = (torch.rand(8, 2, generator=g) - 0.5) * 50.0
+        pos = cen[torch.randint(0, 8, (n,), generator=g)] + torch.randn(n, 2, generator=g) * 2.0
+        pos[: n // 5] = (torch.rand(n // 5, 2, generator=g) - 0.5) * 66.0
+        pos = pos.float()[None]
+        mass = (0.5 + torch.rand(1, n, generator=g)).float()
+        mask = (torch.rand(1, n, generator=g) > 0.05).float()
+        with torch.no_grad():
+            acc = m.pp_acc(pos, mass, mask)
+        params = torch.cat([t.detach().reshape(-1) for t in (m.ppmlp[0].weight, m.ppmlp[0].bias, m.ppmlp[2].weight,
+                                                             m.ppmlp[2].bias, m.ppmlp[4].weight, m.ppmlp[4].bias)])
+        extra = [math.log(m.eps_cur / sf.EPS0)] if c["epsin"] else []
+        k = c["name"]
+        out[f"{k}_pos"] = pos[0].numpy()
+        out[f"{k}_mass"] = mass[0].numpy()
+        out[f"{k}_mask"] = mask[0].numpy()
+        out[f"{k}_params"] = params.numpy().astype(np.float32)
+        out[f"{k}_extra"] = np.array(extra, np.float32)
+        out[f"{k}_ncol"] = np.int32(m.ppmlp[0].in_features)
+        out[f"{k}_flags"] = np.int32((1 if c["cu"] else 0) | (2 if c["prior"] else 0))
+        out[f"{k}_ppe"] = np.float64(m.ppe())
+        out[f"{k}_eps"] = np.float64(m.eps)
+        out[f"{k}_h"] = np.float64(m.h)
+        out[f"{k}_extent"] = np.float64(64.0)
+        out[f"{k}_knn"] = np.int32(16)
+        out[f"{k}_acc"] = acc[0].numpy()
+    np.savez_compressed(OUT / "pair_acc.npz", **out)
+
+
 CASES = {"cell_index": cell_index_cases, "scatter_gather": scatter_gather_cases, "pm_acc": pm_acc_cases,
-         "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases}
+         "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases, "pair_acc": pair_acc_cases}
 
 if __name__ == "__main__":
     for name in (sys.argv[1:] or list(CASES)):
