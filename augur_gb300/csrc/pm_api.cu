@@ -52,8 +52,12 @@ struct augur_pm_plan {
   float *phi_ext;  // isolated, kpad = "ext": potential at rows/columns -1 .. G, (G+2)^2
   float *kparams;  // learned kernel MLP parameters (device copy)
   int kpad_ext;
-  // pair term: cell keys and body order (max_n each), cell counts / starts / fill cursors
-  uint32_t *pair_key, *pair_order, *pair_cnt, *pair_start, *pair_fill;
+  // pair term: cell key and rank per body, the bodies in cell order, the two-level cell scan
+  uint32_t *pair_key, *pair_rank, *pair_cnt, *pair_start, *pair_tsum, *pair_toff;
+  float4 *pair_sorted;
+  uint32_t *pair_nbj;  // neighbour lists, max_n x pair_kp
+  float *pair_nbq;
+  int pair_kp;
   size_t pair_cells_cap;
   float *pair_params;
   int64_t run_n;
@@ -575,7 +579,8 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
                   p->row_start, p->tile_sum, p->tile_off, p->d_err, p->d_mmax, p->spec, p->spec3, p->khat,
                   p->F4_own, p->real_tmp, p->phi2d, p->rho2d, p->phi_ext, p->kparams, p->dep_nch, p->dep_item_off, p->dep_slot_off,
                   p->dep_counters, p->dep_scratch, p->dep_item_blk, p->dep_seg_tab, p->epart,
-                  p->pair_key, p->pair_order, p->pair_cnt, p->pair_start, p->pair_fill, p->pair_params};
+                  p->pair_key, p->pair_rank, p->pair_cnt, p->pair_start, p->pair_tsum, p->pair_toff,
+                  p->pair_sorted, p->pair_params, p->pair_nbj, p->pair_nbq};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   delete p;
@@ -946,42 +951,67 @@ int augur_pm_pair_acc(augur_pm_plan *p, const float *pos, const float *mass, con
   if (n == 0) return AUGUR_OK;
   cudaStream_t st = S(stream);
   p->launches = 0;
-  PairArgs a{};
+  // cells of side ppe / 4 (fewer candidates per search in dense regions), at most PAIR_CMAX a side
   const double E = p->extent;
-  const double cells = std::ceil(E / ppe);
-  a.C = cells > PAIR_CMAX ? PAIR_CMAX : (int)std::max(1.0, cells);
-  a.cs = cells > PAIR_CMAX ? (float)(E / PAIR_CMAX) : (float)ppe;  // a coarser side still holds every pair < ppe
+  double cs = ppe / 4.0;
+  if (std::ceil(E / cs) > PAIR_CMAX) cs = E / PAIR_CMAX;
+  PairArgs a{};
+  a.C = (int)std::max(1.0, std::min((double)PAIR_CMAX, std::ceil(E / cs)));
+  a.cs = (float)cs;
+  a.W = (int)std::ceil(ppe / cs) + 1;  // one ring more than the pair radius needs: rounding at cell edges
   a.knn = knn;
   a.half_ext = (float)(E / 2);
   a.inv_ppe = (float)(1.0 / ppe);
+  a.thr0 = (float)(ppe * ppe * (1.0 + 1.0 / 4096));  // |d|^2 + 1e-8 >= thr0  =>  r / ppe rounds >= 1, weight 0
+  a.slack = (float)((E / 2 + 2 * ppe + cs) / 65536.0);
   a.eps2 = (float)(eps * eps);
   a.h = (float)(E / p->G);
   a.flags = ((flags & AUGUR_KERNEL_CELL_UNITS) ? 1 : 0) | ((flags & AUGUR_KERNEL_PRIOR) ? 2 : 0);
   a.nbase = nbase;
   a.ncol = params ? ncol : nbase;
   for (int j = 0; j < KMLP_MAXCOL; ++j) a.extra[j] = (params && j < n_extra) ? extra[j] : 0.f;
-  const size_t ncells = (size_t)a.C * a.C + 1;
+  const size_t ncells = (size_t)a.C * a.C + 1;  // + the bucket of bodies with mask <= 0
+  const int ntiles = (int)((ncells + SCAN_TILE - 1) / SCAN_TILE);
   int rc = AUGUR_OK;
   if (!p->pair_key) {
     rc |= dalloc(p, &p->pair_key, (size_t)p->max_n);
-    rc |= dalloc(p, &p->pair_order, (size_t)p->max_n);
+    rc |= dalloc(p, &p->pair_rank, (size_t)p->max_n);
+    rc |= dalloc(p, &p->pair_sorted, (size_t)p->max_n);
     rc |= dalloc(p, &p->pair_params, (size_t)KMLP_H * KMLP_MAXCOL + KMLP_H * KMLP_H + 3 * KMLP_H + 1);
     if (rc) return AUGUR_ENOMEM;
   }
   if (ncells > p->pair_cells_cap) {
-    for (uint32_t **q : {&p->pair_cnt, &p->pair_start, &p->pair_fill}) {
-      if (*q) {
-        cudaFree(*q);
-        p->bytes -= p->pair_cells_cap * sizeof(uint32_t);
-        *q = nullptr;
-      }
-      rc |= dalloc(p, q, ncells);
-    }
-    if (rc) {
-      p->pair_cells_cap = 0;
-      return AUGUR_ENOMEM;
-    }
+    const size_t nt = (p->pair_cells_cap + SCAN_TILE - 1) / SCAN_TILE;
+    const size_t old_bytes = sizeof(uint32_t) * (p->pair_cells_cap + (nt + 1) * SCAN_TILE + 2 * nt + 1);
+    for (uint32_t *q : {p->pair_cnt, p->pair_start, p->pair_tsum, p->pair_toff})
+      if (q) cudaFree(q);
+    if (p->pair_cnt) p->bytes -= old_bytes;
+    p->pair_cnt = p->pair_start = p->pair_tsum = p->pair_toff = nullptr;
+    p->pair_cells_cap = 0;
+    rc |= dalloc(p, &p->pair_cnt, ncells);
+    rc |= dalloc(p, &p->pair_start, (size_t)(ntiles + 1) * SCAN_TILE);
+    rc |= dalloc(p, &p->pair_tsum, (size_t)ntiles);
+    rc |= dalloc(p, &p->pair_toff, (size_t)ntiles + 1);
+    if (rc) return AUGUR_ENOMEM;
+    // the scan clears the counts it reads, so they stay zero between calls
+    if (cudaMemset(p->pair_cnt, 0, ncells * sizeof(uint32_t)) != cudaSuccess) return AUGUR_ECUDA;
     p->pair_cells_cap = ncells;
+  }
+  int KP = 1;
+  while (KP < knn) KP <<= 1;
+  if (KP > p->pair_kp) {
+    if (p->pair_nbj) {
+      cudaFree(p->pair_nbj);
+      cudaFree(p->pair_nbq);
+      p->bytes -= (size_t)p->max_n * p->pair_kp * 8;
+      p->pair_nbj = nullptr;
+      p->pair_nbq = nullptr;
+    }
+    p->pair_kp = 0;
+    rc |= dalloc(p, &p->pair_nbj, (size_t)p->max_n * KP);
+    rc |= dalloc(p, &p->pair_nbq, (size_t)p->max_n * KP);
+    if (rc) return AUGUR_ENOMEM;
+    p->pair_kp = KP;
   }
   size_t np = 0;
   if (params) {
@@ -989,17 +1019,21 @@ int augur_pm_pair_acc(augur_pm_plan *p, const float *pos, const float *mass, con
     if (cudaMemcpyAsync(p->pair_params, params, np * sizeof(float), cudaMemcpyDefault, st) != cudaSuccess)
       return AUGUR_ECUDA;
   }
-  if (cudaMemsetAsync(p->pair_cnt, 0, ncells * sizeof(uint32_t), st) != cudaSuccess) return AUGUR_ECUDA;
   const unsigned nb = blocks_for(n, 256);
-  pair_keys_kernel<<<nb, 256, 0, st>>>(pos, mask, n, a, p->pair_key, p->pair_cnt);
+  pair_keys_kernel<<<nb, 256, 0, st>>>(pos, mask, n, a, p->pair_key, p->pair_rank, p->pair_cnt);
   AUGUR_LAUNCH_CHECK(p);
-  pair_scan_kernel<<<1, 1024, 0, st>>>(p->pair_cnt, (int)(ncells - 1), p->pair_start, p->pair_fill);
+  scan_local_kernel<<<ntiles, 1024, 0, st>>>(p->pair_cnt, p->pair_start, p->pair_tsum, (int)ncells);
   AUGUR_LAUNCH_CHECK(p);
-  pair_scatter_kernel<<<nb, 256, 0, st>>>(p->pair_key, n, p->pair_fill, p->pair_order);
+  scan_tiles_kernel<<<1, 1024, 0, st>>>(p->pair_tsum, p->pair_toff, ntiles);
   AUGUR_LAUNCH_CHECK(p);
-  pair_acc_kernel<<<blocks_for(n, 128), 128, np * sizeof(float), st>>>(pos, mass, mask, n, p->pair_start,
-                                                                        p->pair_order, params ? p->pair_params : nullptr,
-                                                                        a, acc);
+  pair_scatter_kernel<<<nb, 256, 0, st>>>(pos, p->pair_key, p->pair_rank, n, p->pair_start, p->pair_toff,
+                                          p->pair_sorted);
+  AUGUR_LAUNCH_CHECK(p);
+  pair_search_kernel<<<blocks_for(n, 128), 128, 0, st>>>(p->pair_sorted, n, p->pair_start, p->pair_toff, a, KP,
+                                                          p->pair_nbj, p->pair_nbq);
+  AUGUR_LAUNCH_CHECK(p);
+  pair_weight_kernel<<<blocks_for(n * KP, 128), 128, np * sizeof(float), st>>>(
+      p->pair_sorted, pos, mass, mask, n, KP, p->pair_nbj, p->pair_nbq, params ? p->pair_params : nullptr, a, acc);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }

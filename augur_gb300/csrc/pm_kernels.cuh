@@ -820,181 +820,214 @@ __global__ void __launch_bounds__(256) kmlp_lattice_kernel(const float *__restri
 
 // ---------------------------------------------------------------------------------
 // Pair term of the isolated 2D model (ScatterField.pp_acc, scripts/scatter_field.py:291-300,
-// 324-364, 500-521): cells of side ppe (clamped into the C x C box), a counting sort of the
-// bodies with mask > 0 by cell, then per body the knn nearest others among the 3 x 3 cells
-// around its own (every body closer than ppe lies there; the weight vanishes beyond ppe).
+// 324-364, 500-521). The reference sorts bodies with mask > 0 into cells of side ppe and takes
+// each body's knn nearest among the 3 x 3 cells around it; a pair's weight is exactly zero once
+// r / ppe rounds to 1, so the knn nearest within ppe decide the sum. Here the cells are finer
+// (side ppe / m, clamped into C x C as in _cell_keys) and a body searches rings of cells outwards
+// from its own, skipping every cell that cannot hold a candidate nearer than its current knn-th;
+// candidates are ranked by (|d|^2 + 1e-8, index), which fixes the selection and the summation
+// order whatever the order of the bodies in memory.
 // ---------------------------------------------------------------------------------
 struct PairArgs {
-  int C, knn, ncol, nbase, flags;
-  float half_ext, cs, inv_ppe, eps2, h;  // cs: cell side (ppe, or coarser when ceil(extent/ppe) > PAIR_CMAX)
+  int C, W, knn, ncol, nbase, flags;
+  float half_ext, cs, inv_ppe, thr0, eps2, h, slack;
   float extra[KMLP_MAXCOL];
 };
 constexpr int PAIR_CMAX = 2048;
+constexpr int PAIR_KMAX = 32;
 
 __device__ __forceinline__ int pair_cell(float x, const PairArgs &a) {
   const float c = floorf(__fdiv_rn(__fadd_rn(x, a.half_ext), a.cs));
   return (int)fminf(fmaxf(c, 0.f), (float)(a.C - 1));
 }
 
+// key (cell, or C*C for mask <= 0) and rank of the body within its cell
 __global__ void pair_keys_kernel(const float *__restrict__ pos, const float *__restrict__ mask, int64_t n, PairArgs a,
-                                 uint32_t *__restrict__ key, uint32_t *__restrict__ counts) {
+                                 uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
+                                 uint32_t *__restrict__ counts) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint32_t k = (uint32_t)(a.C * a.C);  // excluded
+  uint32_t k = (uint32_t)(a.C * a.C);
   if (mask[i] > 0.f) k = (uint32_t)(pair_cell(pos[2 * i + 1], a) * a.C + pair_cell(pos[2 * i], a));
   key[i] = k;
-  atomicAdd(&counts[k], 1u);
+  rank[i] = atomicAdd(&counts[k], 1u);
 }
 
-// exclusive scan of counts[0 .. ncell] into start and fill (one CTA)
-__global__ void __launch_bounds__(1024) pair_scan_kernel(const uint32_t *__restrict__ counts, int ncell,
-                                                         uint32_t *__restrict__ start, uint32_t *__restrict__ fill) {
-  __shared__ uint32_t ws[32];
-  __shared__ uint32_t carry;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) carry = 0;
-  __syncthreads();
-  for (int base = 0; base <= ncell; base += 1024) {
-    const int e = base + tid;
-    const uint32_t v = e <= ncell ? counts[e] : 0u;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) ws[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = ws[lane], t = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
+// sorted[slot] = (x, y, 0, index bits); slot = cell start (two-level scan) + rank
+__global__ void pair_scatter_kernel(const float *__restrict__ pos, const uint32_t *__restrict__ key,
+                                    const uint32_t *__restrict__ rank, int64_t n, const uint32_t *__restrict__ start,
+                                    const uint32_t *__restrict__ tile_off, float4 *__restrict__ sorted) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = key[i];
+  const uint32_t s = tile_off[k / SCAN_TILE] + start[k] + rank[i];
+  sorted[s] = make_float4(pos[2 * i], pos[2 * i + 1], 0.f, __uint_as_float((uint32_t)i));
+}
+
+__device__ __forceinline__ float pair_gelu(float t) { return 0.5f * t * (1.f + erff(t * 0.70710678118654752440f)); }
+
+// lower bound of the distance from coordinate x to cell c's extent along one axis (edge cells
+// extend to infinity: they hold the clamped bodies)
+__device__ __forceinline__ float pair_gap(float x, int c, const PairArgs &a) {
+  float g = 0.f;
+  if (c > 0) g = fmaxf(g, ((float)c * a.cs - a.half_ext) - x);
+  if (c < a.C - 1) g = fmaxf(g, x - ((float)(c + 1) * a.cs - a.half_ext));
+  return fmaxf(g - a.slack, 0.f);
+}
+
+// Search: one thread per sorted slot; writes the slot's neighbour list (index, |d|^2 + 1e-8) in
+// ascending (|d|^2 + 1e-8, index) order to nb_j / nb_q[slot * KP ..], unused entries j = ~0u.
+__global__ void __launch_bounds__(128) pair_search_kernel(const float4 *__restrict__ sorted, int64_t n,
+                                                          const uint32_t *__restrict__ start,
+                                                          const uint32_t *__restrict__ tile_off, PairArgs a, int KP,
+                                                          uint32_t *__restrict__ nb_j, float *__restrict__ nb_q) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float4 me = sorted[t];
+  const uint32_t i = __float_as_uint(me.w);
+  const uint32_t excl = (uint32_t)a.C * a.C;
+  auto begin = [&](uint32_t c) { return tile_off[c / SCAN_TILE] + start[c]; };
+  float qk[PAIR_KMAX];
+  uint32_t jk[PAIR_KMAX];
+  int cnt = 0;
+  if ((uint32_t)t < begin(excl)) {
+    const float xi = me.x, yi = me.y;
+    const int cx = pair_cell(xi, a), cy = pair_cell(yi, a);
+    const int K = a.knn;
+    float thr = a.thr0;  // candidates at or beyond thr0 have exactly zero weight
+    for (int d = 0; d <= a.W; ++d) {
+      if (d >= 2) {
+        const float lb = fmaxf((float)(d - 1) * a.cs - a.slack, 0.f);
+        if (lb * lb > thr) break;
       }
-      ws[lane] = t - w;
+      for (int oy = -d; oy <= d; ++oy) {
+        const int yy = cy + oy;
+        if (yy < 0 || yy >= a.C) continue;
+        const float gy = pair_gap(yi, yy, a);
+        if (gy * gy > thr) continue;
+        const int step = (d == 0 || oy == -d || oy == d) ? 1 : 2 * d;
+        for (int ox = -d; ox <= d; ox += step) {
+          const int xx = cx + ox;
+          if (xx < 0 || xx >= a.C) continue;
+          const float gx = pair_gap(xi, xx, a);
+          if (gx * gx + gy * gy > thr) continue;
+          const uint32_t c = (uint32_t)(yy * a.C + xx);
+          const uint32_t s1 = begin(c + 1);
+          for (uint32_t s = begin(c); s < s1; ++s) {
+            const float4 v = sorted[s];
+            const uint32_t j = __float_as_uint(v.w);
+            const float dx = v.x - xi, dy = v.y - yi;
+            const float q = dx * dx + dy * dy + 1e-8f;
+            if (!(q < thr || (q == thr && cnt == K && j < jk[K - 1])) || j == i) continue;
+            int p = cnt < K ? cnt : K - 1;
+            while (p > 0 && (qk[p - 1] > q || (qk[p - 1] == q && jk[p - 1] > j))) {
+              qk[p] = qk[p - 1];
+              jk[p] = jk[p - 1];
+              --p;
+            }
+            qk[p] = q;
+            jk[p] = j;
+            if (cnt < K) ++cnt;
+            if (cnt == K) thr = qk[K - 1];
+          }
+        }
+      }
     }
-    __syncthreads();
-    const uint32_t ex = carry + ws[warp] + x - v;
-    if (e <= ncell) {
-      start[e] = ex;
-      fill[e] = ex;
-    }
-    __syncthreads();
-    if (tid == 1023) carry = ex + v;
-    __syncthreads();
+  }
+  for (int q = 0; q < KP; ++q) {
+    nb_j[t * KP + q] = q < cnt ? jk[q] : ~0u;
+    nb_q[t * KP + q] = q < cnt ? qk[q] : 0.f;
   }
 }
 
-__global__ void pair_scatter_kernel(const uint32_t *__restrict__ key, int64_t n, uint32_t *__restrict__ fill,
-                                    uint32_t *__restrict__ order) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  order[atomicAdd(&fill[key[i]], 1u)] = (uint32_t)i;
-}
-
-constexpr int PAIR_KMAX = 32;
-__global__ void __launch_bounds__(128) pair_acc_kernel(const float *__restrict__ pos, const float *__restrict__ mass,
-                                                       const float *__restrict__ mask, int64_t n,
-                                                       const uint32_t *__restrict__ start,
-                                                       const uint32_t *__restrict__ order,
-                                                       const float *__restrict__ params, PairArgs a,
-                                                       float *__restrict__ acc) {
-  extern __shared__ float sp[];  // ppmlp: W1 (64 x ncol), b1, W2 (64 x 64), b2, W3 (64), b3
+// Weights: KP lanes (a power of two) per sorted slot, one neighbour each, reduced over the lanes
+// by a fixed butterfly; lane 0 writes the body's acceleration (0 for mask <= 0).
+__global__ void __launch_bounds__(128) pair_weight_kernel(const float4 *__restrict__ sorted, const float *__restrict__ pos,
+                                                          const float *__restrict__ mass,
+                                                          const float *__restrict__ mask, int64_t n, int KP,
+                                                          const uint32_t *__restrict__ nb_j,
+                                                          const float *__restrict__ nb_q,
+                                                          const float *__restrict__ params, PairArgs a,
+                                                          float *__restrict__ acc) {
+  extern __shared__ __align__(16) float sp[];  // ppmlp: W1 (64 x ncol), b1, W2 (64 x 64), b2, W3 (64), b3
   const bool mlp = params != nullptr;
   if (mlp) {
     const int np = KMLP_H * a.ncol + KMLP_H + KMLP_H * KMLP_H + KMLP_H + KMLP_H + 1;
     for (int e = threadIdx.x; e < np; e += blockDim.x) sp[e] = params[e];
     __syncthreads();
   }
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float ax = 0.f, ay = 0.f;
-  if (mask[i] > 0.f) {
-    const float xi = pos[2 * i], yi = pos[2 * i + 1];
-    const int cx = pair_cell(xi, a), cy = pair_cell(yi, a);
-    float rk[PAIR_KMAX];
-    uint32_t jk[PAIR_KMAX];
-    int cnt = 0;
-    const int K = a.knn;
-    for (int oy = -1; oy <= 1; ++oy) {
-      const int yy = cy + oy;
-      if (yy < 0 || yy >= a.C) continue;
-      for (int ox = -1; ox <= 1; ++ox) {
-        const int xx = cx + ox;
-        if (xx < 0 || xx >= a.C) continue;
-        const int c = yy * a.C + xx;
-        for (uint32_t t = start[c]; t < start[c + 1]; ++t) {
-          const uint32_t j = order[t];
-          if (j == (uint32_t)i) continue;
-          const float dx = pos[2 * j] - xi, dy = pos[2 * j + 1] - yi;
-          const float r = sqrtf(dx * dx + dy * dy + 1e-8f);
-          // ascending (r, j): equal distances keep the lower index first
-          if (cnt == K && (r > rk[K - 1] || (r == rk[K - 1] && j > jk[K - 1]))) continue;
-          int p = cnt < K ? cnt : K - 1;
-          while (p > 0 && (rk[p - 1] > r || (rk[p - 1] == r && jk[p - 1] > j))) {
-            rk[p] = rk[p - 1];
-            jk[p] = jk[p - 1];
-            --p;
-          }
-          rk[p] = r;
-          jk[p] = j;
-          if (cnt < K) ++cnt;
-        }
+  const int64_t g_id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = g_id / KP;  // KP divides 32: a slot's lanes share a warp
+  const bool live = t < n;      // every lane stays for the shuffles below
+  const uint32_t j = live ? nb_j[g_id] : ~0u;
+  float cx = 0.f, cy = 0.f;
+  const float4 me = live ? sorted[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (j != ~0u) {
+    const float r = sqrtf(nb_q[g_id]);
+    const float dx = pos[2 * j] - me.x, dy = pos[2 * j + 1] - me.y;
+    const float u0 = fminf(r * a.inv_ppe, 1.f), u = u0 * u0;
+    const float win = (1.f - u) * (1.f - u);
+    float w = 0.f;
+    if (mlp && win > 0.f) {
+      const float *W1 = sp, *b1 = W1 + KMLP_H * a.ncol, *W2 = b1 + KMLP_H, *b2 = W2 + KMLP_H * KMLP_H;
+      const float *W3 = b2 + KMLP_H, *b3 = W3 + KMLP_H;
+      float f[KMLP_MAXCOL];
+      if (a.flags & 1) {
+        f[0] = r / a.h;
+        f[1] = logf(r / a.h + 0.1f);
+        f[2] = logf(0.5f / a.h);
+      } else {
+        f[0] = r;
+        f[1] = logf(r + 0.05f);
       }
+#pragma unroll
+      for (int e = 2; e < KMLP_MAXCOL; ++e)
+        if (e >= a.nbase) f[e] = e < a.ncol ? a.extra[e - a.nbase] : 0.f;
+      float h1[KMLP_H];
+#pragma unroll
+      for (int o = 0; o < KMLP_H; ++o) {
+        float z = b1[o];
+#pragma unroll
+        for (int e = 0; e < KMLP_MAXCOL; ++e)
+          if (e < a.ncol) z += W1[o * a.ncol + e] * f[e];
+        h1[o] = pair_gelu(z);
+      }
+      float gsum = b3[0];
+#pragma unroll 1
+      for (int o = 0; o < KMLP_H; ++o) {
+        const float4 *w4 = reinterpret_cast<const float4 *>(W2 + o * KMLP_H);
+        float z = b2[o];
+#pragma unroll
+        for (int e = 0; e < KMLP_H / 4; ++e) {
+          const float4 wv = w4[e];
+          z += wv.x * h1[4 * e];
+          z += wv.y * h1[4 * e + 1];
+          z += wv.z * h1[4 * e + 2];
+          z += wv.w * h1[4 * e + 3];
+        }
+        gsum += W3[o] * pair_gelu(z);
+      }
+      w = gsum * win;
     }
-    const float *W1 = sp, *b1 = W1 + KMLP_H * a.ncol, *W2 = b1 + KMLP_H, *b2 = W2 + KMLP_H * KMLP_H;
-    const float *W3 = b2 + KMLP_H, *b3 = W3 + KMLP_H;
-    for (int q = 0; q < cnt; ++q) {
-      const float r = rk[q];
-      const uint32_t j = jk[q];
-      const float u0 = fminf(r * a.inv_ppe, 1.f), u = u0 * u0;
-      const float win = (1.f - u) * (1.f - u);
-      float w = 0.f;
-      if (mlp && win > 0.f) {
-        float f[KMLP_MAXCOL];
-        if (a.flags & 1) {
-          f[0] = r / a.h;
-          f[1] = logf(r / a.h + 0.1f);
-          f[2] = logf(0.5f / a.h);
-        } else {
-          f[0] = r;
-          f[1] = logf(r + 0.05f);
-        }
-#pragma unroll
-        for (int e = 2; e < KMLP_MAXCOL; ++e)
-          if (e >= a.nbase) f[e] = e < a.ncol ? a.extra[e - a.nbase] : 0.f;
-        float h1[KMLP_H];
-#pragma unroll
-        for (int o = 0; o < KMLP_H; ++o) {
-          float t = b1[o];
-#pragma unroll
-          for (int e = 0; e < KMLP_MAXCOL; ++e)
-            if (e < a.ncol) t += W1[o * a.ncol + e] * f[e];
-          h1[o] = 0.5f * t * (1.f + erff(t * 0.70710678118654752440f));
-        }
-        float g = b3[0];
-        for (int o = 0; o < KMLP_H; ++o) {
-          float t = b2[o];
-#pragma unroll 8
-          for (int e = 0; e < KMLP_H; ++e) t += W2[o * KMLP_H + e] * h1[e];
-          g += W3[o] * (0.5f * t * (1.f + erff(t * 0.70710678118654752440f)));
-        }
-        w = g * win;
-      }
-      if (a.flags & 2) {
-        const float qd = sqrtf(r * r + a.eps2);
-        const float q3 = qd * qd * qd;
-        const float a_mesh = -4.f * (1.f - u) * r * a.inv_ppe * a.inv_ppe / qd + (1.f - win) * r / q3;
-        w += r / q3 - a_mesh;
-      }
-      w *= mass[j] * mask[j];
-      ax += w * (pos[2 * j] - xi) / r;
-      ay += w * (pos[2 * j + 1] - yi) / r;
+    if (a.flags & 2) {
+      const float qd = sqrtf(r * r + a.eps2);
+      const float q3 = qd * qd * qd;
+      const float a_mesh = -4.f * (1.f - u) * r * a.inv_ppe * a.inv_ppe / qd + (1.f - win) * r / q3;
+      w += r / q3 - a_mesh;
     }
+    w *= mass[j] * mask[j];
+    cx = w * dx / r;
+    cy = w * dy / r;
   }
-  acc[2 * i] = ax;
-  acc[2 * i + 1] = ay;
+  for (int o = KP >> 1; o > 0; o >>= 1) {
+    cx += __shfl_xor_sync(0xffffffffu, cx, o);
+    cy += __shfl_xor_sync(0xffffffffu, cy, o);
+  }
+  if (live && (g_id & (KP - 1)) == 0) {
+    const uint32_t i = __float_as_uint(me.w);
+    acc[2 * (int64_t)i] = cx;
+    acc[2 * (int64_t)i + 1] = cy;
+  }
 }
 
 // ---------------------------------------------------------------------------------

@@ -134,9 +134,11 @@ int augur_pm_reset_kernel(augur_pm_plan *plan, void *stream);
  * features [r, log(r + 0.05)], or with AUGUR_KERNEL_CELL_UNITS [r/h, log(r/h + 0.1), log(0.5/h)]
  * (h = extent/grid), then the n_extra constants; AUGUR_KERNEL_PRIOR adds
  * r/q^3 - a_mesh, q = sqrt(r^2 + eps^2), a_mesh = -4 (1 - u) r / (ppe^2 q) + (1 - (1 - u)^2) r / q^3.
- * Bodies with mask <= 0 get 0. The weight vanishes at r >= ppe, so the 3 x 3 search equals the
- * reference's dense top-knn; equal distances rank the lower index first. Deterministic. The
- * first call (and one that needs more cells than before) allocates scratch: make it before
+ * Bodies with mask <= 0 get 0. The weight is exactly 0 once r/ppe rounds to 1, so only the knn
+ * nearest within ppe count, as in every mode of the reference; the search runs on cells of side
+ * ppe/4 (coarser when that needs more than 2048 a side) and ranks candidates by
+ * (|d|^2 + 1e-8, index), so the result does not depend on the order of the bodies. The first call
+ * (and one that needs more cells or a larger knn than before) allocates scratch: make it before
  * any stream capture. pos (N, 2), mass, mask (N,), acc_out (N, 2): device float32.
  */
 int augur_pm_pair_acc(augur_pm_plan *plan, const float *pos, const float *mass, const float *mask,
