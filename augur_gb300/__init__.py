@@ -6,5 +6,6 @@ package: calls on CPU tensors raise.
 """
 from .pm import PMPlan, direct_sum_fp64, energy_fp64
 from .scatter_field import ScatterField, pm_acc
+from .field2d import UNetScatterField
 
-__all__ = ["PMPlan", "ScatterField", "pm_acc", "direct_sum_fp64", "energy_fp64"]
+__all__ = ["PMPlan", "ScatterField", "UNetScatterField", "pm_acc", "direct_sum_fp64", "energy_fp64"]

@@ -50,6 +50,18 @@ SIGNATURES = {
     "augur_direct_sum_fp64": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp]),
     "augur_energy_fp64": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp]),
     "augur_direct_sum_fp64_noalloc": (_i32, [_vp, _vp, _i64, _vp, _vp, _i64, _i32, _f64, _vp, _vp]),
+    # include/augur_field2d.h
+    "augur_field2d_scatter_work_bytes": (C.c_size_t, [_i32]),
+    "augur_field2d_scatter": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp, _vp]),
+    "augur_field2d_inputs": (_i32, [_vp, _vp, _i32, _i32, _vp, _vp]),
+    "augur_unet2d_param_count": (_i64, [_i32, _i32, _i32, _i32]),
+    "augur_unet2d_work_bytes": (C.c_size_t, [_i32, _i32, _i32]),
+    "augur_unet2d_forward": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, C.c_size_t, _vp]),
+    "augur_field2d_accel": (_i32, [_vp, _vp, _i32, _f64, _vp, _vp]),
+    "augur_field2d_finish_work_bytes": (C.c_size_t, []),
+    "augur_field2d_finish": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "augur_field2d_drift": (_i32, [_vp, _vp, _vp, _i64, _f64, _vp, _vp, _vp]),
+    "augur_field2d_kick": (_i32, [_vp, _vp, _vp, _i64, _f64, _vp, _vp, _vp]),
     # include/augur_cnn.h
     "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp, _vp]),
     "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),

@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libaugur_gb300.so"
 
-SOURCES = ["pm_api.cu", "direct_sum.cu", "conv3d.cu"]
+SOURCES = ["pm_api.cu", "direct_sum.cu", "conv3d.cu", "field2d.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

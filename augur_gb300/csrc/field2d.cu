@@ -1,0 +1,528 @@
+// field2d.cu — the reference's production 2D scatter-field model around the PM plan:
+// three-channel CIC scatter, the 5-level U-Net grid net with the recurrent potential input,
+// potential gradient + learned kernel acceleration, momentum fix and the velocity-Verlet
+// pieces (ScatterField with net="unet", potential=True, kernel=True, pp>0, verlet=True;
+// scripts/scatter_field.py:28-67, 221-261, 551-555, 561-688).
+//
+// The U-Net runs in fp32 on the CUDA cores, as the reference's default path does: a 3x3
+// convolution kernel whose input loader also performs avg_pool2d(2) of the previous level,
+// or nearest upsampling by 2 concatenated with the skip tensor, so pooling, upsampling and
+// concatenation never materialise. Layout: channels-first (C, H, W) per scene, as torch's
+// NCHW with B = 1.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+
+#include "augur_common.cuh"
+#include "augur_field2d.h"
+
+namespace {
+
+cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+unsigned nblocks(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+#define F2_LAUNCH_CHECK()                                                                                  \
+  do {                                                                                                     \
+    cudaError_t _e = cudaGetLastError();                                                                   \
+    if (_e != cudaSuccess) {                                                                               \
+      fprintf(stderr, "augur: launch failed: %s (%s:%d)\n", cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return AUGUR_ECUDA;                                                                                  \
+    }                                                                                                      \
+  } while (0)
+
+__device__ __forceinline__ float gelu_erf(float t) { return 0.5f * t * (1.f + erff(t * 0.70710678118654752440f)); }
+
+// ---------------------------------------------------------------------------------
+// Three-channel scatter [m, m vx, m vy] * in_scale / h^2 (ScatterField.scatter,
+// scripts/scatter_field.py:237-250), out-of-grid corners dropped (:208). Deterministic:
+// each corner's fp32 contribution is rounded to a per-channel fixed point 2^-e_c and summed
+// with 64-bit integer atomics, where e_c keeps n * max|value_c| below 2^61.
+// ---------------------------------------------------------------------------------
+struct ScatterArgs {
+  int G;
+  float E, h, scale;  // scale = in_scale / h^2
+};
+
+__device__ __forceinline__ void cic2(float x, float y, const ScatterArgs &a, int &ix, int &iy, float &wx, float &wy) {
+  // ScatterField._corners: u = (x + E/2) / h - 0.5, i0 = floor(u), w = u - i0 (fp32)
+  const float ux = __fsub_rn(__fdiv_rn(__fadd_rn(x, 0.5f * a.E), a.h), 0.5f);
+  const float uy = __fsub_rn(__fdiv_rn(__fadd_rn(y, 0.5f * a.E), a.h), 0.5f);
+  const float fx = floorf(ux), fy = floorf(uy);
+  ix = (int)fx;
+  iy = (int)fy;
+  wx = __fsub_rn(ux, fx);
+  wy = __fsub_rn(uy, fy);
+}
+
+__global__ void f2_absmax_kernel(const float *__restrict__ vel, const float *__restrict__ mass,
+                                 const float *__restrict__ mask, int64_t n, float scale, unsigned *__restrict__ mx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+  if (i < n) {
+    const float mm = mass[i] * mask[i];
+    const float v0 = mm * scale, v1 = mm * vel[2 * i] * scale, v2 = mm * vel[2 * i + 1] * scale;
+    m0 = fabsf(v0);
+    m1 = fabsf(v1);
+    m2 = fabsf(v2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {  // non-negative floats order as their bit patterns
+    atomicMax(&mx[0], __float_as_uint(m0));
+    atomicMax(&mx[1], __float_as_uint(m1));
+    atomicMax(&mx[2], __float_as_uint(m2));
+  }
+}
+
+__device__ __forceinline__ int fix_exp(unsigned mbits, int64_t n) {
+  const float m = __uint_as_float(mbits);
+  if (!(m > 0.f) || !isfinite(m)) return 0;
+  int ex;
+  frexpf(m, &ex);  // m < 2^ex
+  int ln = 0;
+  while ((1ll << ln) < n) ++ln;  // n <= 2^ln
+  return 61 - ex - ln;
+}
+
+__global__ void f2_scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
+                                  const float *__restrict__ mass, const float *__restrict__ mask, int64_t n,
+                                  ScatterArgs a, const unsigned *__restrict__ mx,
+                                  unsigned long long *__restrict__ acc) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float mm = mass[i] * mask[i];
+  const float val[3] = {mm * a.scale, mm * vel[2 * i] * a.scale, mm * vel[2 * i + 1] * a.scale};
+  double sc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) sc[c] = ldexp(1.0, fix_exp(mx[c], n));
+  int ix, iy;
+  float wx, wy;
+  cic2(pos[2 * i], pos[2 * i + 1], a, ix, iy, wx, wy);
+  const int G = a.G;
+#pragma unroll
+  for (int oy = 0; oy < 2; ++oy) {
+#pragma unroll
+    for (int ox = 0; ox < 2; ++ox) {
+      const int x = ix + ox, y = iy + oy;
+      if (x < 0 || x >= G || y < 0 || y >= G) continue;
+      const float w = (ox ? wx : 1.f - wx) * (oy ? wy : 1.f - wy);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long q = __double2ll_rn((double)(val[c] * w) * sc[c]);
+        atomicAdd(&acc[((size_t)c * G + y) * G + x], (unsigned long long)q);
+      }
+    }
+  }
+}
+
+__global__ void f2_convert_kernel(const unsigned long long *__restrict__ acc, const unsigned *__restrict__ mx, int64_t n,
+                                  int G, float *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 3ll * G * G) return;
+  const int c = (int)(e / ((int64_t)G * G));
+  const long long q = (long long)acc[e];
+  out[e] = (float)ldexp((double)q, -fix_exp(mx[c], n));
+}
+
+// ---------------------------------------------------------------------------------
+// Input stack channels 3.. : kernel acceleration (a_x, a_y lanes of the plan's force grid)
+// then the recurrent field (ScatterField._grid_force concatenation order, :633-640).
+// ---------------------------------------------------------------------------------
+__global__ void f2_inputs_kernel(const float4 *__restrict__ F4k, const float *__restrict__ field, int cf, int G,
+                                 float *__restrict__ x) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int GG = G * G;
+  if (e >= GG) return;
+  const float4 f = F4k[e];
+  x[3 * GG + e] = f.x;
+  x[4 * GG + e] = f.y;
+  for (int c = 0; c < cf; ++c) x[(5 + c) * GG + e] = field ? field[c * GG + e] : 0.f;
+}
+
+// ---------------------------------------------------------------------------------
+// 3x3 convolution, zero padding 1, fp32. One CTA = an 8 x 8 output tile x all output
+// channels (<= 32): thread (pixel, group of 8 output channels). Input channels in chunks of
+// 8, staged with their halo in shared memory by a loader that applies the source mode:
+//   A_SAME: srcA at the output resolution; A_POOL: 2x2 average of srcA at twice the
+//   resolution (avg_pool2d(2)); A_UP: srcA at half the resolution, nearest (interpolate x2).
+// Channels [CA, CA + CB) come from srcB at the output resolution (the U-Net's skip).
+// ---------------------------------------------------------------------------------
+enum { A_SAME = 0, A_POOL = 1, A_UP = 2 };
+constexpr int CT = 8;   // output tile side
+constexpr int KC = 8;   // input channels per chunk
+constexpr int CO = 32;  // output channels per CTA (max)
+
+struct ConvSrc {
+  const float *a;
+  const float *b;
+  int ca, cb, mode;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(256) f2_conv3_kernel(ConvSrc src, const float *__restrict__ W,
+                                                       const float *__restrict__ bias, int cout, int H,
+                                                       int act, float *__restrict__ out) {
+  __shared__ float sx[KC][CT + 2][CT + 2];
+  __shared__ __align__(16) float sw[KC][9][CO];
+  const int tid = threadIdx.x;
+  const int p = tid & 63, cg = tid >> 6;
+  const int px = p & 7, py = p >> 3;
+  const int x0 = blockIdx.x * CT, y0 = blockIdx.y * CT;
+  const int cin = src.ca + src.cb;
+  float acc[8];
+#pragma unroll
+  for (int o = 0; o < 8; ++o) acc[o] = 0.f;
+  for (int c0 = 0; c0 < cin; c0 += KC) {
+    // input chunk with halo
+    for (int e = tid; e < KC * (CT + 2) * (CT + 2); e += 256) {
+      const int c = e / ((CT + 2) * (CT + 2)), r = e % ((CT + 2) * (CT + 2));
+      const int yy = y0 + r / (CT + 2) - 1, xx = x0 + r % (CT + 2) - 1;
+      const int ch = c0 + c;
+      float v = 0.f;
+      if (ch < cin && yy >= 0 && yy < H && xx >= 0 && xx < H) {
+        if (ch < src.ca) {
+          if (MODE == A_SAME) {
+            v = src.a[((size_t)ch * H + yy) * H + xx];
+          } else if (MODE == A_POOL) {
+            const int H2 = 2 * H;
+            const float *q = src.a + ((size_t)ch * H2 + 2 * yy) * H2 + 2 * xx;
+            v = (((q[0] + q[1]) + q[H2]) + q[H2 + 1]) * 0.25f;
+          } else {
+            const int Hh = H >> 1;
+            v = src.a[((size_t)ch * Hh + (yy >> 1)) * Hh + (xx >> 1)];
+          }
+        } else {
+          v = src.b[((size_t)(ch - src.ca) * H + yy) * H + xx];
+        }
+      }
+      sx[c][r / (CT + 2)][r % (CT + 2)] = v;
+    }
+    // weights W[o][ch][tap] -> sw[c][tap][o]
+    for (int e = tid; e < KC * 9 * CO; e += 256) {
+      const int o = e % CO, t = (e / CO) % 9, c = e / (9 * CO);
+      const int ch = c0 + c;
+      sw[c][t][o] = (o < cout && ch < cin) ? W[((size_t)o * cin + ch) * 9 + t] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < KC; ++c) {
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const float v = sx[c][py + t / 3][px + t % 3];
+        const float4 w0 = *reinterpret_cast<const float4 *>(&sw[c][t][cg * 8]);
+        const float4 w1 = *reinterpret_cast<const float4 *>(&sw[c][t][cg * 8 + 4]);
+        acc[0] += w0.x * v;
+        acc[1] += w0.y * v;
+        acc[2] += w0.z * v;
+        acc[3] += w0.w * v;
+        acc[4] += w1.x * v;
+        acc[5] += w1.y * v;
+        acc[6] += w1.z * v;
+        acc[7] += w1.w * v;
+      }
+    }
+    __syncthreads();
+  }
+  const int x = x0 + px, y = y0 + py;
+  if (x >= H || y >= H) return;
+#pragma unroll
+  for (int o = 0; o < 8; ++o) {
+    const int oc = cg * 8 + o;
+    if (oc < cout) {
+      const float z = acc[o] + bias[oc];
+      out[((size_t)oc * H + y) * H + x] = act ? gelu_erf(z) : z;
+    }
+  }
+}
+
+int conv3(const ConvSrc &s, const float *W, const float *b, int cout, int H, int act, float *out, cudaStream_t st) {
+  if (cout < 1 || cout > CO) return AUGUR_EINVAL;
+  dim3 grid((H + CT - 1) / CT, (H + CT - 1) / CT);
+  switch (s.mode) {
+    case A_SAME: f2_conv3_kernel<A_SAME><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
+    case A_POOL: f2_conv3_kernel<A_POOL><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
+    default: f2_conv3_kernel<A_UP><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
+  }
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Grid acceleration -grad(phi) (central differences, zero padding; ScatterField.neg_grad,
+// :551-555) plus the kernel acceleration, as a float4 grid (a_x, a_y, 0, 0) for the gather.
+// ---------------------------------------------------------------------------------
+__global__ void f2_accel_kernel(const float *__restrict__ phi, const float4 *__restrict__ F4k, int G, float two_h,
+                                float4 *__restrict__ F4) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= G * G) return;
+  const int y = e / G, x = e - y * G;
+  const float xp = x + 1 < G ? phi[e + 1] : 0.f, xm = x > 0 ? phi[e - 1] : 0.f;
+  const float yp = y + 1 < G ? phi[e + G] : 0.f, ym = y > 0 ? phi[e - G] : 0.f;
+  float ax = -((xp - xm) / two_h), ay = -((yp - ym) / two_h);
+  if (F4k) {
+    const float4 k = F4k[e];
+    ax += k.x;
+    ay += k.y;
+  }
+  F4[e] = make_float4(ax, ay, 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------------------------
+// a = a_grid (+ a_pair); momentum fix a -= sum(mm a) / max(sum(mm), 1e-9) (:612-614), then
+// a *= mask (:615). FP64 sums in a fixed order: MF_BLOCKS grid-strided partials, one fold.
+// ---------------------------------------------------------------------------------
+constexpr int MF_BLOCKS = 256;
+constexpr int MF_THREADS = 256;
+
+__global__ void __launch_bounds__(MF_THREADS) f2_momsum_kernel(const float *__restrict__ a1,
+                                                               const float *__restrict__ a2,
+                                                               const float *__restrict__ mass,
+                                                               const float *__restrict__ mask, int64_t n,
+                                                               double *__restrict__ part) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * MF_THREADS + threadIdx.x; i < n; i += (int64_t)MF_BLOCKS * MF_THREADS) {
+    const float mm = mass[i] * mask[i];
+    float ax = a1[2 * i], ay = a1[2 * i + 1];
+    if (a2) {
+      ax += a2[2 * i];
+      ay += a2[2 * i + 1];
+    }
+    s0 += (double)mm;
+    s1 += (double)(mm * ax);
+    s2 += (double)(mm * ay);
+  }
+  __shared__ double sh[3][MF_THREADS];
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = MF_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) part[threadIdx.x * MF_BLOCKS + blockIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(MF_BLOCKS) f2_momfold_kernel(double *__restrict__ part, float *__restrict__ mean) {
+  __shared__ double sh[3][MF_BLOCKS];
+  for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = part[c * MF_BLOCKS + threadIdx.x];
+  __syncthreads();
+  for (int w = MF_BLOCKS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double m = fmax(sh[0][0], 1e-9);
+    mean[0] = (float)(sh[1][0] / m);
+    mean[1] = (float)(sh[2][0] / m);
+  }
+}
+
+__global__ void f2_finish_kernel(const float *__restrict__ a1, const float *__restrict__ a2,
+                                 const float *__restrict__ mask, int64_t n, const float *__restrict__ mean,
+                                 float *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float ax = a1[2 * i], ay = a1[2 * i + 1];
+  if (a2) {
+    ax += a2[2 * i];
+    ay += a2[2 * i + 1];
+  }
+  if (mean) {
+    ax -= mean[0];
+    ay -= mean[1];
+  }
+  out[2 * i] = ax * mask[i];
+  out[2 * i + 1] = ay * mask[i];
+}
+
+// ---------------------------------------------------------------------------------
+// Velocity Verlet pieces of ScatterField._step (:677-688).
+// ---------------------------------------------------------------------------------
+__global__ void f2_drift_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
+                                const float *__restrict__ acc, int64_t n2, float dt, float hdt2,
+                                float *__restrict__ pos_out, float *__restrict__ vel_pred) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n2) return;
+  const float a = acc[e], v = vel[e];
+  pos_out[e] = (pos[e] + dt * v) + hdt2 * a;
+  vel_pred[e] = v + dt * a;
+}
+
+__global__ void f2_kick_kernel(const float *__restrict__ vel, const float *__restrict__ a0,
+                               const float *__restrict__ a1, int64_t n2, float hdt, float *__restrict__ vel_out,
+                               float *__restrict__ dv) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n2) return;
+  const float d = hdt * (a0[e] + a1[e]);
+  if (dv) dv[e] = d;
+  vel_out[e] = vel[e] + d;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t augur_field2d_scatter_work_bytes(int grid) {
+  return grid < 1 ? 0 : (size_t)3 * grid * grid * sizeof(unsigned long long) + 16;
+}
+
+int augur_field2d_scatter(const float *pos, const float *vel, const float *mass, const float *mask, int64_t n,
+                          int grid, double extent, double in_scale, float *out3, void *work, void *stream) {
+  if (grid < 2 || grid > 4096 || !(extent > 0.0) || !out3 || !work) return AUGUR_EINVAL;
+  if (n < 0 || (n > 0 && (!pos || !vel || !mass || !mask))) return AUGUR_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(work) & 7) != 0) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  const size_t GG = (size_t)grid * grid;
+  auto *acc = reinterpret_cast<unsigned long long *>(work);
+  auto *mx = reinterpret_cast<unsigned *>(acc + 3 * GG);
+  if (cudaMemsetAsync(work, 0, augur_field2d_scatter_work_bytes(grid), st) != cudaSuccess) return AUGUR_ECUDA;
+  ScatterArgs a;
+  a.G = grid;
+  a.E = (float)extent;
+  a.h = (float)(extent / grid);
+  a.scale = (float)(in_scale / ((double)a.h * (double)a.h));
+  if (n > 0) {
+    f2_absmax_kernel<<<nblocks(n, 256), 256, 0, st>>>(vel, mass, mask, n, a.scale, mx);
+    F2_LAUNCH_CHECK();
+    f2_scatter_kernel<<<nblocks(n, 256), 256, 0, st>>>(pos, vel, mass, mask, n, a, mx, acc);
+    F2_LAUNCH_CHECK();
+  }
+  f2_convert_kernel<<<nblocks(3 * (int64_t)GG, 256), 256, 0, st>>>(acc, mx, n > 0 ? n : 1, grid, out3);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int augur_field2d_inputs(const float *force4, const float *field, int cf, int grid, float *x, void *stream) {
+  if (!force4 || !x || grid < 2 || cf < 0 || cf > 8) return AUGUR_EINVAL;
+  f2_inputs_kernel<<<nblocks((int64_t)grid * grid, 256), 256, 0, S(stream)>>>(
+      reinterpret_cast<const float4 *>(force4), field, cf, grid, x);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int64_t augur_unet2d_param_count(int cin, int cout, int width, int levels) {
+  if (cin < 1 || cout < 1 || width < 1 || levels < 0) return -1;
+  const int64_t w = width;
+  int64_t n = w * cin * 9 + w;                       // inp
+  n += (levels + 1) * 2 * (w * w * 9 + w);           // enc blocks
+  n += levels * ((w * 2 * w * 9 + w) + (w * w * 9 + w));  // dec blocks
+  n += cout * w * 9 + cout;                          // out
+  return n;
+}
+
+size_t augur_unet2d_work_bytes(int grid, int width, int levels) {
+  if (grid < 1 || width < 1 || levels < 0) return 0;
+  size_t f = 2 * (size_t)width * grid * grid;  // two full-resolution temporaries
+  for (int l = 0; l <= levels; ++l) f += (size_t)width * (grid >> l) * (grid >> l);  // encoder outputs (skips)
+  return f * sizeof(float);
+}
+
+int augur_unet2d_forward(const float *params, int cin, int cout, int width, int levels, int grid, const float *x,
+                         float *y, void *work, size_t work_bytes, void *stream) {
+  if (!params || !x || !y || !work) return AUGUR_EINVAL;
+  if (cin < 1 || cout < 1 || cout > CO || width < 1 || width > CO || levels < 0 || levels > 10) return AUGUR_EINVAL;
+  if (grid < 1 || (grid % (1 << levels)) != 0) return AUGUR_EINVAL;
+  if (work_bytes < augur_unet2d_work_bytes(grid, width, levels)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  const size_t GG = (size_t)grid * grid;
+  float *T0 = reinterpret_cast<float *>(work), *T1 = T0 + width * GG;
+  float *Sk[11];
+  Sk[0] = T1 + width * GG;
+  for (int l = 1; l <= levels; ++l) Sk[l] = Sk[l - 1] + (size_t)width * (grid >> (l - 1)) * (grid >> (l - 1));
+  const float *p = params;
+  auto take = [&](int64_t k) {
+    const float *q = p;
+    p += k;
+    return q;
+  };
+  const int w = width;
+  int rc;
+  // h = gelu(inp(x)); enc[0]
+  const float *Wi = take((int64_t)w * cin * 9), *bi = take(w);
+  rc = conv3({x, nullptr, cin, 0, A_SAME}, Wi, bi, w, grid, 1, T0, st);
+  if (rc) return rc;
+  for (int l = 0; l <= levels; ++l) {
+    const int H = grid >> l;
+    const float *W1 = take((int64_t)w * w * 9), *b1 = take(w), *W2 = take((int64_t)w * w * 9), *b2 = take(w);
+    const ConvSrc s1 = l == 0 ? ConvSrc{T0, nullptr, w, 0, A_SAME} : ConvSrc{Sk[l - 1], nullptr, w, 0, A_POOL};
+    if ((rc = conv3(s1, W1, b1, w, H, 1, T1, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, W2, b2, w, H, 1, Sk[l], st))) return rc;
+  }
+  // decoder blocks are stored dec[0] .. dec[levels-1]; they run from the deepest level up
+  const float *dec0 = p;
+  const int64_t dec_block = ((int64_t)w * 2 * w * 9 + w) + ((int64_t)w * w * 9 + w);
+  const float *h = Sk[levels];
+  for (int l = levels - 1; l >= 0; --l) {
+    const int H = grid >> l;
+    const float *q = dec0 + l * dec_block;
+    const float *W1 = q, *b1 = W1 + (int64_t)w * 2 * w * 9, *W2 = b1 + w, *b2 = W2 + (int64_t)w * w * 9;
+    if ((rc = conv3({h, Sk[l], w, w, A_UP}, W1, b1, w, H, 1, T1, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, W2, b2, w, H, 1, T0, st))) return rc;
+    h = T0;
+  }
+  p = dec0 + levels * dec_block;
+  const float *Wo = take((int64_t)cout * w * 9), *bo = take(cout);
+  return conv3({h, nullptr, w, 0, A_SAME}, Wo, bo, cout, grid, 0, y, st);
+}
+
+int augur_field2d_accel(const float *phi, const float *force4_kernel, int grid, double h, float *force4_out,
+                        void *stream) {
+  if (!phi || !force4_out || grid < 2 || !(h > 0.0)) return AUGUR_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(force4_out) & 15) || (reinterpret_cast<uintptr_t>(force4_kernel) & 15))
+    return AUGUR_EINVAL;
+  f2_accel_kernel<<<nblocks((int64_t)grid * grid, 256), 256, 0, S(stream)>>>(
+      phi, reinterpret_cast<const float4 *>(force4_kernel), grid, (float)(2.0 * h),
+      reinterpret_cast<float4 *>(force4_out));
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+size_t augur_field2d_finish_work_bytes(void) { return (size_t)3 * MF_BLOCKS * sizeof(double) + 16; }
+
+int augur_field2d_finish(const float *acc_grid, const float *acc_pair, const float *mass, const float *mask,
+                         int64_t n, int momfix, float *acc_out, void *work, void *stream) {
+  if (n < 0 || (n > 0 && (!acc_grid || !mass || !mask || !acc_out))) return AUGUR_EINVAL;
+  if (momfix && (!work || (reinterpret_cast<uintptr_t>(work) & 7))) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  cudaStream_t st = S(stream);
+  float *mean = nullptr;
+  if (momfix) {
+    double *part = reinterpret_cast<double *>(work);
+    mean = reinterpret_cast<float *>(part + 3 * MF_BLOCKS);
+    f2_momsum_kernel<<<MF_BLOCKS, MF_THREADS, 0, st>>>(acc_grid, acc_pair, mass, mask, n, part);
+    F2_LAUNCH_CHECK();
+    f2_momfold_kernel<<<1, MF_BLOCKS, 0, st>>>(part, mean);
+    F2_LAUNCH_CHECK();
+  }
+  f2_finish_kernel<<<nblocks(n, 256), 256, 0, st>>>(acc_grid, acc_pair, mask, n, mean, acc_out);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int augur_field2d_drift(const float *pos, const float *vel, const float *acc, int64_t n, double dt, float *pos_out,
+                        float *vel_pred, void *stream) {
+  if (n < 0 || (n > 0 && (!pos || !vel || !acc || !pos_out || !vel_pred))) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  f2_drift_kernel<<<nblocks(2 * n, 256), 256, 0, S(stream)>>>(pos, vel, acc, 2 * n, (float)dt,
+                                                              (float)(0.5 * dt * dt), pos_out, vel_pred);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int augur_field2d_kick(const float *vel, const float *acc0, const float *acc1, int64_t n, double dt, float *vel_out,
+                       float *dv_out, void *stream) {
+  if (n < 0 || (n > 0 && (!vel || !acc0 || !acc1 || !vel_out))) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  f2_kick_kernel<<<nblocks(2 * n, 256), 256, 0, S(stream)>>>(vel, acc0, acc1, 2 * n, (float)(0.5 * dt), vel_out,
+                                                             dv_out);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+}  // extern "C"

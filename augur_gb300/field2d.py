@@ -1,0 +1,173 @@
+"""The reference's production 2D scatter-field model on the GPU, behind its call signature.
+
+Reference: ScatterField(grid=128, extent=64, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+potential=True, verlet=True) -- the configuration of its browser port (web/scatter/weights.json) --
+in scripts/scatter_field.py:
+    force(pos, vel, mass, mask, field) -> (acc, field)           :561-615
+    step(pos, vel, mass, mask, field)  -> (pos, vel, field, dv)  :668-688
+    init_field(B, device)                                        :557-559
+    load_state_dict(...) with its parameter names (ppmlp.*, kmlp.*, net.*)
+One force evaluation per scene: three-channel CIC scatter, the learned radial kernel's
+acceleration (FFT convolution on the isolated 2D plan), the 5-level U-Net on
+[scatter, kernel acceleration, previous potential], minus the potential's gradient plus the
+kernel acceleration gathered at the bodies, the k-nearest pair term, the momentum fix.
+Every stage is a kernel of libaugur_gb300 (include/augur_field2d.h, include/augur_pm.h); this
+module only sequences them and owns the buffers. Layouts are the reference's: pos/vel
+(B, N, 2) float32, mass/mask (B, N), field (B, 1, G, G).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from .pm import PMPlan, _stream
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+class UNetScatterField:
+    def __init__(self, grid: int = 128, extent: float = 64.0, dt: float = 0.1, width: int = 32, levels: int = 5,
+                 pp: float = 2.0, knn: int = 16, split: bool = True, momfix: bool = True, in_scale: float = 1.0,
+                 eps: float = 0.5, device=None):
+        self.lib = _lib.load()
+        self.grid, self.extent, self.h = int(grid), float(extent), float(extent) / int(grid)
+        self.dt, self.width, self.levels = float(dt), int(width), int(levels)
+        self.pp, self.knn, self.split, self.momfix = float(pp), int(knn), bool(split), bool(momfix)
+        self.in_scale, self.eps = float(in_scale), float(eps)
+        self.cf, self.cin = 1, 6  # potential field; inputs [m, m vx, m vy, k_x, k_y, field]
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if self.grid % (1 << self.levels):
+            raise ValueError(f"grid {grid} is not divisible by 2^{levels}")
+        self.n_net = int(self.lib.augur_unet2d_param_count(self.cin, self.cf, self.width, self.levels))
+        self.plan: PMPlan | None = None
+        self.net = self.kparams = self.pparams = None
+        G, dev = self.grid, self.device
+        self._x = torch.zeros((self.cin, G, G), device=dev)
+        self._f4a = torch.empty((G, G, 4), device=dev)
+        self._ws = torch.empty(int(self.lib.augur_field2d_scatter_work_bytes(G)), dtype=torch.uint8, device=dev)
+        self._wu_bytes = int(self.lib.augur_unet2d_work_bytes(G, self.width, self.levels))
+        self._wu = torch.empty(self._wu_bytes, dtype=torch.uint8, device=dev)
+        self._wf = torch.empty(int(self.lib.augur_field2d_finish_work_bytes()), dtype=torch.uint8, device=dev)
+
+    # ---- parameters ------------------------------------------------------------------------
+    def ppe(self) -> float:
+        return self.pp
+
+    def load_state_dict(self, sd: dict) -> None:
+        """Parameters under the reference's names (ppmlp.*, kmlp.*, net.*), any float dtype/device."""
+        t = {k: torch.as_tensor(v).to(self.device, torch.float32).reshape(-1) for k, v in sd.items()}
+
+        def mlp(prefix):
+            return torch.cat([t[f"{prefix}.{i}.{w}"] for i in (0, 2, 4) for w in ("weight", "bias")]).contiguous()
+
+        self.pparams = mlp("ppmlp") if self.pp > 0 else None
+        self.kparams = mlp("kmlp")
+        names = ["net.inp.weight", "net.inp.bias"]
+        for blk in [f"enc.{l}" for l in range(self.levels + 1)] + [f"dec.{l}" for l in range(self.levels)]:
+            names += [f"net.{blk}.{i}.{w}" for i in (0, 2) for w in ("weight", "bias")]
+        names += ["net.out.weight", "net.out.bias"]
+        self.net = torch.cat([t[k] for k in names]).contiguous()
+        if self.net.numel() != self.n_net:
+            raise ValueError(f"U-Net parameters: {self.net.numel()} values, expected {self.n_net}")
+        self._plan(1)
+
+    def _plan(self, n: int) -> PMPlan:
+        if self.plan is None or self.plan.max_bodies < n:
+            if self.plan is not None:
+                self.plan.close()
+            self.plan = PMPlan(2, self.grid, max(int(n), 1), "isolated", self.extent, eps=self.eps, device=self.device)
+            if self.kparams is not None:
+                self.plan.set_kernel_mlp(self.kparams, 2, split=self.split, split_radius=self.ppe())
+        return self.plan
+
+    def close(self) -> None:
+        if self.plan is not None:
+            self.plan.close()
+            self.plan = None
+
+    # ---- reference interface ---------------------------------------------------------------
+    def init_field(self, B: int, device=None, dtype=torch.float32):
+        return (torch.zeros(B, self.cf, self.grid, self.grid, device=device or self.device, dtype=dtype), None)
+
+    def _call(self, name, *args):
+        with torch.cuda.device(self.device):
+            rc = getattr(self.lib, name)(*args, _stream(self.device))
+        _lib.check(rc, name)
+
+    def scatter(self, pos, vel, mass, mask):
+        """(B, 3, G, G): [m, m vx, m vy] * in_scale / h^2 (ScatterField.scatter, :237-250)."""
+        B, N = pos.shape[:2]
+        out = torch.empty((B, 3, self.grid, self.grid), device=self.device)
+        for b in range(B):
+            self._call("augur_field2d_scatter", pos[b].data_ptr(), vel[b].data_ptr(), mass[b].data_ptr(),
+                       mask[b].data_ptr(), N, self.grid, self.extent, self.in_scale, out[b].data_ptr(),
+                       self._ws.data_ptr())
+        return out
+
+    def unet(self, x: torch.Tensor) -> torch.Tensor:
+        """The grid net alone: (B, 6, G, G) -> (B, 1, G, G)."""
+        x = x.to(self.device, torch.float32).contiguous()
+        y = torch.empty((x.shape[0], self.cf, self.grid, self.grid), device=self.device)
+        for b in range(x.shape[0]):
+            self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels,
+                       self.grid, x[b].data_ptr(), y[b].data_ptr(), self._wu.data_ptr(), self._wu_bytes)
+        return y
+
+    def _force1(self, pos, vel, mass, mask, field, acc_out, field_out):
+        n = pos.shape[0]
+        plan = self._plan(n)
+        x, G = self._x, self.grid
+        self._call("augur_field2d_scatter", pos.data_ptr(), vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), n,
+                   G, self.extent, self.in_scale, x.data_ptr(), self._ws.data_ptr())
+        f4k = plan.poisson(x[0])  # the learned kernel's acceleration (kernel_acc)
+        self._call("augur_field2d_inputs", f4k.data_ptr(), field.data_ptr(), self.cf, G, x.data_ptr())
+        self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels, G,
+                   x.data_ptr(), field_out.data_ptr(), self._wu.data_ptr(), self._wu_bytes)
+        self._call("augur_field2d_accel", field_out.data_ptr(), f4k.data_ptr(), G, self.h, self._f4a.data_ptr())
+        a_grid, _ = plan.gather(self._f4a, pos)
+        a_pair = None
+        if self.pparams is not None:
+            a_pair = plan.pair_acc(pos, mass, mask, ppe=self.ppe(), knn=self.knn, params=self.pparams, ncol=2)
+        self._call("augur_field2d_finish", a_grid.data_ptr(), _ptr(a_pair), mass.data_ptr(), mask.data_ptr(), n,
+                   int(self.momfix), acc_out.data_ptr(), self._wf.data_ptr())
+
+    def _check(self, pos, vel, mass, mask):
+        if self.net is None:
+            raise RuntimeError("load_state_dict first")
+        for name, t in (("pos", pos), ("vel", vel), ("mass", mass), ("mask", mask)):
+            if not (t.is_cuda and t.device == self.device and t.dtype == torch.float32 and t.is_contiguous()):
+                raise ValueError(f"{name} must be a contiguous float32 tensor on {self.device}")
+        if pos.dim() != 3 or pos.shape[2] != 2 or vel.shape != pos.shape or mass.shape != pos.shape[:2] \
+                or mask.shape != pos.shape[:2]:
+            raise ValueError("pos/vel must be (B, N, 2) and mass/mask (B, N)")
+
+    def force(self, pos, vel, mass, mask, field):
+        """(acc (B, N, 2), new field (B, 1, G, G)) -- ScatterField.force (:561-615)."""
+        self._check(pos, vel, mass, mask)
+        B = pos.shape[0]
+        acc = torch.empty_like(pos)
+        out = torch.empty((B, self.cf, self.grid, self.grid), device=self.device)
+        field = field.to(self.device, torch.float32).contiguous()
+        for b in range(B):
+            self._force1(pos[b], vel[b], mass[b], mask[b], field[b], acc[b], out[b])
+        return acc, out
+
+    def step(self, pos, vel, mass, mask, field):
+        """One velocity-Verlet step, ScatterField._step (:677-688): field = (potential, a_prev)."""
+        self._check(pos, vel, mass, mask)
+        f, a_prev = field
+        if a_prev is None:
+            a_prev, f = self.force(pos, vel, mass, mask, f)
+        n = pos.numel() // 2
+        pos_new, vel_pred = torch.empty_like(pos), torch.empty_like(vel)
+        self._call("augur_field2d_drift", pos.data_ptr(), vel.data_ptr(), a_prev.data_ptr(), n, self.dt,
+                   pos_new.data_ptr(), vel_pred.data_ptr())
+        a_new, f = self.force(pos_new, vel_pred, mass, mask, f)
+        vel_new, dv = torch.empty_like(vel), torch.empty_like(vel)
+        self._call("augur_field2d_kick", vel.data_ptr(), a_prev.data_ptr(), a_new.data_ptr(), n, self.dt,
+                   vel_new.data_ptr(), dv.data_ptr())
+        return pos_new, vel_new, (f, a_new), dv

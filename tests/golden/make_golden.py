@@ -205,8 +205,73 @@ def pair_acc_cases():
     np.savez_compressed(OUT / "pair_acc.npz", **out)
 
 
+def field2d_cases():
+    """The production 2D model of the reference's browser port (web/scatter/weights.json config:
+    ScatterField(grid=128, extent=64, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+    potential=True, verlet=True), levels 5, width 32) in float64, as
+    scripts/export_web_testvectors_scatter.py runs it, with seeded weights rounded to float16
+    (so float32 holds them exactly; the zero-initialised output layers get seeded values):
+    the U-Net alone on a seeded input, the three-channel scatter, and free Verlet rollouts of
+    the exporter's scenes (30 and 100 bodies) with the recurrent potential."""
+    torch.manual_seed(4738)
+    m = sf.ScatterField(grid=128, extent=64.0, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+                        potential=True, verlet=True)
+    g = torch.Generator().manual_seed(9300)
+    with torch.no_grad():
+        m.ppmlp[-1].weight.copy_(torch.randn(m.ppmlp[-1].weight.shape, generator=g) * 0.3)
+        m.ppmlp[-1].bias.copy_(torch.randn(1, generator=g) * 0.3)
+        m.kmlp[-1].weight.copy_(torch.randn(m.kmlp[-1].weight.shape, generator=g) * 0.3)
+        m.kmlp[-1].bias.copy_(torch.randn(1, generator=g) * 0.3)
+        m.net.out.weight.copy_(torch.randn(m.net.out.weight.shape, generator=g) * 1.0)
+        m.net.out.bias.copy_(torch.randn(1, generator=g) * 0.05)
+        for t in m.parameters():
+            t.copy_(t.half().float())
+    m32 = sf.ScatterField(grid=128, extent=64.0, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+                          potential=True, verlet=True).eval()  # the reference's own float32 path, same weights
+    m32.load_state_dict(m.state_dict())
+    m = m.double().eval()
+    names = [k for k, _ in m.named_parameters()]
+    out = {"names": np.array(names), "steps": np.int32(4)}
+    for k, t in m.named_parameters():
+        out["w_" + k] = t.detach().numpy().astype(np.float16)
+    G = 128
+    x = torch.randn(1, 6, G, G, generator=g, dtype=torch.float64)
+    x[:, 0] = torch.rand(1, G, G, generator=g, dtype=torch.float64) * (torch.rand(1, G, G, generator=g) < 0.05)
+    x = x.half().double()
+    with torch.no_grad():
+        out["unet_x"] = x[0].numpy().astype(np.float16)
+        out["unet_y"] = m.net(x)[0].numpy().astype(np.float32)
+    rng = np.random.default_rng(4738)
+    for n in (30, 100):
+        f, fv = (n / 8) ** 0.5, (n / 8) ** 0.25
+        p0 = rng.uniform(-5.0 * f, 5.0 * f, (n, 2)).astype(np.float32)
+        v0 = rng.normal(0.0, 0.5 * fv, (n, 2))
+        v0 = (v0 - v0.mean(0)).astype(np.float32)
+        pos, vel = torch.tensor(p0, dtype=torch.float64)[None], torch.tensor(v0, dtype=torch.float64)[None]
+        mass, mask = torch.ones(1, n, dtype=torch.float64), torch.ones(1, n, dtype=torch.float64)
+        k = f"n{n}"
+        out[k + "_pos0"], out[k + "_vel0"] = p0, v0
+        with torch.no_grad():
+            out[k + "_scatter"] = m.scatter(pos, vel, mass, mask)[0].numpy().astype(np.float32)
+            field = m.init_field(1, "cpu", torch.float64)
+            a0, f1 = m.force(pos, vel, mass, mask, field[0])
+            out[k + "_acc0"], out[k + "_field1"] = a0[0].numpy(), f1[0, 0].numpy().astype(np.float32)
+            p32, v32, o32 = pos.float(), vel.float(), torch.ones(1, n)
+            out[k + "_scatter32"] = m32.scatter(p32, v32, o32, o32)[0].numpy()
+            out[k + "_acc0_32"] = m32.force(p32, v32, o32, o32, m32.init_field(1, "cpu")[0])[0][0].numpy()
+            ps, vs = [], []
+            for _ in range(4):
+                pos, vel, field, _ = m.step(pos, vel, mass, mask, field)
+                ps.append(pos[0].numpy())
+                vs.append(vel[0].numpy())
+            out[k + "_pos"], out[k + "_vel"] = np.stack(ps), np.stack(vs)
+            out[k + "_field"] = field[0][0, 0].numpy().astype(np.float32)
+    np.savez_compressed(OUT / "field2d.npz", **out)
+
+
 CASES = {"cell_index": cell_index_cases, "scatter_gather": scatter_gather_cases, "pm_acc": pm_acc_cases,
-         "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases, "pair_acc": pair_acc_cases}
+         "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases, "pair_acc": pair_acc_cases,
+         "field2d": field2d_cases}
 
 if __name__ == "__main__":
     for name in (sys.argv[1:] or list(CASES)):

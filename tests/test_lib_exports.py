@@ -4,6 +4,7 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -69,3 +70,13 @@ def test_product_rejects_cpu_tensors():
 
     with pytest.raises(ValueError, match="CUDA"):
         _need(torch.zeros(4, 3), "pos")
+
+
+def test_unet2d_param_count_matches_reference_layout(golden):
+    """augur_unet2d_param_count equals the reference UNet's parameter count (levels 5, width 32,
+    6 inputs, 1 output: the net.* tensors of tests/golden/field2d.npz)."""
+    from augur_gb300 import _lib
+
+    g = golden["field2d"]
+    n = sum(int(np.prod(g["w_" + k].shape)) for k in g["names"] if k.startswith("net."))
+    assert _lib.load().augur_unet2d_param_count(6, 1, 32, 5) == n
