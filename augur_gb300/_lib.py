@@ -55,6 +55,8 @@ SIGNATURES = {
     "augur_field2d_scatter": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _f64, _f64, _vp, _vp, _vp]),
     "augur_field2d_inputs": (_i32, [_vp, _vp, _i32, _i32, _vp, _vp]),
     "augur_unet2d_param_count": (_i64, [_i32, _i32, _i32, _i32]),
+    "augur_unet2d_prepared_count": (_i64, [_i32, _i32, _i32, _i32]),
+    "augur_unet2d_prepare": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp]),
     "augur_unet2d_work_bytes": (C.c_size_t, [_i32, _i32, _i32]),
     "augur_unet2d_forward": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, C.c_size_t, _vp]),
     "augur_field2d_accel": (_i32, [_vp, _vp, _i32, _f64, _vp, _vp]),

@@ -9,6 +9,7 @@
 // or nearest upsampling by 2 concatenated with the skip tensor, so pooling, upsampling and
 // concatenation never materialise. Layout: channels-first (C, H, W) per scene, as torch's
 // NCHW with B = 1.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -144,16 +145,19 @@ __global__ void f2_inputs_kernel(const float4 *__restrict__ F4k, const float *__
 
 // ---------------------------------------------------------------------------------
 // 3x3 convolution, zero padding 1, fp32. One CTA = an 8 x 8 output tile x all output
-// channels (<= 32): thread (pixel, group of 8 output channels). Input channels in chunks of
-// 8, staged with their halo in shared memory by a loader that applies the source mode:
+// channels (<= 32): thread (pixel, group of 8 output channels). The CTA stages the layer's
+// whole weight block (prepared layout [in][tap][32 outputs], float4 copies) and its input tile
+// with halo for every input channel in shared memory, all loads in flight at once, then
+// accumulates without further barriers. The input loader applies the source mode:
 //   A_SAME: srcA at the output resolution; A_POOL: 2x2 average of srcA at twice the
 //   resolution (avg_pool2d(2)); A_UP: srcA at half the resolution, nearest (interpolate x2).
 // Channels [CA, CA + CB) come from srcB at the output resolution (the U-Net's skip).
 // ---------------------------------------------------------------------------------
 enum { A_SAME = 0, A_POOL = 1, A_UP = 2 };
 constexpr int CT = 8;   // output tile side
-constexpr int KC = 8;   // input channels per chunk
-constexpr int CO = 32;  // output channels per CTA (max)
+constexpr int CTH = CT + 2;
+constexpr int CO = 32;  // output channels per CTA (max); prepared weights are padded to it
+constexpr int CIN_MAX = 64;
 
 struct ConvSrc {
   const float *a;
@@ -161,73 +165,94 @@ struct ConvSrc {
   int ca, cb, mode;
 };
 
-template <int MODE>
-__global__ void __launch_bounds__(256) f2_conv3_kernel(ConvSrc src, const float *__restrict__ W,
-                                                       const float *__restrict__ bias, int cout, int H,
-                                                       int act, float *__restrict__ out) {
-  __shared__ float sx[KC][CT + 2][CT + 2];
-  __shared__ __align__(16) float sw[KC][9][CO];
-  const int tid = threadIdx.x;
-  const int p = tid & 63, cg = tid >> 6;
-  const int px = p & 7, py = p >> 3;
-  const int x0 = blockIdx.x * CT, y0 = blockIdx.y * CT;
+size_t conv_smem(int cin) { return (size_t)cin * 9 * CO * sizeof(float) + (size_t)cin * CTH * CTH * sizeof(float); }
+
+// KS threads share one (pixel, 8 outputs): each sums a contiguous range of the input channels,
+// then the partial sums are added in ks order through shared memory (deterministic).
+template <int MODE, int KS>
+__global__ void __launch_bounds__(256 * KS) f2_conv3_kernel(ConvSrc src, const float *__restrict__ Wp, int cout,
+                                                            int H, int act, float *__restrict__ out) {
+  extern __shared__ __align__(16) float smem[];
   const int cin = src.ca + src.cb;
+  float *sw = smem;                         // [cin][9][CO]
+  float *sx = smem + (size_t)cin * 9 * CO;  // [cin][CTH][CTH]
+  const int tid = threadIdx.x;
+  constexpr int NT = 256 * KS;
+  {
+    const float4 *w4 = reinterpret_cast<const float4 *>(Wp);
+    float4 *s4 = reinterpret_cast<float4 *>(sw);
+    const int n4 = cin * 9 * CO / 4;
+#pragma unroll 4
+    for (int e = tid; e < n4; e += NT) s4[e] = w4[e];
+  }
+  const int x0 = blockIdx.x * CT, y0 = blockIdx.y * CT;
+#pragma unroll 4
+  for (int e = tid; e < cin * CTH * CTH; e += NT) {
+    const int ch = e / (CTH * CTH), r = e % (CTH * CTH);
+    const int yy = y0 + r / CTH - 1, xx = x0 + r % CTH - 1;
+    float v = 0.f;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < H) {
+      if (ch < src.ca) {
+        if (MODE == A_SAME) {
+          v = src.a[((size_t)ch * H + yy) * H + xx];
+        } else if (MODE == A_POOL) {
+          const int H2 = 2 * H;
+          const float *q = src.a + ((size_t)ch * H2 + 2 * yy) * H2 + 2 * xx;
+          v = (((q[0] + q[1]) + q[H2]) + q[H2 + 1]) * 0.25f;
+        } else {
+          const int Hh = H >> 1;
+          v = src.a[((size_t)ch * Hh + (yy >> 1)) * Hh + (xx >> 1)];
+        }
+      } else {
+        v = src.b[((size_t)(ch - src.ca) * H + yy) * H + xx];
+      }
+    }
+    sx[e] = v;
+  }
+  __syncthreads();
+  const int ks = tid >> 8, lt = tid & 255;
+  const int p = lt & 63, cg = lt >> 6;
+  const int px = p & 7, py = p >> 3;
+  const int per = (cin + KS - 1) / KS;
+  const int c_lo = ks * per, c_hi = min(cin, c_lo + per);
   float acc[8];
 #pragma unroll
   for (int o = 0; o < 8; ++o) acc[o] = 0.f;
-  for (int c0 = 0; c0 < cin; c0 += KC) {
-    // input chunk with halo
-    for (int e = tid; e < KC * (CT + 2) * (CT + 2); e += 256) {
-      const int c = e / ((CT + 2) * (CT + 2)), r = e % ((CT + 2) * (CT + 2));
-      const int yy = y0 + r / (CT + 2) - 1, xx = x0 + r % (CT + 2) - 1;
-      const int ch = c0 + c;
-      float v = 0.f;
-      if (ch < cin && yy >= 0 && yy < H && xx >= 0 && xx < H) {
-        if (ch < src.ca) {
-          if (MODE == A_SAME) {
-            v = src.a[((size_t)ch * H + yy) * H + xx];
-          } else if (MODE == A_POOL) {
-            const int H2 = 2 * H;
-            const float *q = src.a + ((size_t)ch * H2 + 2 * yy) * H2 + 2 * xx;
-            v = (((q[0] + q[1]) + q[H2]) + q[H2 + 1]) * 0.25f;
-          } else {
-            const int Hh = H >> 1;
-            v = src.a[((size_t)ch * Hh + (yy >> 1)) * Hh + (xx >> 1)];
-          }
-        } else {
-          v = src.b[((size_t)(ch - src.ca) * H + yy) * H + xx];
-        }
-      }
-      sx[c][r / (CT + 2)][r % (CT + 2)] = v;
+#pragma unroll 2
+  for (int c = c_lo; c < c_hi; ++c) {
+    const float *xc = sx + c * CTH * CTH + py * CTH + px;
+    const float *wc = sw + c * 9 * CO + cg * 8;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const float v = xc[(t / 3) * CTH + t % 3];
+      const float4 w0 = *reinterpret_cast<const float4 *>(wc + t * CO);
+      const float4 w1 = *reinterpret_cast<const float4 *>(wc + t * CO + 4);
+      acc[0] += w0.x * v;
+      acc[1] += w0.y * v;
+      acc[2] += w0.z * v;
+      acc[3] += w0.w * v;
+      acc[4] += w1.x * v;
+      acc[5] += w1.y * v;
+      acc[6] += w1.z * v;
+      acc[7] += w1.w * v;
     }
-    // weights W[o][ch][tap] -> sw[c][tap][o]
-    for (int e = tid; e < KC * 9 * CO; e += 256) {
-      const int o = e % CO, t = (e / CO) % 9, c = e / (9 * CO);
-      const int ch = c0 + c;
-      sw[c][t][o] = (o < cout && ch < cin) ? W[((size_t)o * cin + ch) * 9 + t] : 0.f;
+  }
+  if (KS > 1) {
+    __syncthreads();  // the weight region is free: partial sums [ks][o][lt]
+    if (ks > 0) {
+#pragma unroll
+      for (int o = 0; o < 8; ++o) sw[((ks - 1) * 8 + o) * 256 + lt] = acc[o];
     }
     __syncthreads();
+    if (ks > 0) return;
 #pragma unroll
-    for (int c = 0; c < KC; ++c) {
+    for (int k = 1; k < KS; ++k)
 #pragma unroll
-      for (int t = 0; t < 9; ++t) {
-        const float v = sx[c][py + t / 3][px + t % 3];
-        const float4 w0 = *reinterpret_cast<const float4 *>(&sw[c][t][cg * 8]);
-        const float4 w1 = *reinterpret_cast<const float4 *>(&sw[c][t][cg * 8 + 4]);
-        acc[0] += w0.x * v;
-        acc[1] += w0.y * v;
-        acc[2] += w0.z * v;
-        acc[3] += w0.w * v;
-        acc[4] += w1.x * v;
-        acc[5] += w1.y * v;
-        acc[6] += w1.z * v;
-        acc[7] += w1.w * v;
-      }
-    }
-    __syncthreads();
+      for (int o = 0; o < 8; ++o) acc[o] += sw[((k - 1) * 8 + o) * 256 + lt];
   }
   const int x = x0 + px, y = y0 + py;
   if (x >= H || y >= H) return;
+  const float *bias = Wp + (size_t)cin * 9 * CO;
 #pragma unroll
   for (int o = 0; o < 8; ++o) {
     const int oc = cg * 8 + o;
@@ -238,17 +263,67 @@ __global__ void __launch_bounds__(256) f2_conv3_kernel(ConvSrc src, const float 
   }
 }
 
-int conv3(const ConvSrc &s, const float *W, const float *b, int cout, int H, int act, float *out, cudaStream_t st) {
-  if (cout < 1 || cout > CO) return AUGUR_EINVAL;
+// torch layout W (cout, cin, 3, 3), b (cout) -> Wp [cin][9][CO] (zero-padded outputs), then CO biases
+__global__ void f2_prep_kernel(const float *__restrict__ W, const float *__restrict__ b, int cout, int cin,
+                               float *__restrict__ Wp) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nw = cin * 9 * CO;
+  if (e < nw) {
+    const int o = e % CO, t = (e / CO) % 9, c = e / (9 * CO);
+    Wp[e] = o < cout ? W[((size_t)o * cin + c) * 9 + t] : 0.f;
+  } else if (e < nw + CO) {
+    const int o = e - nw;
+    Wp[e] = o < cout ? b[o] : 0.f;
+  }
+}
+
+template <int KS>
+int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, cudaStream_t st) {
+  static bool raised = false;  // opt in to the large shared-memory carve-out once per process
+  if (!raised) {
+    const int lim = (int)conv_smem(CIN_MAX);
+    if (cudaFuncSetAttribute(f2_conv3_kernel<A_SAME, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) ||
+        cudaFuncSetAttribute(f2_conv3_kernel<A_POOL, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) ||
+        cudaFuncSetAttribute(f2_conv3_kernel<A_UP, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))
+      return AUGUR_ECUDA;
+    raised = true;
+  }
   dim3 grid((H + CT - 1) / CT, (H + CT - 1) / CT);
+  // the partial-sum exchange reuses the staging region: (KS - 1) x 8 x 256 floats
+  const size_t sm = std::max(conv_smem(s.ca + s.cb), (size_t)(KS - 1) * 8 * 256 * sizeof(float));
   switch (s.mode) {
-    case A_SAME: f2_conv3_kernel<A_SAME><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
-    case A_POOL: f2_conv3_kernel<A_POOL><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
-    default: f2_conv3_kernel<A_UP><<<grid, 256, 0, st>>>(s, W, b, cout, H, act, out); break;
+    case A_SAME: f2_conv3_kernel<A_SAME, KS><<<grid, 256 * KS, sm, st>>>(s, Wp, cout, H, act, out); break;
+    case A_POOL: f2_conv3_kernel<A_POOL, KS><<<grid, 256 * KS, sm, st>>>(s, Wp, cout, H, act, out); break;
+    default: f2_conv3_kernel<A_UP, KS><<<grid, 256 * KS, sm, st>>>(s, Wp, cout, H, act, out); break;
   }
   F2_LAUNCH_CHECK();
   return AUGUR_OK;
 }
+
+// Input channels are split over 2 threads per output at 64^2 and above (two CTAs of 512 per
+// SM), over 4 below (the few CTAs of the coarse levels get 32 warps each).
+int conv3(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, cudaStream_t st) {
+  const int cin = s.ca + s.cb;
+  if (cout < 1 || cout > CO || cin < 1 || cin > CIN_MAX) return AUGUR_EINVAL;
+  return H >= 64 ? conv3_ks<2>(s, Wp, cout, H, act, out, st) : conv3_ks<4>(s, Wp, cout, H, act, out, st);
+}
+
+// The U-Net's convolutions in parameter order: (cin, cout) of each.
+int unet_layers(int cin, int cout, int width, int levels, int *ci, int *co) {
+  int k = 0;
+  ci[k] = cin, co[k++] = width;
+  for (int l = 0; l <= levels; ++l) {
+    ci[k] = width, co[k++] = width;
+    ci[k] = width, co[k++] = width;
+  }
+  for (int l = 0; l < levels; ++l) {
+    ci[k] = 2 * width, co[k++] = width;
+    ci[k] = width, co[k++] = width;
+  }
+  ci[k] = width, co[k++] = cout;
+  return k;
+}
+constexpr int UNET_MAX_LAYERS = 4 * 11 + 2;
 
 // ---------------------------------------------------------------------------------
 // Grid acceleration -grad(phi) (central differences, zero padding; ScatterField.neg_grad,
@@ -407,13 +482,41 @@ int augur_field2d_inputs(const float *force4, const float *field, int cf, int gr
 }
 
 int64_t augur_unet2d_param_count(int cin, int cout, int width, int levels) {
-  if (cin < 1 || cout < 1 || width < 1 || levels < 0) return -1;
-  const int64_t w = width;
-  int64_t n = w * cin * 9 + w;                       // inp
-  n += (levels + 1) * 2 * (w * w * 9 + w);           // enc blocks
-  n += levels * ((w * 2 * w * 9 + w) + (w * w * 9 + w));  // dec blocks
-  n += cout * w * 9 + cout;                          // out
+  if (cin < 1 || cout < 1 || width < 1 || levels < 0 || levels > 10) return -1;
+  int ci[UNET_MAX_LAYERS], co[UNET_MAX_LAYERS];
+  const int nl = unet_layers(cin, cout, width, levels, ci, co);
+  int64_t n = 0;
+  for (int k = 0; k < nl; ++k) n += (int64_t)co[k] * ci[k] * 9 + co[k];
   return n;
+}
+
+int64_t augur_unet2d_prepared_count(int cin, int cout, int width, int levels) {
+  if (cin < 1 || cout < 1 || width < 1 || levels < 0 || levels > 10) return -1;
+  int ci[UNET_MAX_LAYERS], co[UNET_MAX_LAYERS];
+  const int nl = unet_layers(cin, cout, width, levels, ci, co);
+  int64_t n = 0;
+  for (int k = 0; k < nl; ++k) n += (int64_t)ci[k] * 9 * CO + CO;
+  return n;
+}
+
+int augur_unet2d_prepare(const float *params, int cin, int cout, int width, int levels, float *prepared,
+                         void *stream) {
+  if (!params || !prepared || cin < 1 || cin > CIN_MAX || cout < 1 || cout > CO || width < 1 || width > CO ||
+      2 * width > CIN_MAX || levels < 0 || levels > 10)
+    return AUGUR_EINVAL;
+  if (reinterpret_cast<uintptr_t>(prepared) & 15) return AUGUR_EINVAL;
+  int ci[UNET_MAX_LAYERS], co[UNET_MAX_LAYERS];
+  const int nl = unet_layers(cin, cout, width, levels, ci, co);
+  const float *p = params;
+  float *q = prepared;
+  for (int k = 0; k < nl; ++k) {
+    const int64_t nw = (int64_t)ci[k] * 9 * CO + CO;
+    f2_prep_kernel<<<nblocks(nw, 256), 256, 0, S(stream)>>>(p, p + (int64_t)co[k] * ci[k] * 9, co[k], ci[k], q);
+    F2_LAUNCH_CHECK();
+    p += (int64_t)co[k] * ci[k] * 9 + co[k];
+    q += nw;
+  }
+  return AUGUR_OK;
 }
 
 size_t augur_unet2d_work_bytes(int grid, int width, int levels) {
@@ -423,52 +526,49 @@ size_t augur_unet2d_work_bytes(int grid, int width, int levels) {
   return f * sizeof(float);
 }
 
-int augur_unet2d_forward(const float *params, int cin, int cout, int width, int levels, int grid, const float *x,
+int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, int levels, int grid, const float *x,
                          float *y, void *work, size_t work_bytes, void *stream) {
-  if (!params || !x || !y || !work) return AUGUR_EINVAL;
-  if (cin < 1 || cout < 1 || cout > CO || width < 1 || width > CO || levels < 0 || levels > 10) return AUGUR_EINVAL;
+  if (!prepared || !x || !y || !work) return AUGUR_EINVAL;
+  if (cin < 1 || cin > CIN_MAX || cout < 1 || cout > CO || width < 1 || width > CO || 2 * width > CIN_MAX ||
+      levels < 0 || levels > 10)
+    return AUGUR_EINVAL;
   if (grid < 1 || (grid % (1 << levels)) != 0) return AUGUR_EINVAL;
   if (work_bytes < augur_unet2d_work_bytes(grid, width, levels)) return AUGUR_EINVAL;
+  if (reinterpret_cast<uintptr_t>(prepared) & 15) return AUGUR_EINVAL;
   cudaStream_t st = S(stream);
   const size_t GG = (size_t)grid * grid;
   float *T0 = reinterpret_cast<float *>(work), *T1 = T0 + width * GG;
   float *Sk[11];
   Sk[0] = T1 + width * GG;
   for (int l = 1; l <= levels; ++l) Sk[l] = Sk[l - 1] + (size_t)width * (grid >> (l - 1)) * (grid >> (l - 1));
-  const float *p = params;
-  auto take = [&](int64_t k) {
-    const float *q = p;
-    p += k;
-    return q;
-  };
+  int ci[UNET_MAX_LAYERS], co[UNET_MAX_LAYERS];
+  const int nl = unet_layers(cin, cout, width, levels, ci, co);
+  const float *Lw[UNET_MAX_LAYERS];
+  const float *q = prepared;
+  for (int k = 0; k < nl; ++k) {
+    Lw[k] = q;
+    q += (int64_t)ci[k] * 9 * CO + CO;
+  }
   const int w = width;
-  int rc;
-  // h = gelu(inp(x)); enc[0]
-  const float *Wi = take((int64_t)w * cin * 9), *bi = take(w);
-  rc = conv3({x, nullptr, cin, 0, A_SAME}, Wi, bi, w, grid, 1, T0, st);
-  if (rc) return rc;
+  int rc, k = 0;
+  // h = gelu(inp(x)); encoder blocks at grid / 2^l, each after avg_pool2d(2) of the previous
+  if ((rc = conv3({x, nullptr, cin, 0, A_SAME}, Lw[k++], w, grid, 1, T0, st))) return rc;
   for (int l = 0; l <= levels; ++l) {
     const int H = grid >> l;
-    const float *W1 = take((int64_t)w * w * 9), *b1 = take(w), *W2 = take((int64_t)w * w * 9), *b2 = take(w);
     const ConvSrc s1 = l == 0 ? ConvSrc{T0, nullptr, w, 0, A_SAME} : ConvSrc{Sk[l - 1], nullptr, w, 0, A_POOL};
-    if ((rc = conv3(s1, W1, b1, w, H, 1, T1, st))) return rc;
-    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, W2, b2, w, H, 1, Sk[l], st))) return rc;
+    if ((rc = conv3(s1, Lw[k++], w, H, 1, T1, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[k++], w, H, 1, Sk[l], st))) return rc;
   }
   // decoder blocks are stored dec[0] .. dec[levels-1]; they run from the deepest level up
-  const float *dec0 = p;
-  const int64_t dec_block = ((int64_t)w * 2 * w * 9 + w) + ((int64_t)w * w * 9 + w);
+  const int kdec = k;
   const float *h = Sk[levels];
   for (int l = levels - 1; l >= 0; --l) {
     const int H = grid >> l;
-    const float *q = dec0 + l * dec_block;
-    const float *W1 = q, *b1 = W1 + (int64_t)w * 2 * w * 9, *W2 = b1 + w, *b2 = W2 + (int64_t)w * w * 9;
-    if ((rc = conv3({h, Sk[l], w, w, A_UP}, W1, b1, w, H, 1, T1, st))) return rc;
-    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, W2, b2, w, H, 1, T0, st))) return rc;
+    if ((rc = conv3({h, Sk[l], w, w, A_UP}, Lw[kdec + 2 * l], w, H, 1, T1, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * l + 1], w, H, 1, T0, st))) return rc;
     h = T0;
   }
-  p = dec0 + levels * dec_block;
-  const float *Wo = take((int64_t)cout * w * 9), *bo = take(cout);
-  return conv3({h, nullptr, w, 0, A_SAME}, Wo, bo, cout, grid, 0, y, st);
+  return conv3({h, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * levels], cout, grid, 0, y, st);
 }
 
 int augur_field2d_accel(const float *phi, const float *force4_kernel, int grid, double h, float *force4_out,

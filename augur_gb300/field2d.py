@@ -17,7 +17,6 @@ module only sequences them and owns the buffers. Layouts are the reference's: po
 """
 from __future__ import annotations
 
-import ctypes as C
 
 import torch
 
@@ -70,9 +69,14 @@ class UNetScatterField:
         for blk in [f"enc.{l}" for l in range(self.levels + 1)] + [f"dec.{l}" for l in range(self.levels)]:
             names += [f"net.{blk}.{i}.{w}" for i in (0, 2) for w in ("weight", "bias")]
         names += ["net.out.weight", "net.out.bias"]
-        self.net = torch.cat([t[k] for k in names]).contiguous()
-        if self.net.numel() != self.n_net:
-            raise ValueError(f"U-Net parameters: {self.net.numel()} values, expected {self.n_net}")
+        net = torch.cat([t[k] for k in names]).contiguous()
+        if net.numel() != self.n_net:
+            raise ValueError(f"U-Net parameters: {net.numel()} values, expected {self.n_net}")
+        self.net = torch.empty(int(self.lib.augur_unet2d_prepared_count(self.cin, self.cf, self.width, self.levels)),
+                               device=self.device)
+        self._call("augur_unet2d_prepare", net.data_ptr(), self.cin, self.cf, self.width, self.levels,
+                   self.net.data_ptr())
+        torch.cuda.synchronize(self.device)
         self._plan(1)
 
     def _plan(self, n: int) -> PMPlan:

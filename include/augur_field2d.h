@@ -54,12 +54,18 @@ int augur_field2d_inputs(const float *force4, const float *field, int cf, int gr
  * out = Conv(width, cout), no activation. 3x3 convolutions, zero padding 1, exact (erf) GELU.
  * params: fp32 device array in torch's parameter order (inp.weight, inp.bias, enc.0.0.weight,
  * enc.0.0.bias, enc.0.2.weight, enc.0.2.bias, ..., dec.*, out.weight, out.bias), each conv weight
- * (out, in, 3, 3); augur_unet2d_param_count gives its length. x (cin, G, G) -> y (cout, G, G).
- * Needs width <= 32, cout <= 32 and grid divisible by 2^levels; work: augur_unet2d_work_bytes.
+ * (out, in, 3, 3); augur_unet2d_param_count gives its length. augur_unet2d_prepare rewrites it
+ * once into the kernels' layout (per convolution [in][tap][32 outputs, zero-padded] then 32
+ * biases; augur_unet2d_prepared_count floats, 16-byte aligned), which augur_unet2d_forward reads.
+ * x (cin, G, G) -> y (cout, G, G). Needs cin <= 64, width <= 32, cout <= 32 and grid divisible
+ * by 2^levels; work: augur_unet2d_work_bytes(grid, width, levels) bytes.
  */
 int64_t augur_unet2d_param_count(int cin, int cout, int width, int levels);
+int64_t augur_unet2d_prepared_count(int cin, int cout, int width, int levels);
+int augur_unet2d_prepare(const float *params, int cin, int cout, int width, int levels,
+                         float *prepared, void *stream);
 size_t augur_unet2d_work_bytes(int grid, int width, int levels);
-int augur_unet2d_forward(const float *params, int cin, int cout, int width, int levels, int grid,
+int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, int levels, int grid,
                          const float *x, float *y, void *work, size_t work_bytes, void *stream);
 
 /*
