@@ -6,6 +6,6 @@ package: calls on CPU tensors raise.
 """
 from .pm import PMPlan, direct_sum_fp64, energy_fp64
 from .scatter_field import ScatterField, pm_acc
-from .field2d import UNetScatterField
+from .field2d import ChunkedTick2D, UNetScatterField
 
-__all__ = ["PMPlan", "ScatterField", "UNetScatterField", "pm_acc", "direct_sum_fp64", "energy_fp64"]
+__all__ = ["PMPlan", "ScatterField", "UNetScatterField", "ChunkedTick2D", "pm_acc", "direct_sum_fp64", "energy_fp64"]

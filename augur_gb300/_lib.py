@@ -64,6 +64,13 @@ SIGNATURES = {
     "augur_field2d_finish": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
     "augur_field2d_drift": (_i32, [_vp, _vp, _vp, _i64, _f64, _vp, _vp, _vp]),
     "augur_field2d_kick": (_i32, [_vp, _vp, _vp, _i64, _f64, _vp, _vp, _vp]),
+    "augur_tick2d_work_bytes": (C.c_size_t, [_i32]),
+    "augur_tick2d_drift_scatter": (_i32, [_vp, _vp, _i64, _i32, _i32, _f64, _f64, _f64, _i32, _i32, _f64, _f64, _vp,
+                                          _vp, _vp]),
+    "augur_tick2d_drift": (_i32, [_vp, _vp, _i64, _i32, _i32, _f64, _f64, _f64, _vp]),
+    "augur_tick2d_mean_acc": (_i32, [_vp, _vp, _i32, _f64, _i64, _vp, _vp, _vp]),
+    "augur_tick2d_gather_kick": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _f64, _f64, _vp, _i32, _f64, _i32, _f64,
+                                        _f64, _vp]),
     # include/augur_cnn.h
     "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp, _vp]),
     "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),

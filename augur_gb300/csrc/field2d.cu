@@ -9,6 +9,9 @@
 // or nearest upsampling by 2 concatenated with the skip tensor, so pooling, upsampling and
 // concatenation never materialise. Layout: channels-first (C, H, W) per scene, as torch's
 // NCHW with B = 1.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -96,9 +99,9 @@ __global__ void f2_scatter_kernel(const float *__restrict__ pos, const float *__
   if (i >= n) return;
   const float mm = mass[i] * mask[i];
   const float val[3] = {mm * a.scale, mm * vel[2 * i] * a.scale, mm * vel[2 * i + 1] * a.scale};
-  double sc[3];
+  float sc[3];  // 2^e, exact in fp32 (fix_exp keeps e within +-126 for finite values)
 #pragma unroll
-  for (int c = 0; c < 3; ++c) sc[c] = ldexp(1.0, fix_exp(mx[c], n));
+  for (int c = 0; c < 3; ++c) sc[c] = __int_as_float((127 + max(-120, min(120, fix_exp(mx[c], n)))) << 23);
   int ix, iy;
   float wx, wy;
   cic2(pos[2 * i], pos[2 * i + 1], a, ix, iy, wx, wy);
@@ -112,7 +115,7 @@ __global__ void f2_scatter_kernel(const float *__restrict__ pos, const float *__
       const float w = (ox ? wx : 1.f - wx) * (oy ? wy : 1.f - wy);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const long long q = __double2ll_rn((double)(val[c] * w) * sc[c]);
+        const long long q = __float2ll_rn(__fmul_rn(val[c] * w, sc[c]));
         atomicAdd(&acc[((size_t)c * G + y) * G + x], (unsigned long long)q);
       }
     }
@@ -125,7 +128,7 @@ __global__ void f2_convert_kernel(const unsigned long long *__restrict__ acc, co
   if (e >= 3ll * G * G) return;
   const int c = (int)(e / ((int64_t)G * G));
   const long long q = (long long)acc[e];
-  out[e] = (float)ldexp((double)q, -fix_exp(mx[c], n));
+  out[e] = (float)ldexp((double)q, -max(-120, min(120, fix_exp(mx[c], n))));
 }
 
 // ---------------------------------------------------------------------------------
@@ -439,6 +442,249 @@ __global__ void f2_kick_kernel(const float *__restrict__ vel, const float *__res
   vel_out[e] = vel[e] + d;
 }
 
+// ---------------------------------------------------------------------------------
+// Chunked large-N tick (scripts/scatter_bh_1b.py:107-146): body state stored in fp32, fp16 or
+// bf16, widened to fp32 per body; relativistic speed v = p / sqrt(1 + |p|^2 / c^2)
+// (scripts/scatter_bh.py:22-23); drift fused into the three-channel scatter, gather fused with
+// the kick. Unit masses and masks, as the reference's Sim.
+// ---------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ float ld_f(const T *p, int64_t i);
+template <> __device__ __forceinline__ float ld_f<float>(const float *p, int64_t i) { return p[i]; }
+template <> __device__ __forceinline__ float ld_f<__half>(const __half *p, int64_t i) { return __half2float(p[i]); }
+template <> __device__ __forceinline__ float ld_f<__nv_bfloat16>(const __nv_bfloat16 *p, int64_t i) {
+  return __bfloat162float(p[i]);
+}
+template <typename T> __device__ __forceinline__ float st_f(T *p, int64_t i, float v);  // returns the stored value
+template <> __device__ __forceinline__ float st_f<float>(float *p, int64_t i, float v) { p[i] = v; return v; }
+template <> __device__ __forceinline__ float st_f<__half>(__half *p, int64_t i, float v) {
+  const __half h = __float2half_rn(v);
+  p[i] = h;
+  return __half2float(h);
+}
+template <> __device__ __forceinline__ float st_f<__nv_bfloat16>(__nv_bfloat16 *p, int64_t i, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  p[i] = h;
+  return __bfloat162float(h);
+}
+
+// (x, y) of body i as one 2-element load / store
+template <typename T> __device__ __forceinline__ float2 ld2(const T *p, int64_t i);
+template <> __device__ __forceinline__ float2 ld2<float>(const float *p, int64_t i) {
+  return reinterpret_cast<const float2 *>(p)[i];
+}
+template <> __device__ __forceinline__ float2 ld2<__half>(const __half *p, int64_t i) {
+  return __half22float2(reinterpret_cast<const __half2 *>(p)[i]);
+}
+template <> __device__ __forceinline__ float2 ld2<__nv_bfloat16>(const __nv_bfloat16 *p, int64_t i) {
+  return __bfloat1622float2(reinterpret_cast<const __nv_bfloat162 *>(p)[i]);
+}
+template <typename T> __device__ __forceinline__ void st2(T *p, int64_t i, float2 v);  // v already representable
+template <> __device__ __forceinline__ void st2<float>(float *p, int64_t i, float2 v) {
+  reinterpret_cast<float2 *>(p)[i] = v;
+}
+template <> __device__ __forceinline__ void st2<__half>(__half *p, int64_t i, float2 v) {
+  reinterpret_cast<__half2 *>(p)[i] = __floats2half2_rn(v.x, v.y);
+}
+template <> __device__ __forceinline__ void st2<__nv_bfloat16>(__nv_bfloat16 *p, int64_t i, float2 v) {
+  reinterpret_cast<__nv_bfloat162 *>(p)[i] = __floats2bfloat162_rn(v.x, v.y);
+}
+
+template <typename T> __device__ __forceinline__ float round_f(float v);  // v rounded to T, widened back
+template <> __device__ __forceinline__ float round_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float round_f<__half>(float v) { return __half2float(__float2half_rn(v)); }
+template <> __device__ __forceinline__ float round_f<__nv_bfloat16>(float v) {
+  return __bfloat162float(__float2bfloat16_rn(v));
+}
+
+struct TickArgs {
+  int G;
+  float E, h, scale;       // scale = in_scale / h^2
+  float ms, c2, dt;        // momentum scale, c^2, drift step
+  int e[3];                // fixed-point exponents of the three channels
+  float p2[3];             // 2^e, exact in fp32: value * 2^e is exact, so the integer is the rounded value
+};
+
+// fp32 in torch's operation order, no contractions: p / sqrt(1 + (px^2 + py^2) / c^2)
+__device__ __forceinline__ void rel_speed(float px, float py, const TickArgs &a, float &vx, float &vy) {
+  const float s = __fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py));
+  const float d = __fsqrt_rn(__fadd_rn(1.f, __fdiv_rn(s, a.c2)));
+  vx = __fdiv_rn(px, d);
+  vy = __fdiv_rn(py, d);
+}
+
+// Position after the drift as the state type stores it: (pos + dt v) rounded to TP.
+template <typename TP, typename TM>
+__device__ __forceinline__ void drifted(const TP *pos, const TM *mom, int64_t i, const TickArgs &a, int drift,
+                                        float &x, float &y, float &vx, float &vy) {
+  const float2 p = ld2(mom, i), q = ld2(pos, i);
+  rel_speed(__fmul_rn(p.x, a.ms), __fmul_rn(p.y, a.ms), a, vx, vy);
+  x = q.x;
+  y = q.y;
+  if (drift) {
+    x = round_f<TP>(__fadd_rn(x, __fmul_rn(a.dt, vx)));
+    y = round_f<TP>(__fadd_rn(y, __fmul_rn(a.dt, vy)));
+  }
+}
+
+__device__ __forceinline__ void cic_w(float x, float y, const TickArgs &a, int &ix, int &iy, float &wx, float &wy) {
+  const float ux = __fsub_rn(__fdiv_rn(__fadd_rn(x, 0.5f * a.E), a.h), 0.5f);
+  const float uy = __fsub_rn(__fdiv_rn(__fadd_rn(y, 0.5f * a.E), a.h), 0.5f);
+  const float fx = floorf(ux), fy = floorf(uy);
+  wx = __fsub_rn(ux, fx);
+  wy = __fsub_rn(uy, fy);
+  ix = (int)fx;
+  iy = (int)fy;
+}
+
+// Scatter at the drifted positions (the state is not written here). SMEM: one channel per CTA
+// (blockIdx.y) in int64 shared accumulators (G^2 words), a grid-stride loop over the bodies,
+// one flush per CTA into the global int64 grid; otherwise int64 global atomics, all channels.
+template <typename TP, typename TM, bool SMEM>
+__global__ void __launch_bounds__(1024) t2_scatter_kernel(const TP *__restrict__ pos, const TM *__restrict__ mom,
+                                                          int64_t n, TickArgs a, int drift,
+                                                          unsigned long long *__restrict__ acc) {
+  extern __shared__ unsigned long long s_acc64[];
+  const int G = a.G, GG = G * G;
+  const int ch = SMEM ? blockIdx.y : 0;
+  if (SMEM) {
+    for (int e = threadIdx.x; e < GG; e += blockDim.x) s_acc64[e] = 0ull;
+    __syncthreads();
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float x, y, vx, vy;
+    drifted(pos, mom, i, a, drift, x, y, vx, vy);
+    const float val[3] = {a.scale, __fmul_rn(vx, a.scale), __fmul_rn(vy, a.scale)};
+    int ix, iy;
+    float wx, wy;
+    cic_w(x, y, a, ix, iy, wx, wy);
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const int cx = ix + ox, cy = iy + oy;
+        if (cx < 0 || cx >= G || cy < 0 || cy >= G) continue;
+        const float w = __fmul_rn(ox ? wx : __fsub_rn(1.f, wx), oy ? wy : __fsub_rn(1.f, wy));
+        if (SMEM) {
+          const long long q = __float2ll_rn(__fmul_rn(__fmul_rn(val[ch], w), a.p2[ch]));
+          atomicAdd(&s_acc64[cy * G + cx], (unsigned long long)q);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const long long q = __float2ll_rn(__fmul_rn(__fmul_rn(val[c], w), a.p2[c]));
+            atomicAdd(&acc[(size_t)c * GG + cy * G + cx], (unsigned long long)q);
+          }
+        }
+      }
+    }
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < GG; e += blockDim.x) {
+      const unsigned long long v = s_acc64[e];
+      if (v) atomicAdd(&acc[(size_t)ch * GG + e], v);
+    }
+  }
+}
+
+// the drift alone, stored (Sim.scatter_pass's pos update when no scatter follows)
+template <typename TP, typename TM>
+__global__ void t2_drift_kernel(TP *__restrict__ pos, const TM *__restrict__ mom, int64_t n, TickArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x, y, vx, vy;
+  drifted(pos, mom, i, a, 1, x, y, vx, vy);
+  st2(pos, i, make_float2(x, y));
+}
+
+__global__ void t2_convert_kernel(const unsigned long long *__restrict__ acc, TickArgs a, float *__restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int GG = a.G * a.G;
+  if (e >= 3 * GG) return;
+  out[e] = (float)ldexp((double)(long long)acc[e], -a.e[e / GG]);
+}
+
+// mean acceleration from the grid: sum_cells acc * rho * cell_mass / n, FP64 in a fixed order
+// (Sim.grid_force, scripts/scatter_bh_1b.py:113-121)
+__global__ void __launch_bounds__(MF_THREADS) t2_abar_part_kernel(const float4 *__restrict__ F4,
+                                                                  const float *__restrict__ rho, int GG,
+                                                                  double cell_mass, double *__restrict__ part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int e = blockIdx.x * MF_THREADS + threadIdx.x; e < GG; e += MF_BLOCKS * MF_THREADS) {
+    const double w = (double)rho[e] * cell_mass;
+    const float4 f = F4[e];
+    s1 += (double)f.x * w;
+    s2 += (double)f.y * w;
+  }
+  __shared__ double sh[2][MF_THREADS];
+  sh[0][threadIdx.x] = s1;
+  sh[1][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = MF_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = 0.0;  // count slot unused
+    part[MF_BLOCKS + blockIdx.x] = sh[0][0];
+    part[2 * MF_BLOCKS + blockIdx.x] = sh[1][0];
+  }
+}
+
+__global__ void __launch_bounds__(MF_BLOCKS) t2_abar_fold_kernel(const double *__restrict__ part, double inv_n,
+                                                                 float *__restrict__ abar) {
+  __shared__ double sh[2][MF_BLOCKS];
+  sh[0][threadIdx.x] = part[MF_BLOCKS + threadIdx.x];
+  sh[1][threadIdx.x] = part[2 * MF_BLOCKS + threadIdx.x];
+  __syncthreads();
+  for (int w = MF_BLOCKS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    abar[0] = (float)(sh[0][0] * inv_n);
+    abar[1] = (float)(sh[1][0] * inv_n);
+  }
+}
+
+// a = gather(acc grid) in the reference's corner order (ScatterField._corner_iter: x offset
+// outer, y inner; off-grid corners dropped), mom = mom + kick * (a - abar) / ms
+template <typename TP, typename TM>
+__global__ void t2_gather_kick_kernel(const float4 *__restrict__ F4, TP *__restrict__ pos, TM *__restrict__ mom,
+                                      int64_t n, TickArgs a, int drift, float kick, const float *__restrict__ abar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int G = a.G;
+  float x, y, vx, vy;
+  drifted(pos, mom, i, a, drift, x, y, vx, vy);
+  if (drift) st2(pos, i, make_float2(x, y));
+  int ix, iy;
+  float wx, wy;
+  cic_w(x, y, a, ix, iy, wx, wy);
+  float ax = 0.f, ay = 0.f;
+#pragma unroll
+  for (int ox = 0; ox < 2; ++ox) {
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      const int cx = ix + ox, cy = iy + oy;
+      const bool ok = cx >= 0 && cx < G && cy >= 0 && cy < G;
+      const float w = __fmul_rn(ox ? wx : __fsub_rn(1.f, wx), oy ? wy : __fsub_rn(1.f, wy));
+      const float4 f = F4[min(max(cy, 0), G - 1) * G + min(max(cx, 0), G - 1)];
+      const float wk = ok ? w : 0.f;
+      ax = __fadd_rn(ax, __fmul_rn(f.x, wk));
+      ay = __fadd_rn(ay, __fmul_rn(f.y, wk));
+    }
+  }
+  const float2 m0 = ld2(mom, i);
+  st2(mom, i, make_float2(__fadd_rn(m0.x, __fdiv_rn(__fmul_rn(kick, __fsub_rn(ax, abar[0])), a.ms)),
+                          __fadd_rn(m0.y, __fdiv_rn(__fmul_rn(kick, __fsub_rn(ay, abar[1])), a.ms))));
+}
+
 }  // namespace
 
 extern "C" {
@@ -623,6 +869,148 @@ int augur_field2d_kick(const float *vel, const float *acc0, const float *acc1, i
                                                              dv_out);
   F2_LAUNCH_CHECK();
   return AUGUR_OK;
+}
+
+}  // extern "C"
+
+// ---- chunked large-N tick ----------------------------------------------------------------
+namespace {
+TickArgs tick_args(int grid, double extent, double in_scale, double ms, double c, double dt) {
+  TickArgs a{};
+  a.G = grid;
+  a.E = (float)extent;
+  a.h = (float)(extent / grid);
+  a.scale = (float)(in_scale / ((double)a.h * (double)a.h));
+  a.ms = (float)ms;
+  a.c2 = (float)(c * c);
+  a.dt = (float)dt;
+  return a;
+}
+int ceil_log2(double v) {
+  int e;
+  std::frexp(v, &e);  // v < 2^e
+  return e;
+}
+constexpr size_t T2_SMEM_MAX = 200 * 1024;
+
+template <typename TP, typename TM>
+int tick_launch(int what, void *pos, void *mom, int64_t n, TickArgs a, int drift, unsigned long long *acc,
+                const float4 *F4, float kick, const float *abar, cudaStream_t st) {
+  if (what == 0) {  // scatter
+    const size_t sm = (size_t)a.G * a.G * sizeof(unsigned long long);
+    if (sm <= T2_SMEM_MAX) {
+      static bool raised = false;
+      if (!raised) {
+        if (cudaFuncSetAttribute(t2_scatter_kernel<TP, TM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)T2_SMEM_MAX))
+          return AUGUR_ECUDA;
+        raised = true;
+      }
+      // persistent CTAs per channel (one per SM at this shared-memory size), each flushes once
+      const unsigned per = (unsigned)std::max<int64_t>(1, std::min<int64_t>(101, (n + 1023) / 1024));
+      t2_scatter_kernel<TP, TM, true><<<dim3(per, 3), 1024, sm, st>>>((const TP *)pos, (const TM *)mom, n, a, drift,
+                                                                      acc);
+    } else {
+      t2_scatter_kernel<TP, TM, false><<<(unsigned)std::min<int64_t>((n + 1023) / 1024, 4096), 1024, 0, st>>>(
+          (const TP *)pos, (const TM *)mom, n, a, drift, acc);
+    }
+  } else if (what == 1) {
+    t2_drift_kernel<TP, TM><<<nblocks(n, 256), 256, 0, st>>>((TP *)pos, (const TM *)mom, n, a);
+  } else {
+    t2_gather_kick_kernel<TP, TM><<<nblocks(n, 256), 256, 0, st>>>(F4, (TP *)pos, (TM *)mom, n, a, drift, kick, abar);
+  }
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+template <typename TP>
+int tick_m(int mt, int what, void *pos, void *mom, int64_t n, TickArgs a, int drift, unsigned long long *acc,
+           const float4 *F4, float kick, const float *abar, cudaStream_t st) {
+  switch (mt) {
+    case AUGUR_DTYPE_F32: return tick_launch<TP, float>(what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+    case AUGUR_DTYPE_F16: return tick_launch<TP, __half>(what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+    case AUGUR_DTYPE_BF16:
+      return tick_launch<TP, __nv_bfloat16>(what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+  }
+  return AUGUR_EINVAL;
+}
+int tick_dispatch(int pt, int mt, int what, void *pos, void *mom, int64_t n, TickArgs a, int drift,
+                  unsigned long long *acc, const float4 *F4, float kick, const float *abar, cudaStream_t st) {
+  switch (pt) {
+    case AUGUR_DTYPE_F32: return tick_m<float>(mt, what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+    case AUGUR_DTYPE_F16: return tick_m<__half>(mt, what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+    case AUGUR_DTYPE_BF16: return tick_m<__nv_bfloat16>(mt, what, pos, mom, n, a, drift, acc, F4, kick, abar, st);
+  }
+  return AUGUR_EINVAL;
+}
+}  // namespace
+
+extern "C" {
+
+size_t augur_tick2d_work_bytes(int grid) {
+  return grid < 1 ? 0 : (size_t)3 * grid * grid * sizeof(unsigned long long) + 3 * MF_BLOCKS * sizeof(double);
+}
+
+int augur_tick2d_drift_scatter(const void *pos, const void *mom, int64_t n, int pos_type, int mom_type,
+                               double mom_scale, double c, double dt, int drift, int grid, double extent,
+                               double in_scale, float *out3, void *work, void *stream) {
+  if (grid < 2 || grid > 4096 || !(extent > 0.0) || !(c > 0.0) || !(mom_scale > 0.0) || !out3 || !work)
+    return AUGUR_EINVAL;
+  if (n < 0 || (n > 0 && (!pos || !mom)) || (reinterpret_cast<uintptr_t>(work) & 7)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  TickArgs a = tick_args(grid, extent, in_scale, mom_scale, c, dt);
+  // |v| < c bounds every channel value before the pass: n of them fit in 61 bits
+  const double vmax[3] = {(double)a.scale, c * a.scale, c * a.scale};
+  for (int k = 0; k < 3; ++k) {
+    a.e[k] = 61 - ceil_log2((double)std::max<int64_t>(n, 1)) - ceil_log2(vmax[k]);
+    a.e[k] = std::max(-120, std::min(120, a.e[k]));  // 2^e stays a normal fp32 power of two
+    a.p2[k] = std::ldexp(1.0f, a.e[k]);
+  }
+  auto *acc = reinterpret_cast<unsigned long long *>(work);
+  if (cudaMemsetAsync(acc, 0, (size_t)3 * grid * grid * sizeof(unsigned long long), st) != cudaSuccess)
+    return AUGUR_ECUDA;
+  if (n > 0) {
+    const int rc = tick_dispatch(pos_type, mom_type, 0, const_cast<void *>(pos), const_cast<void *>(mom), n, a,
+                                 drift, acc, nullptr, 0.f, nullptr, st);
+    if (rc) return rc;
+  }
+  t2_convert_kernel<<<nblocks(3 * (int64_t)grid * grid, 256), 256, 0, st>>>(acc, a, out3);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int augur_tick2d_drift(void *pos, const void *mom, int64_t n, int pos_type, int mom_type, double mom_scale, double c,
+                       double dt, void *stream) {
+  if (!(c > 0.0) || !(mom_scale > 0.0) || n < 0 || (n > 0 && (!pos || !mom))) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  TickArgs a = tick_args(2, 1.0, 1.0, mom_scale, c, dt);
+  return tick_dispatch(pos_type, mom_type, 1, pos, const_cast<void *>(mom), n, a, 1, nullptr, nullptr, 0.f, nullptr,
+                       S(stream));
+}
+
+int augur_tick2d_mean_acc(const float *force4, const float *rho, int grid, double cell_mass, int64_t n, float *abar,
+                          void *work, void *stream) {
+  if (!force4 || !rho || !abar || !work || grid < 1 || n < 1) return AUGUR_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(force4) & 15) || (reinterpret_cast<uintptr_t>(work) & 7)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  double *part = reinterpret_cast<double *>(reinterpret_cast<unsigned long long *>(work) + (size_t)3 * grid * grid);
+  t2_abar_part_kernel<<<MF_BLOCKS, MF_THREADS, 0, st>>>(reinterpret_cast<const float4 *>(force4), rho, grid * grid,
+                                                        cell_mass, part);
+  F2_LAUNCH_CHECK();
+  t2_abar_fold_kernel<<<1, MF_BLOCKS, 0, st>>>(part, 1.0 / (double)n, abar);
+  F2_LAUNCH_CHECK();
+  return AUGUR_OK;
+}
+
+int augur_tick2d_gather_kick(const float *force4, void *pos, void *mom, int64_t n, int pos_type, int mom_type,
+                             double mom_scale, double kick_dt, const float *abar, int grid, double extent, int drift,
+                             double c, double dt, void *stream) {
+  if (!force4 || !abar || grid < 2 || !(extent > 0.0) || !(mom_scale > 0.0) || (drift && !(c > 0.0)))
+    return AUGUR_EINVAL;
+  if (n < 0 || (n > 0 && (!pos || !mom)) || (reinterpret_cast<uintptr_t>(force4) & 15)) return AUGUR_EINVAL;
+  if (n == 0) return AUGUR_OK;
+  TickArgs a = tick_args(grid, extent, 1.0, mom_scale, drift ? c : 1.0, dt);
+  return tick_dispatch(pos_type, mom_type, 2, pos, mom, n, a, drift, nullptr, reinterpret_cast<const float4 *>(force4),
+                       (float)kick_dt, abar, S(stream));
 }
 
 }  // extern "C"

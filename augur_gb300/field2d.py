@@ -175,3 +175,84 @@ class UNetScatterField:
         self._call("augur_field2d_kick", vel.data_ptr(), a_prev.data_ptr(), a_new.data_ptr(), n, self.dt,
                    vel_new.data_ptr(), dv.data_ptr())
         return pos_new, vel_new, (f, a_new), dv
+
+
+class ChunkedTick2D:
+    """The reference's large-N tick, Sim (scripts/scatter_bh_1b.py:107-146), on a loaded
+    UNetScatterField: unit-mass bodies whose (N, 2) position and momentum tensors are stored in
+    float32, float16 or bfloat16 and updated in place. State is kept half-kicked (M = p + dt/2 a):
+    tick = drift with the relativistic speed fused into the scatter, grid force (learned kernel,
+    U-Net with the recurrent potential, -grad + kernel acceleration), the density-weighted mean
+    acceleration from the grid, gather fused with the kick. The reference loops over chunks of
+    bodies to bound its fp32 temporaries; here every kernel widens one body at a time, so there
+    are no temporaries and no chunking."""
+
+    DTYPES = {torch.float32: 0, torch.float16: 1, torch.bfloat16: 2}
+
+    def __init__(self, model: UNetScatterField, n: int, c: float = 10.0, dt: float = 0.1,
+                 pos_dtype=torch.float16, mom_dtype=torch.float16, mom_scale: float = 1.0):
+        if model.net is None:
+            raise RuntimeError("load the model's weights first")
+        if pos_dtype not in self.DTYPES or mom_dtype not in self.DTYPES:
+            raise ValueError("state dtypes: float32, float16 or bfloat16")
+        self.m, self.n, self.c, self.dt, self.ms = model, int(n), float(c), float(dt), float(mom_scale)
+        self.pd, self.md = pos_dtype, mom_dtype
+        G, dev = model.grid, model.device
+        self.field = torch.zeros(model.cf, G, G, device=dev)
+        self.x = torch.zeros(model.cin, G, G, device=dev)
+        self.f4a = torch.empty(G, G, 4, device=dev)
+        self.abar = torch.zeros(2, device=dev)
+        self.work = torch.empty(int(model.lib.augur_tick2d_work_bytes(G)), dtype=torch.uint8, device=dev)
+
+    def _check(self, pos, mom):
+        for name, t, dt in (("pos", pos, self.pd), ("mom", mom, self.md)):
+            if t.dtype != dt or t.shape != (self.n, 2) or not t.is_contiguous() or t.device != self.m.device:
+                raise ValueError(f"{name} must be a contiguous ({self.n}, 2) {dt} tensor on {self.m.device}")
+
+    def _scatter(self, pos, mom, drift: bool):
+        m = self.m
+        m._call("augur_tick2d_drift_scatter", pos.data_ptr(), mom.data_ptr(), self.n, self.DTYPES[self.pd],
+                self.DTYPES[self.md], self.ms, self.c, self.dt, int(bool(drift)), m.grid, m.extent, m.in_scale,
+                self.x.data_ptr(), self.work.data_ptr())
+
+    def scatter_pass(self, pos, mom, drift: bool) -> torch.Tensor:
+        """Sim.scatter_pass: (3, G, G) scatter of [1, vx, vy]; with drift=True pos is drifted first."""
+        self._check(pos, mom)
+        self._scatter(pos, mom, drift)
+        if drift:
+            self.m._call("augur_tick2d_drift", pos.data_ptr(), mom.data_ptr(), self.n, self.DTYPES[self.pd],
+                         self.DTYPES[self.md], self.ms, self.c, self.dt)
+        return self.x[:3]
+
+    def grid_force(self):
+        """Sim.grid_force on the current scatter: (acceleration grid (G, G, 4), abar (2,))."""
+        m, G = self.m, self.m.grid
+        f4k = m.plan.poisson(self.x[0])
+        m._call("augur_field2d_inputs", f4k.data_ptr(), self.field.data_ptr(), m.cf, G, self.x.data_ptr())
+        m._call("augur_unet2d_forward", m.net.data_ptr(), m.cin, m.cf, m.width, m.levels, G, self.x.data_ptr(),
+                self.field.data_ptr(), m._wu.data_ptr(), m._wu_bytes)
+        m._call("augur_field2d_accel", self.field.data_ptr(), f4k.data_ptr(), G, m.h, self.f4a.data_ptr())
+        m._call("augur_tick2d_mean_acc", self.f4a.data_ptr(), self.x.data_ptr(), G, m.h * m.h / m.in_scale, self.n,
+                self.abar.data_ptr(), self.work.data_ptr())
+        return self.f4a, self.abar
+
+    def _kick(self, pos, mom, kick, drift: bool):
+        m = self.m
+        m._call("augur_tick2d_gather_kick", self.f4a.data_ptr(), pos.data_ptr(), mom.data_ptr(), self.n,
+                self.DTYPES[self.pd], self.DTYPES[self.md], self.ms, kick, self.abar.data_ptr(), m.grid, m.extent,
+                int(bool(drift)), self.c, self.dt)
+
+    def tick(self, pos, mom) -> None:
+        """Sim.tick: drift, scatter, grid force, mom += dt (a - abar) / ms, in place. The scatter
+        reads the drifted positions without storing them; the gather-kick stores them."""
+        self._check(pos, mom)
+        self._scatter(pos, mom, True)
+        self.grid_force()
+        self._kick(pos, mom, self.dt, True)
+
+    def init_kick(self, pos, mom) -> None:
+        """Sim.init_kick: the first half kick, mom += dt/2 (a - abar) / ms."""
+        self._check(pos, mom)
+        self._scatter(pos, mom, False)
+        self.grid_force()
+        self._kick(pos, mom, 0.5 * self.dt, False)

@@ -96,6 +96,41 @@ int augur_field2d_drift(const float *pos, const float *vel, const float *acc, in
 int augur_field2d_kick(const float *vel, const float *acc0, const float *acc1, int64_t n, double dt,
                        float *vel_out, float *dv_out, void *stream);
 
+/*
+ * Chunked large-N tick of the 2D model (Sim, scripts/scatter_bh_1b.py:107-146): unit-mass
+ * bodies whose state (pos, momentum; (N, 2) each) is stored as fp32, fp16 or bf16 and widened
+ * per body, with the relativistic speed v = p ms / sqrt(1 + |p ms|^2 / c^2)
+ * (scripts/scatter_bh.py:22-23); drift = (pos + dt v) rounded to the position type. One tick is
+ *   augur_tick2d_drift_scatter(drift = 1)  out3 = scatter of [1, vx, vy] * in_scale / h^2 at the
+ *                                          drifted positions (the state is not written)
+ *   grid force as above (kernel acceleration, U-Net on [out3, kernel acc, field], -grad + kernel)
+ *   augur_tick2d_mean_acc                  abar = sum_cells acc * rho * h^2 / in_scale / N (FP64)
+ *   augur_tick2d_gather_kick(drift = 1, kick = dt)   stores the drifted pos (from the same,
+ *                                          not yet kicked momentum), then mom += kick (gather(acc,
+ *                                          pos) - abar) / ms
+ * and init_kick is the same with drift = 0 and kick = dt/2; augur_tick2d_drift stores the drift
+ * alone. The scatter is deterministic: contributions are rounded to a fixed point bounded by
+ * |v| < c and N, summed in int64 (one channel per CTA in shared memory for grid <= 160, then one
+ * flush per CTA). fp32 arithmetic follows torch's operation order without contractions.
+ * work: augur_tick2d_work_bytes(grid) bytes, 8-byte aligned.
+ */
+#define AUGUR_DTYPE_F32  0
+#define AUGUR_DTYPE_F16  1
+#define AUGUR_DTYPE_BF16 2
+size_t augur_tick2d_work_bytes(int grid);
+int augur_tick2d_drift_scatter(const void *pos, const void *mom, int64_t n, int pos_type,
+                               int mom_type, double mom_scale, double c, double dt, int drift,
+                               int grid, double extent, double in_scale, float *out3, void *work,
+                               void *stream);
+int augur_tick2d_drift(void *pos, const void *mom, int64_t n, int pos_type, int mom_type,
+                       double mom_scale, double c, double dt, void *stream);
+int augur_tick2d_mean_acc(const float *force4, const float *rho, int grid, double cell_mass,
+                          int64_t n, float *abar, void *work, void *stream);
+int augur_tick2d_gather_kick(const float *force4, void *pos, void *mom, int64_t n, int pos_type,
+                             int mom_type, double mom_scale, double kick_dt, const float *abar,
+                             int grid, double extent, int drift, double c, double dt,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -269,9 +269,49 @@ def field2d_cases():
     np.savez_compressed(OUT / "field2d.npz", **out)
 
 
+def tick2d_cases():
+    """The reference's chunked large-N tick (scripts/scatter_bh_1b.py: make_ic :66-104, Sim
+    :107-146) on the CPU: the production 2D model without its pair term (ops.no_pp), relativistic
+    speed (scripts/scatter_bh.py:22-23), state stored in float16 / float32, an 8000-body Gaussian
+    scene in chunks of 3000; init_kick and two ticks. Weights: those of field2d.npz."""
+    from types import SimpleNamespace
+
+    from scripts import scatter_bh_1b as bh
+
+    gw = np.load(OUT / "field2d.npz")
+    m = sf.ScatterField(grid=128, extent=64.0, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+                        potential=True, verlet=True).eval()
+    m.load_state_dict({k: torch.from_numpy(gw["w_" + k].astype(np.float32)) for k in gw["names"]}, strict=False)
+    ops.no_pp(m)
+    n, chunk, ticks = 8000, 3000, 2
+    args = SimpleNamespace(sigma=8.0, vfac=0.3, c=10.0, seed=4738, ic="gaussian", ic_resample=False)
+    out = {"n": np.int32(n), "c": np.float64(10.0), "dt": np.float64(0.1), "ticks": np.int32(ticks)}
+    for name, pd, md in (("f16", torch.float16, torch.float16), ("f32", torch.float32, torch.float32)):
+        with torch.no_grad():
+            pos, mom = bh.make_ic(n, chunk, args, pd, md, 1.0, torch.device("cpu"))
+            sim = bh.Sim(m, n, chunk, 10.0, 0.1, pd, md, 1.0, torch.device("cpu"))
+            out[f"{name}_pos0"], out[f"{name}_mom0"] = pos.numpy().copy(), mom.numpy().copy()
+            x = sim.scatter_pass(pos, mom, False)
+            acc, abar = sim.grid_force(x)
+            if name == "f32":
+                out[f"{name}_x0"] = x[0].numpy()
+            out[f"{name}_abar0"] = abar.numpy()
+            sim.field = m.init_field(1, "cpu")[0]
+            sim.init_kick(pos, mom)
+            out[f"{name}_mom_ik"] = mom.numpy().copy()
+            ps, ms_ = [], []
+            for _ in range(ticks):
+                sim.tick(pos, mom)
+                ps.append(pos.numpy().copy())
+                ms_.append(mom.numpy().copy())
+            out[f"{name}_pos"], out[f"{name}_mom"] = np.stack(ps), np.stack(ms_)
+            out[f"{name}_field"] = sim.field[0, 0].numpy().astype(np.float32)
+    np.savez_compressed(OUT / "tick2d.npz", **out)
+
+
 CASES = {"cell_index": cell_index_cases, "scatter_gather": scatter_gather_cases, "pm_acc": pm_acc_cases,
          "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases, "pair_acc": pair_acc_cases,
-         "field2d": field2d_cases}
+         "field2d": field2d_cases, "tick2d": tick2d_cases}
 
 if __name__ == "__main__":
     for name in (sys.argv[1:] or list(CASES)):
