@@ -502,7 +502,12 @@ struct TickArgs {
   float ms, c2, dt;        // momentum scale, c^2, drift step
   int e[3];                // fixed-point exponents of the three channels
   float p2[3];             // 2^e, exact in fp32: value * 2^e is exact, so the integer is the rounded value
+  float inv_h, inv_ms;     // 1/h, 1/ms when h, ms are powers of two (x / h == x * (1/h) exactly), else 0
 };
+
+__device__ __forceinline__ float div_or_mul(float x, float d, float inv) {
+  return inv != 0.f ? __fmul_rn(x, inv) : __fdiv_rn(x, d);
+}
 
 // fp32 in torch's operation order, no contractions: p / sqrt(1 + (px^2 + py^2) / c^2)
 __device__ __forceinline__ void rel_speed(float px, float py, const TickArgs &a, float &vx, float &vy) {
@@ -527,8 +532,8 @@ __device__ __forceinline__ void drifted(const TP *pos, const TM *mom, int64_t i,
 }
 
 __device__ __forceinline__ void cic_w(float x, float y, const TickArgs &a, int &ix, int &iy, float &wx, float &wy) {
-  const float ux = __fsub_rn(__fdiv_rn(__fadd_rn(x, 0.5f * a.E), a.h), 0.5f);
-  const float uy = __fsub_rn(__fdiv_rn(__fadd_rn(y, 0.5f * a.E), a.h), 0.5f);
+  const float ux = __fsub_rn(div_or_mul(__fadd_rn(x, 0.5f * a.E), a.h, a.inv_h), 0.5f);
+  const float uy = __fsub_rn(div_or_mul(__fadd_rn(y, 0.5f * a.E), a.h, a.inv_h), 0.5f);
   const float fx = floorf(ux), fy = floorf(uy);
   wx = __fsub_rn(ux, fx);
   wy = __fsub_rn(uy, fy);
@@ -681,8 +686,8 @@ __global__ void t2_gather_kick_kernel(const float4 *__restrict__ F4, TP *__restr
     }
   }
   const float2 m0 = ld2(mom, i);
-  st2(mom, i, make_float2(__fadd_rn(m0.x, __fdiv_rn(__fmul_rn(kick, __fsub_rn(ax, abar[0])), a.ms)),
-                          __fadd_rn(m0.y, __fdiv_rn(__fmul_rn(kick, __fsub_rn(ay, abar[1])), a.ms))));
+  st2(mom, i, make_float2(__fadd_rn(m0.x, div_or_mul(__fmul_rn(kick, __fsub_rn(ax, abar[0])), a.ms, a.inv_ms)),
+                          __fadd_rn(m0.y, div_or_mul(__fmul_rn(kick, __fsub_rn(ay, abar[1])), a.ms, a.inv_ms))));
 }
 
 }  // namespace
@@ -884,6 +889,12 @@ TickArgs tick_args(int grid, double extent, double in_scale, double ms, double c
   a.ms = (float)ms;
   a.c2 = (float)(c * c);
   a.dt = (float)dt;
+  auto inv_pow2 = [](float v) {
+    int e;
+    return (v > 0.f && std::frexp(v, &e) == 0.5f) ? 1.0f / v : 0.f;  // exact reciprocal of a power of two
+  };
+  a.inv_h = inv_pow2(a.h);
+  a.inv_ms = inv_pow2(a.ms);
   return a;
 }
 int ceil_log2(double v) {

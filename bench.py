@@ -568,12 +568,186 @@ def run_1e9(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def seeded_field2d_state(seed: int = 4738) -> dict:
+    """Parameters of the production 2D model under the reference's names, drawn as torch's default
+    Linear / Conv2d initialisation does (uniform, bound 1/sqrt(fan_in)), with the output layers of
+    the pair MLP, the kernel MLP and the U-Net zeroed as the reference initialises them
+    (scripts/scatter_field.py:123-136). The work per step does not depend on the values."""
+    g = torch.Generator().manual_seed(seed)
+    shapes = {}
+    for pre in ("ppmlp", "kmlp"):
+        shapes.update({f"{pre}.0.weight": (64, 2), f"{pre}.0.bias": (64,), f"{pre}.2.weight": (64, 64),
+                       f"{pre}.2.bias": (64,), f"{pre}.4.weight": (1, 64), f"{pre}.4.bias": (1,)})
+    shapes.update({"net.inp.weight": (32, 6, 3, 3), "net.inp.bias": (32,)})
+    for blk, cin in [(f"enc.{l}", 32) for l in range(6)] + [(f"dec.{l}", 64) for l in range(5)]:
+        shapes.update({f"net.{blk}.0.weight": (32, cin, 3, 3), f"net.{blk}.0.bias": (32,),
+                       f"net.{blk}.2.weight": (32, 32, 3, 3), f"net.{blk}.2.bias": (32,)})
+    shapes.update({"net.out.weight": (1, 32, 3, 3), "net.out.bias": (1,)})
+    sd = {}
+    for k, shp in shapes.items():
+        wshape = shapes[k.replace(".bias", ".weight")]
+        fan_in = int(np.prod(wshape[1:]))
+        b = 1.0 / math.sqrt(fan_in)
+        sd[k] = (torch.rand(shp, generator=g) * 2 - 1) * b
+    for k in ("ppmlp.4.weight", "ppmlp.4.bias", "kmlp.4.weight", "kmlp.4.bias", "net.out.weight", "net.out.bias"):
+        sd[k].zero_()
+    return sd
+
+
+def _line(args, world, metric, value, unit, ms, config, **extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
+         "config": config}
+    d.update(extra)
+    return d
+
+
+def run_widened(args, world, rank, local):
+    """The widened rows: the pair term (--workload pair), the production 2D model's Verlet step
+    (--workload field2d) and its chunked large-N tick at 10^9 bodies in fp16 (--workload tick1e9)."""
+    from augur_gb300 import ChunkedTick2D, PMPlan, UNetScatterField
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream(dev)
+    K, W = args.steps, args.warmup
+    g = torch.Generator(device=dev)
+    g.manual_seed(9100 + rank)
+
+    def timed(fn):
+        for _ in range(W):
+            fn()
+        torch.cuda.synchronize(dev)
+        clocks = Clocks(local)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(K):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(b) / K
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, clocks.stop()
+
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 FMA rate, TFLOP/s (no measured FP32 peak)
+    if args.workload == "pair":
+        n, ppe, knn, sigma = args.bodies, 0.5, 16, 10.7
+        pos = (torch.randn(n, 2, device=dev, generator=g) * sigma).contiguous()
+        mass, mask = torch.ones(n, device=dev), torch.ones(n, device=dev)
+        params = torch.cat([t.reshape(-1) for k, t in seeded_field2d_state().items() if k.startswith("ppmlp")]).to(dev)
+        params[-65:] = torch.linspace(-0.2, 0.2, 65)  # non-zero output layer
+        plan = PMPlan(2, 128, n, "isolated", 64.0, eps=0.5, device=dev)
+        plan.pair_acc(pos, mass, mask, ppe=ppe, knn=knn, params=params, ncol=2)
+        ms, clk = timed(lambda: plan.pair_acc(pos, mass, mask, ppe=ppe, knn=knn, params=params, ncol=2))
+        launches = plan.last_launches
+        # end to end: host buffers in, accelerations back, every step
+        hp, hm = pos.cpu().pin_memory(), mass.cpu().pin_memory()
+        ha = torch.empty(n, 2).pin_memory()
+
+        def e2e():
+            p, m_ = hp.to(dev, non_blocking=True), hm.to(dev, non_blocking=True)
+            a = plan.pair_acc(p, m_, m_, ppe=ppe, knn=knn, params=params, ncol=2)
+            ha.copy_(a, non_blocking=True)
+        ems, _ = timed(e2e)
+        flop = n * knn * 2 * (64 * 2 + 64 * 64 + 64 + 64 + 64)  # MLP FMAs of the knn pairs (an upper bound)
+        cpu = None
+        if rank == 0 and not args.no_cpu:
+            from oracle import pm_oracle as O
+            q = np.arange(0, n, n // 100)[:100]
+            pn, mn = pos.cpu().numpy(), np.ones(n, np.float32)
+            t0 = time.time()
+            O.pair_acc_2d(pn, mn, mn, params.cpu().numpy(), 2, [], 0, ppe, 0.5, 0.5, knn, queries=q)
+            cpu = {"value": len(q) / (time.time() - t0), "unit": "bodies/s", "cores": 1, "kind": "port",
+                   "sample": "100 query bodies of the same scene, float64 brute-force top-knn (oracle/pm_oracle.py)"}
+        if rank:
+            return
+        print(json.dumps(_line(
+            args, world, "pair-term bodies/s (knn 16, pair-weight MLP), 1e6 Gaussian bodies", world * n / (ms * 1e-3),
+            "bodies/s", ms, {"workload": f"pair term of ScatterField.pp_acc: {n} bodies N(0, {sigma}^2) in 2D, "
+                                         f"ppe {ppe}, knn {knn}, MLP 2-64-64-1", "bodies": n},
+            dtype="f32", gpu_launches=launches * K, clocks=clk,
+            roofline={"bound": "fp32", "kernel": "pair_weight_kernel (with the search)", "achieved": flop / (ms * 1e-3) / 1e12,
+                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": flop / (ms * 1e-3) / 1e12 / fp32_peak,
+                      "peak_kind": "nominal FP32 (152 SMs x 128 FMA x 2.07 GHz)", "traffic": None},
+            e2e={"value": world * n / (ems * 1e-3), "unit": "bodies/s", "h2d_bytes_per_step": 12 * n,
+                 "d2h_bytes_per_step": 8 * n},
+            cpu_baseline=cpu)), flush=True)
+        return
+    m = UNetScatterField(device=dev)
+    m.load_state_dict(seeded_field2d_state())
+    if args.workload == "field2d":
+        n = args.bodies
+        pos = (torch.rand(1, n, 2, device=dev, generator=g) * 40 - 20).contiguous()
+        vel = torch.randn(1, n, 2, device=dev, generator=g).contiguous()
+        mass, mask = torch.ones(1, n, device=dev), torch.ones(1, n, device=dev)
+        state = {"p": pos, "v": vel, "f": m.init_field(1)}
+
+        def step():
+            state["p"], state["v"], state["f"], _ = m.step(state["p"], state["v"], mass, mask, state["f"])
+        ms, clk = timed(step)
+        flop = 2 * 1_039_000_000 * 2  # U-Net MACs per forward (levels 5, width 32, 128^2) x 2 flop
+        if rank:
+            return
+        print(json.dumps(_line(
+            args, world, "body-steps/s of the production 2D model (U-Net, kernel and pair terms, Verlet)",
+            world * n / (ms * 1e-3), "body-steps/s", ms,
+            {"workload": f"ScatterField(grid=128, extent=64, net=unet, kernel, pp=2, split, potential, verlet): one "
+                         f"scene of {n} uniform bodies, dt 0.1, seeded weights (reference init)", "bodies": n},
+            dtype="f32", clocks=clk,
+            roofline={"bound": "fp32", "kernel": "U-Net (f2_conv3_kernel)", "achieved": flop / 2 / (ms * 1e-3) / 1e12,
+                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": flop / 2 / (ms * 1e-3) / 1e12 / fp32_peak,
+                      "peak_kind": "nominal FP32; achieved counts the U-Net's flops over the whole step", "traffic": None},
+            cpu_baseline=None, cpu_note="the reference's own CPU path is timed in the build container (DESIGN.md)")),
+            flush=True)
+        return
+    # tick1e9: the reference's initial conditions (scripts/scatter_bh_1b.py:66-104, gaussian), fp16 state
+    n, c, sigma = args.bodies, 10.0, 8.0
+    pos = torch.empty(n, 2, device=dev, dtype=torch.float16)
+    mom = torch.empty(n, 2, device=dev, dtype=torch.float16)
+    vscale = 0.3 * math.sqrt(n / (4 * sigma))
+    chunk = 50_000_000
+    for s0 in range(0, n, chunk):
+        e0 = min(n, s0 + chunk)
+        p = (torch.randn(e0 - s0, 2, device=dev, generator=g) * sigma).clamp_(-29.0, 29.0)
+        v = torch.randn(e0 - s0, 2, device=dev, generator=g) * vscale
+        vmag = v.norm(dim=-1, keepdim=True).clamp(max=0.99 * c)
+        v = v / v.norm(dim=-1, keepdim=True).clamp_min(1e-30) * vmag
+        pos[s0:e0] = p.half()
+        mom[s0:e0] = (v * (1 - (vmag / c) ** 2).clamp(min=1e-6).rsqrt()).half()
+        del p, v, vmag
+    sim = ChunkedTick2D(m, n, c=c, dt=0.1, pos_dtype=torch.float16, mom_dtype=torch.float16)
+    sim.init_kick(pos, mom)
+    ms, clk = timed(lambda: sim.tick(pos, mom))
+    ok = bool(torch.isfinite(mom[: 1 << 20].float()).all())
+    peak, peak_kind = peaks()
+    B = 16 * n  # fp16 pos and momentum read once and written once
+    if rank:
+        return
+    print(json.dumps(_line(
+        args, world, "body-ticks/s, 1e9-body 2D scene, fp16 state (chunked large-N tick)", world * n / (ms * 1e-3),
+        "body-ticks/s", ms,
+        {"workload": f"Sim.tick of scripts/scatter_bh_1b.py: {n} unit-mass bodies, Gaussian sigma {sigma} clipped "
+                     f"to +-29, relativistic c={c}, dt 0.1, fp16 pos and momentum, production 2D model without "
+                     f"the pair term, seeded weights (reference init)", "bodies": n,
+         "l2": "per-tick traffic %.0f GB >> L2; no flush" % (B / 1e9)},
+        dtype="f16 state / f32 arithmetic", clocks=clk, finite=ok,
+        step_roofline={"bound": "hbm", "algorithmic_bytes": B, "achieved": B / (ms * 1e-3) / 1e9, "peak": peak,
+                       "unit": "GB/s", "frac": B / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind},
+        reference_published={"ms_per_tick": 1325.0, "hardware": "H200 NVL", "source": "results/scatter_bh_1b.json"},
+        cpu_baseline=None, cpu_note="the reference's Sim.tick on CPU is timed in the build container (DESIGN.md)")),
+        flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", choices=("pm", "batch64", "pm1e9"), default="pm",
+    ap.add_argument("--workload", choices=("pm", "batch64", "pm1e9", "pair", "field2d", "tick1e9"), default="pm",
                     help="pm: one 3M-body scene on 256^3 (default); batch64: 64 uneven scenes in one graph; "
-                         "pm1e9: one 1e9-body scene on 1024^3")
+                         "pm1e9: one 1e9-body scene on 1024^3; pair: the pair term at 1e6 bodies; field2d: the "
+                         "production 2D model; tick1e9: its chunked large-N tick at 1e9 bodies, fp16 state")
     ap.add_argument("--streams", type=int, default=16)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=10)
@@ -587,7 +761,8 @@ def main():
     ap.add_argument("--scene", default="plummer", choices=("plummer", "uniform", "clumpy", "disk", "flyby"))
     args = ap.parse_args()
     defaults = {"pm": (2000, 3_000_000, 256, 5e-4), "batch64": (100, None, None, 5e-4),
-                "pm1e9": (20, 1_000_000_000, 1024, 2.5e-4)}[args.workload]
+                "pm1e9": (20, 1_000_000_000, 1024, 2.5e-4), "pair": (20, 1_000_000, 128, 0.1),
+                "field2d": (50, 10_000, 128, 0.1), "tick1e9": (10, 1_000_000_000, 128, 0.1)}[args.workload]
     for k, v in zip(("steps", "bodies", "grid", "dt"), defaults):
         if getattr(args, k) is None:
             setattr(args, k, v)
@@ -599,6 +774,8 @@ def main():
         run_batch(args, world, rank, local)
     elif args.workload == "pm1e9":
         run_1e9(args, world, rank, local)
+    elif args.workload in ("pair", "field2d", "tick1e9"):
+        run_widened(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
 
