@@ -57,8 +57,8 @@ SIGNATURES = {
     "augur_unet2d_param_count": (_i64, [_i32, _i32, _i32, _i32]),
     "augur_unet2d_prepared_count": (_i64, [_i32, _i32, _i32, _i32]),
     "augur_unet2d_prepare": (_i32, [_vp, _i32, _i32, _i32, _i32, _vp, _vp]),
-    "augur_unet2d_work_bytes": (C.c_size_t, [_i32, _i32, _i32]),
-    "augur_unet2d_forward": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, C.c_size_t, _vp]),
+    "augur_unet2d_work_bytes": (C.c_size_t, [_i32, _i32, _i32, _i32]),
+    "augur_unet2d_forward": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _vp, C.c_size_t, _vp]),
     "augur_field2d_accel": (_i32, [_vp, _vp, _i32, _f64, _vp, _vp]),
     "augur_field2d_finish_work_bytes": (C.c_size_t, []),
     "augur_field2d_finish": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),

@@ -181,6 +181,13 @@ __global__ void __launch_bounds__(256 * KS) f2_conv3_kernel(ConvSrc src, const f
   float *sx = smem + (size_t)cin * 9 * CO;  // [cin][CTH][CTH]
   const int tid = threadIdx.x;
   constexpr int NT = 256 * KS;
+  {  // scene blockIdx.z of a batch: channels-first tensors one after another
+    const size_t z = blockIdx.z;
+    const size_t Ha = MODE == A_POOL ? 2 * (size_t)H : MODE == A_UP ? (size_t)(H >> 1) : (size_t)H;
+    src.a += z * src.ca * Ha * Ha;
+    if (src.b) src.b += z * src.cb * (size_t)H * H;
+    out += z * cout * (size_t)H * H;
+  }
   {
     const float4 *w4 = reinterpret_cast<const float4 *>(Wp);
     float4 *s4 = reinterpret_cast<float4 *>(sw);
@@ -281,7 +288,7 @@ __global__ void f2_prep_kernel(const float *__restrict__ W, const float *__restr
 }
 
 template <int KS>
-int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, cudaStream_t st) {
+int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, int batch, cudaStream_t st) {
   static bool raised = false;  // opt in to the large shared-memory carve-out once per process
   if (!raised) {
     const int lim = (int)conv_smem(CIN_MAX);
@@ -291,7 +298,7 @@ int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float 
       return AUGUR_ECUDA;
     raised = true;
   }
-  dim3 grid((H + CT - 1) / CT, (H + CT - 1) / CT);
+  dim3 grid((H + CT - 1) / CT, (H + CT - 1) / CT, batch);
   // the partial-sum exchange reuses the staging region: (KS - 1) x 8 x 256 floats
   const size_t sm = std::max(conv_smem(s.ca + s.cb), (size_t)(KS - 1) * 8 * 256 * sizeof(float));
   switch (s.mode) {
@@ -305,10 +312,11 @@ int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float 
 
 // Input channels are split over 2 threads per output at 64^2 and above (two CTAs of 512 per
 // SM), over 4 below (the few CTAs of the coarse levels get 32 warps each).
-int conv3(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, cudaStream_t st) {
+int conv3(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, int batch, cudaStream_t st) {
   const int cin = s.ca + s.cb;
-  if (cout < 1 || cout > CO || cin < 1 || cin > CIN_MAX) return AUGUR_EINVAL;
-  return H >= 64 ? conv3_ks<2>(s, Wp, cout, H, act, out, st) : conv3_ks<4>(s, Wp, cout, H, act, out, st);
+  if (cout < 1 || cout > CO || cin < 1 || cin > CIN_MAX || batch < 1 || batch > 65535) return AUGUR_EINVAL;
+  return H >= 64 ? conv3_ks<2>(s, Wp, cout, H, act, out, batch, st)
+                 : conv3_ks<4>(s, Wp, cout, H, act, out, batch, st);
 }
 
 // The U-Net's convolutions in parameter order: (cin, cout) of each.
@@ -770,28 +778,29 @@ int augur_unet2d_prepare(const float *params, int cin, int cout, int width, int 
   return AUGUR_OK;
 }
 
-size_t augur_unet2d_work_bytes(int grid, int width, int levels) {
-  if (grid < 1 || width < 1 || levels < 0) return 0;
+size_t augur_unet2d_work_bytes(int grid, int width, int levels, int batch) {
+  if (grid < 1 || width < 1 || levels < 0 || batch < 1) return 0;
   size_t f = 2 * (size_t)width * grid * grid;  // two full-resolution temporaries
   for (int l = 0; l <= levels; ++l) f += (size_t)width * (grid >> l) * (grid >> l);  // encoder outputs (skips)
-  return f * sizeof(float);
+  return f * sizeof(float) * batch;
 }
 
-int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, int levels, int grid, const float *x,
-                         float *y, void *work, size_t work_bytes, void *stream) {
-  if (!prepared || !x || !y || !work) return AUGUR_EINVAL;
+int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, int levels, int grid, int batch,
+                         const float *x, float *y, void *work, size_t work_bytes, void *stream) {
+  if (!prepared || !x || !y || !work || batch < 1 || batch > 65535) return AUGUR_EINVAL;
   if (cin < 1 || cin > CIN_MAX || cout < 1 || cout > CO || width < 1 || width > CO || 2 * width > CIN_MAX ||
       levels < 0 || levels > 10)
     return AUGUR_EINVAL;
   if (grid < 1 || (grid % (1 << levels)) != 0) return AUGUR_EINVAL;
-  if (work_bytes < augur_unet2d_work_bytes(grid, width, levels)) return AUGUR_EINVAL;
+  if (work_bytes < augur_unet2d_work_bytes(grid, width, levels, batch)) return AUGUR_EINVAL;
   if (reinterpret_cast<uintptr_t>(prepared) & 15) return AUGUR_EINVAL;
   cudaStream_t st = S(stream);
-  const size_t GG = (size_t)grid * grid;
-  float *T0 = reinterpret_cast<float *>(work), *T1 = T0 + width * GG;
+  const size_t GG = (size_t)grid * grid, B = (size_t)batch;
+  // every buffer holds the batch's scenes one after another (channels-first per scene)
+  float *T0 = reinterpret_cast<float *>(work), *T1 = T0 + B * width * GG;
   float *Sk[11];
-  Sk[0] = T1 + width * GG;
-  for (int l = 1; l <= levels; ++l) Sk[l] = Sk[l - 1] + (size_t)width * (grid >> (l - 1)) * (grid >> (l - 1));
+  Sk[0] = T1 + B * width * GG;
+  for (int l = 1; l <= levels; ++l) Sk[l] = Sk[l - 1] + B * width * (grid >> (l - 1)) * (grid >> (l - 1));
   int ci[UNET_MAX_LAYERS], co[UNET_MAX_LAYERS];
   const int nl = unet_layers(cin, cout, width, levels, ci, co);
   const float *Lw[UNET_MAX_LAYERS];
@@ -803,23 +812,23 @@ int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, in
   const int w = width;
   int rc, k = 0;
   // h = gelu(inp(x)); encoder blocks at grid / 2^l, each after avg_pool2d(2) of the previous
-  if ((rc = conv3({x, nullptr, cin, 0, A_SAME}, Lw[k++], w, grid, 1, T0, st))) return rc;
+  if ((rc = conv3({x, nullptr, cin, 0, A_SAME}, Lw[k++], w, grid, 1, T0, batch, st))) return rc;
   for (int l = 0; l <= levels; ++l) {
     const int H = grid >> l;
     const ConvSrc s1 = l == 0 ? ConvSrc{T0, nullptr, w, 0, A_SAME} : ConvSrc{Sk[l - 1], nullptr, w, 0, A_POOL};
-    if ((rc = conv3(s1, Lw[k++], w, H, 1, T1, st))) return rc;
-    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[k++], w, H, 1, Sk[l], st))) return rc;
+    if ((rc = conv3(s1, Lw[k++], w, H, 1, T1, batch, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[k++], w, H, 1, Sk[l], batch, st))) return rc;
   }
   // decoder blocks are stored dec[0] .. dec[levels-1]; they run from the deepest level up
   const int kdec = k;
   const float *h = Sk[levels];
   for (int l = levels - 1; l >= 0; --l) {
     const int H = grid >> l;
-    if ((rc = conv3({h, Sk[l], w, w, A_UP}, Lw[kdec + 2 * l], w, H, 1, T1, st))) return rc;
-    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * l + 1], w, H, 1, T0, st))) return rc;
+    if ((rc = conv3({h, Sk[l], w, w, A_UP}, Lw[kdec + 2 * l], w, H, 1, T1, batch, st))) return rc;
+    if ((rc = conv3({T1, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * l + 1], w, H, 1, T0, batch, st))) return rc;
     h = T0;
   }
-  return conv3({h, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * levels], cout, grid, 0, y, st);
+  return conv3({h, nullptr, w, 0, A_SAME}, Lw[kdec + 2 * levels], cout, grid, 0, y, batch, st);
 }
 
 int augur_field2d_accel(const float *phi, const float *force4_kernel, int grid, double h, float *force4_out,

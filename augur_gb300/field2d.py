@@ -45,12 +45,21 @@ class UNetScatterField:
         self.plan: PMPlan | None = None
         self.net = self.kparams = self.pparams = None
         G, dev = self.grid, self.device
-        self._x = torch.zeros((self.cin, G, G), device=dev)
-        self._f4a = torch.empty((G, G, 4), device=dev)
         self._ws = torch.empty(int(self.lib.augur_field2d_scatter_work_bytes(G)), dtype=torch.uint8, device=dev)
-        self._wu_bytes = int(self.lib.augur_unet2d_work_bytes(G, self.width, self.levels))
-        self._wu = torch.empty(self._wu_bytes, dtype=torch.uint8, device=dev)
         self._wf = torch.empty(int(self.lib.augur_field2d_finish_work_bytes()), dtype=torch.uint8, device=dev)
+        self._batch = 0
+        self._buffers(1)
+
+    def _buffers(self, B: int) -> None:
+        """Per-batch buffers: input stacks (B, 6, G, G), acceleration grids (B, G, G, 4), U-Net work."""
+        if B <= self._batch:
+            return
+        G, dev = self.grid, self.device
+        self._x = torch.zeros((B, self.cin, G, G), device=dev)
+        self._f4a = torch.empty((B, G, G, 4), device=dev)
+        self._wu_bytes = int(self.lib.augur_unet2d_work_bytes(G, self.width, self.levels, B))
+        self._wu = torch.empty(self._wu_bytes, dtype=torch.uint8, device=dev)
+        self._batch = B
 
     # ---- parameters ------------------------------------------------------------------------
     def ppe(self) -> float:
@@ -113,31 +122,40 @@ class UNetScatterField:
         return out
 
     def unet(self, x: torch.Tensor) -> torch.Tensor:
-        """The grid net alone: (B, 6, G, G) -> (B, 1, G, G)."""
+        """The grid net alone: (B, 6, G, G) -> (B, 1, G, G), all scenes in the same launches."""
         x = x.to(self.device, torch.float32).contiguous()
-        y = torch.empty((x.shape[0], self.cf, self.grid, self.grid), device=self.device)
-        for b in range(x.shape[0]):
-            self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels,
-                       self.grid, x[b].data_ptr(), y[b].data_ptr(), self._wu.data_ptr(), self._wu_bytes)
+        B = x.shape[0]
+        self._buffers(B)
+        y = torch.empty((B, self.cf, self.grid, self.grid), device=self.device)
+        self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels,
+                   self.grid, B, x.data_ptr(), y.data_ptr(), self._wu.data_ptr(), self._wu_bytes)
         return y
 
-    def _force1(self, pos, vel, mass, mask, field, acc_out, field_out):
-        n = pos.shape[0]
+    def _forces(self, pos, vel, mass, mask, field, acc_out, field_out):
+        """One force evaluation of B scenes: per-scene scatter and kernel term, one U-Net call for
+        the batch, per-scene gradient, gather, pair term and momentum fix."""
+        B, n = pos.shape[:2]
         plan = self._plan(n)
+        self._buffers(B)
         x, G = self._x, self.grid
-        self._call("augur_field2d_scatter", pos.data_ptr(), vel.data_ptr(), mass.data_ptr(), mask.data_ptr(), n,
-                   G, self.extent, self.in_scale, x.data_ptr(), self._ws.data_ptr())
-        f4k = plan.poisson(x[0])  # the learned kernel's acceleration (kernel_acc)
-        self._call("augur_field2d_inputs", f4k.data_ptr(), field.data_ptr(), self.cf, G, x.data_ptr())
-        self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels, G,
+        f4k = []
+        for b in range(B):
+            self._call("augur_field2d_scatter", pos[b].data_ptr(), vel[b].data_ptr(), mass[b].data_ptr(),
+                       mask[b].data_ptr(), n, G, self.extent, self.in_scale, x[b].data_ptr(), self._ws.data_ptr())
+            f4k.append(plan.poisson(x[b, 0]))  # the learned kernel's acceleration (kernel_acc)
+            self._call("augur_field2d_inputs", f4k[b].data_ptr(), field[b].data_ptr(), self.cf, G, x[b].data_ptr())
+        self._call("augur_unet2d_forward", self.net.data_ptr(), self.cin, self.cf, self.width, self.levels, G, B,
                    x.data_ptr(), field_out.data_ptr(), self._wu.data_ptr(), self._wu_bytes)
-        self._call("augur_field2d_accel", field_out.data_ptr(), f4k.data_ptr(), G, self.h, self._f4a.data_ptr())
-        a_grid, _ = plan.gather(self._f4a, pos)
-        a_pair = None
-        if self.pparams is not None:
-            a_pair = plan.pair_acc(pos, mass, mask, ppe=self.ppe(), knn=self.knn, params=self.pparams, ncol=2)
-        self._call("augur_field2d_finish", a_grid.data_ptr(), _ptr(a_pair), mass.data_ptr(), mask.data_ptr(), n,
-                   int(self.momfix), acc_out.data_ptr(), self._wf.data_ptr())
+        for b in range(B):
+            self._call("augur_field2d_accel", field_out[b].data_ptr(), f4k[b].data_ptr(), G, self.h,
+                       self._f4a[b].data_ptr())
+            a_grid, _ = plan.gather(self._f4a[b], pos[b])
+            a_pair = None
+            if self.pparams is not None:
+                a_pair = plan.pair_acc(pos[b], mass[b], mask[b], ppe=self.ppe(), knn=self.knn, params=self.pparams,
+                                       ncol=2)
+            self._call("augur_field2d_finish", a_grid.data_ptr(), _ptr(a_pair), mass[b].data_ptr(),
+                       mask[b].data_ptr(), n, int(self.momfix), acc_out[b].data_ptr(), self._wf.data_ptr())
 
     def _check(self, pos, vel, mass, mask):
         if self.net is None:
@@ -156,8 +174,7 @@ class UNetScatterField:
         acc = torch.empty_like(pos)
         out = torch.empty((B, self.cf, self.grid, self.grid), device=self.device)
         field = field.to(self.device, torch.float32).contiguous()
-        for b in range(B):
-            self._force1(pos[b], vel[b], mass[b], mask[b], field[b], acc[b], out[b])
+        self._forces(pos, vel, mass, mask, field, acc, out)
         return acc, out
 
     def step(self, pos, vel, mass, mask, field):
@@ -200,6 +217,8 @@ class ChunkedTick2D:
         G, dev = model.grid, model.device
         self.field = torch.zeros(model.cf, G, G, device=dev)
         self.x = torch.zeros(model.cin, G, G, device=dev)
+        self.wu_bytes = int(model.lib.augur_unet2d_work_bytes(G, model.width, model.levels, 1))
+        self.wu = torch.empty(self.wu_bytes, dtype=torch.uint8, device=dev)
         self.f4a = torch.empty(G, G, 4, device=dev)
         self.abar = torch.zeros(2, device=dev)
         self.work = torch.empty(int(model.lib.augur_tick2d_work_bytes(G)), dtype=torch.uint8, device=dev)
@@ -229,8 +248,8 @@ class ChunkedTick2D:
         m, G = self.m, self.m.grid
         f4k = m.plan.poisson(self.x[0])
         m._call("augur_field2d_inputs", f4k.data_ptr(), self.field.data_ptr(), m.cf, G, self.x.data_ptr())
-        m._call("augur_unet2d_forward", m.net.data_ptr(), m.cin, m.cf, m.width, m.levels, G, self.x.data_ptr(),
-                self.field.data_ptr(), m._wu.data_ptr(), m._wu_bytes)
+        m._call("augur_unet2d_forward", m.net.data_ptr(), m.cin, m.cf, m.width, m.levels, G, 1, self.x.data_ptr(),
+                self.field.data_ptr(), self.wu.data_ptr(), self.wu_bytes)
         m._call("augur_field2d_accel", self.field.data_ptr(), f4k.data_ptr(), G, m.h, self.f4a.data_ptr())
         m._call("augur_tick2d_mean_acc", self.f4a.data_ptr(), self.x.data_ptr(), G, m.h * m.h / m.in_scale, self.n,
                 self.abar.data_ptr(), self.work.data_ptr())

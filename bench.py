@@ -689,6 +689,15 @@ def run_widened(args, world, rank, local):
             state["p"], state["v"], state["f"], _ = m.step(state["p"], state["v"], mass, mask, state["f"])
         ms, clk = timed(step)
         flop = 2 * 1_039_000_000 * 2  # U-Net MACs per forward (levels 5, width 32, 128^2) x 2 flop
+        # a batch of 64 small scenes (100 bodies each, the reference's training scale) in one call
+        B, nb = 64, 100
+        bst = {"p": (torch.rand(B, nb, 2, device=dev, generator=g) * 20 - 10).contiguous(),
+               "v": torch.randn(B, nb, 2, device=dev, generator=g).contiguous(), "f": m.init_field(B)}
+        bm = torch.ones(B, nb, device=dev)
+
+        def bstep():
+            bst["p"], bst["v"], bst["f"], _ = m.step(bst["p"], bst["v"], bm, bm, bst["f"])
+        bms, _ = timed(bstep)
         if rank:
             return
         print(json.dumps(_line(
@@ -700,6 +709,9 @@ def run_widened(args, world, rank, local):
             roofline={"bound": "fp32", "kernel": "U-Net (f2_conv3_kernel)", "achieved": flop / 2 / (ms * 1e-3) / 1e12,
                       "peak": fp32_peak, "unit": "TFLOP/s", "frac": flop / 2 / (ms * 1e-3) / 1e12 / fp32_peak,
                       "peak_kind": "nominal FP32; achieved counts the U-Net's flops over the whole step", "traffic": None},
+            batch64={"scenes": B, "bodies_per_scene": nb, "ms_per_step": bms,
+                     "value": world * B * nb / (bms * 1e-3), "unit": "body-steps/s",
+                     "what": "64 scenes stepped together: one U-Net launch sequence for the batch"},
             cpu_baseline=None, cpu_note="the reference's own CPU path is timed in the build container (DESIGN.md)")),
             flush=True)
         return

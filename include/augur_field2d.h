@@ -57,16 +57,18 @@ int augur_field2d_inputs(const float *force4, const float *field, int cf, int gr
  * (out, in, 3, 3); augur_unet2d_param_count gives its length. augur_unet2d_prepare rewrites it
  * once into the kernels' layout (per convolution [in][tap][32 outputs, zero-padded] then 32
  * biases; augur_unet2d_prepared_count floats, 16-byte aligned), which augur_unet2d_forward reads.
- * x (cin, G, G) -> y (cout, G, G). Needs cin <= 64, width <= 32, cout <= 32 and grid divisible
- * by 2^levels; work: augur_unet2d_work_bytes(grid, width, levels) bytes.
+ * x (batch, cin, G, G) -> y (batch, cout, G, G): the batch's scenes run in the same launches
+ * (grid z = scene). Needs cin <= 64, width <= 32, cout <= 32, batch <= 65535 and grid divisible
+ * by 2^levels; work: augur_unet2d_work_bytes(grid, width, levels, batch) bytes.
  */
 int64_t augur_unet2d_param_count(int cin, int cout, int width, int levels);
 int64_t augur_unet2d_prepared_count(int cin, int cout, int width, int levels);
 int augur_unet2d_prepare(const float *params, int cin, int cout, int width, int levels,
                          float *prepared, void *stream);
-size_t augur_unet2d_work_bytes(int grid, int width, int levels);
+size_t augur_unet2d_work_bytes(int grid, int width, int levels, int batch);
 int augur_unet2d_forward(const float *prepared, int cin, int cout, int width, int levels, int grid,
-                         const float *x, float *y, void *work, size_t work_bytes, void *stream);
+                         int batch, const float *x, float *y, void *work, size_t work_bytes,
+                         void *stream);
 
 /*
  * force4_out (G*G float4, 16-byte aligned) = (-d phi/dx + k_x, -d phi/dy + k_y, 0, 0) with
