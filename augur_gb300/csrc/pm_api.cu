@@ -1032,8 +1032,24 @@ int augur_pm_pair_acc(augur_pm_plan *p, const float *pos, const float *mass, con
   pair_search_kernel<<<blocks_for(n, 128), 128, 0, st>>>(p->pair_sorted, n, p->pair_start, p->pair_toff, a, KP,
                                                           p->pair_nbj, p->pair_nbq);
   AUGUR_LAUNCH_CHECK(p);
-  pair_weight_kernel<<<blocks_for(n * KP, 128), 128, np * sizeof(float), st>>>(
-      p->pair_sorted, pos, mass, mask, n, KP, p->pair_nbj, p->pair_nbq, params ? p->pair_params : nullptr, a, acc);
+  if (params) {
+    // the MLP's 64 x 64 layer on the tensor cores; persistent CTAs over 128-row tiles
+    static bool raised = false;
+    if (!raised) {
+      if (cudaFuncSetAttribute(pair_weight_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PTC_SMEM))
+        return AUGUR_ECUDA;
+      raised = true;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const int64_t tiles = (n * KP + PTC_M - 1) / PTC_M;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, (int64_t)std::max(1, sms) * 4);
+    pair_weight_tc_kernel<<<grid, PTC_M, PTC_SMEM, st>>>(p->pair_sorted, pos, mass, mask, n, KP, p->pair_nbj,
+                                                          p->pair_nbq, p->pair_params, a, acc, p->d_err);
+  } else {
+    pair_weight_kernel<<<blocks_for(n * KP, 128), 128, 0, st>>>(p->pair_sorted, pos, mass, mask, n, KP, p->pair_nbj,
+                                                                p->pair_nbq, nullptr, a, acc);
+  }
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -1220,6 +1236,7 @@ int augur_pm_check(augur_pm_plan *p, void *stream) {
   if (cudaMemset(p->d_err, 0, sizeof(unsigned)) != cudaSuccess) return AUGUR_ECUDA;
   if (e & AUGUR_ERRBIT_NONFINITE) return AUGUR_EIO;
   if (e & AUGUR_ERRBIT_RANGE) return AUGUR_ERANGE;
+  if (e & AUGUR_ERRBIT_TIMEOUT) return AUGUR_ETIMEDOUT;
   return AUGUR_OK;
 }
 

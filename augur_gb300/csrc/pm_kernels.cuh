@@ -12,6 +12,7 @@
 #pragma once
 
 #include "augur_common.cuh"
+#include "tcgen05.cuh"
 
 namespace augur {
 
@@ -864,7 +865,18 @@ __global__ void pair_scatter_kernel(const float *__restrict__ pos, const uint32_
   sorted[s] = make_float4(pos[2 * i], pos[2 * i + 1], 0.f, __uint_as_float((uint32_t)i));
 }
 
-__device__ __forceinline__ float pair_gelu(float t) { return 0.5f * t * (1.f + erff(t * 0.70710678118654752440f)); }
+// GELU for the pair MLP, evaluated 128 times per pair: 0.5 x erfc(-x / sqrt 2) with erfc from
+// Abramowitz & Stegun, Handbook of Mathematical Functions, eq. 7.1.26 (|erf error| <= 1.5e-7):
+// erfc(z) ~ t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-z^2), t = 1 / (1 + p z), z >= 0, and
+// 2 - erfc(z) for the other sign, so negative inputs keep their relative accuracy.
+__device__ __forceinline__ float pair_gelu_as(float x) {
+  const float z = fabsf(x) * 0.70710678118654752440f;
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+  const float poly =
+      t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
+  const float ec = poly * __expf(-z * z);  // erfc(|x| / sqrt 2)
+  return 0.5f * x * (x >= 0.f ? 2.0f - ec : ec);
+}
 
 // lower bound of the distance from coordinate x to cell c's extent along one axis (edge cells
 // extend to infinity: they hold the clamped bodies)
@@ -990,7 +1002,7 @@ __global__ void __launch_bounds__(128) pair_weight_kernel(const float4 *__restri
 #pragma unroll
         for (int e = 0; e < KMLP_MAXCOL; ++e)
           if (e < a.ncol) z += W1[o * a.ncol + e] * f[e];
-        h1[o] = pair_gelu(z);
+        h1[o] = pair_gelu_as(z);
       }
       float gsum = b3[0];
 #pragma unroll 1
@@ -1005,7 +1017,7 @@ __global__ void __launch_bounds__(128) pair_weight_kernel(const float4 *__restri
           z += wv.z * h1[4 * e + 2];
           z += wv.w * h1[4 * e + 3];
         }
-        gsum += W3[o] * pair_gelu(z);
+        gsum += W3[o] * pair_gelu_as(z);
       }
       w = gsum * win;
     }
@@ -1028,6 +1040,203 @@ __global__ void __launch_bounds__(128) pair_weight_kernel(const float4 *__restri
     acc[2 * (int64_t)i] = cx;
     acc[2 * (int64_t)i + 1] = cy;
   }
+}
+
+// Pair weights with the MLP's 64 x 64 layer on the tensor cores. A CTA of 128 threads takes
+// tiles of 128 (body, neighbour) rows: each thread builds its row's layer-1 activations h1
+// (fp32, exact GELU) and stores them split as h1 = hi + lo, two BF16 numbers; the layer is
+// D = hi W2hi^T + hi W2lo^T + lo W2hi^T (tcgen05.mma kind::f16, M = 128, N = 64, K = 64, fp32
+// accumulation in TMEM), which keeps about 16 bits of every product (the dropped lo x lo term
+// is 2^-16 relative). The epilogue reads its row back with tcgen05.ld and finishes as
+// pair_weight_kernel does. Operands are K-major without swizzle: element (row, k) of a
+// [rows x 64] operand lives at byte (k / 8) * rows * 16 + row * 16 + (k % 8) * 2.
+constexpr int PTC_M = 128, PTC_N = 64, PTC_K = 64;
+constexpr uint32_t PTC_WAIT = 1u << 20;
+constexpr size_t PTC_A_BYTES = (size_t)PTC_M * PTC_K * 2, PTC_B_BYTES = (size_t)PTC_N * PTC_K * 2;
+constexpr size_t PTC_SMEM = 2 * PTC_A_BYTES + 2 * PTC_B_BYTES +
+                            sizeof(float) * (KMLP_H * KMLP_MAXCOL + 3 * KMLP_H + 1);
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+__global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__restrict__ sorted,
+                                                               const float *__restrict__ pos,
+                                                               const float *__restrict__ mass,
+                                                               const float *__restrict__ mask, int64_t n, int KP,
+                                                               const uint32_t *__restrict__ nb_j,
+                                                               const float *__restrict__ nb_q,
+                                                               const float *__restrict__ params, PairArgs a,
+                                                               float *__restrict__ acc, unsigned *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *sAhi = smem, *sAlo = smem + PTC_A_BYTES;
+  unsigned char *sBhi = smem + 2 * PTC_A_BYTES, *sBlo = sBhi + PTC_B_BYTES;
+  float *sp = reinterpret_cast<float *>(sBlo + PTC_B_BYTES);  // W1 (64 x ncol), b1, b2, W3, b3
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ncol = a.ncol;
+  float *W1 = sp, *b1 = W1 + KMLP_H * ncol, *b2 = b1 + KMLP_H, *W3 = b2 + KMLP_H, *b3 = W3 + KMLP_H;
+  {
+    const float *gW1 = params, *gb1 = gW1 + KMLP_H * ncol, *gW2 = gb1 + KMLP_H, *gb2 = gW2 + KMLP_H * KMLP_H;
+    const float *gW3 = gb2 + KMLP_H, *gb3 = gW3 + KMLP_H;
+    for (int e = tid; e < KMLP_H * ncol; e += PTC_M) W1[e] = gW1[e];
+    for (int e = tid; e < KMLP_H; e += PTC_M) {
+      b1[e] = gb1[e];
+      b2[e] = gb2[e];
+      W3[e] = gW3[e];
+    }
+    if (tid == 0) b3[0] = gb3[0];
+    // B = W2 (n = output, k = input; torch's [out][in] is already K-major), split hi + lo
+    for (int e = tid; e < PTC_N * PTC_K / 2; e += PTC_M) {
+      const int nn = e / (PTC_K / 2), k = 2 * (e % (PTC_K / 2));
+      const float w0 = gW2[nn * PTC_K + k], w1 = gW2[nn * PTC_K + k + 1];
+      const __nv_bfloat16 h0 = __float2bfloat16_rn(w0), h1 = __float2bfloat16_rn(w1);
+      const __nv_bfloat16 l0 = __float2bfloat16_rn(w0 - __bfloat162float(h0));
+      const __nv_bfloat16 l1 = __float2bfloat16_rn(w1 - __bfloat162float(h1));
+      const size_t off = (size_t)(k / 8) * PTC_N * 16 + (size_t)nn * 16 + (k % 8) * 2;
+      *reinterpret_cast<uint32_t *>(sBhi + off) = bf16x2_bits(h0, h1);
+      *reinterpret_cast<uint32_t *>(sBlo + off) = bf16x2_bits(l0, l1);
+    }
+  }
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    s_abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, PTC_N);
+    tmem_relinquish();
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = idesc_bf16_f32(PTC_M, PTC_N);
+  const uint64_t adh = smem_desc(smem_u32(sAhi), PTC_M * 16, 128), adl = smem_desc(smem_u32(sAlo), PTC_M * 16, 128);
+  const uint64_t bdh = smem_desc(smem_u32(sBhi), PTC_N * 16, 128), bdl = smem_desc(smem_u32(sBlo), PTC_N * 16, 128);
+  const int64_t rows = n * KP, ntiles = (rows + PTC_M - 1) / PTC_M;
+  uint32_t phase = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t g_id = tile * PTC_M + tid;
+    const int64_t t = g_id / KP;
+    const bool live = g_id < rows;
+    const uint32_t j = live ? nb_j[g_id] : ~0u;
+    const float4 me = live ? sorted[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float r = 1.f, u = 1.f, win = 0.f, dx = 0.f, dy = 0.f;
+    if (j != ~0u) {
+      r = sqrtf(nb_q[g_id]);
+      dx = pos[2 * j] - me.x;
+      dy = pos[2 * j + 1] - me.y;
+      const float u0 = fminf(r * a.inv_ppe, 1.f);
+      u = u0 * u0;
+      win = (1.f - u) * (1.f - u);
+    }
+    // layer 1 + GELU for this row, split into hi / lo BF16 rows of A (zero for empty rows)
+    {
+      float f[KMLP_MAXCOL];
+      if (a.flags & 1) {
+        f[0] = r / a.h;
+        f[1] = logf(r / a.h + 0.1f);
+        f[2] = logf(0.5f / a.h);
+      } else {
+        f[0] = r;
+        f[1] = logf(r + 0.05f);
+      }
+#pragma unroll
+      for (int e = 2; e < KMLP_MAXCOL; ++e)
+        if (e >= a.nbase) f[e] = e < a.ncol ? a.extra[e - a.nbase] : 0.f;
+      const bool use = j != ~0u && win > 0.f;
+#pragma unroll
+      for (int kb = 0; kb < PTC_K / 8; ++kb) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int q2 = 0; q2 < 4; ++q2) {
+          float hv[2];
+#pragma unroll
+          for (int s2 = 0; s2 < 2; ++s2) {
+            const int o = kb * 8 + q2 * 2 + s2;
+            float z = b1[o];
+#pragma unroll
+            for (int e = 0; e < KMLP_MAXCOL; ++e)
+              if (e < ncol) z += W1[o * ncol + e] * f[e];
+            hv[s2] = use ? pair_gelu_as(z) : 0.f;
+          }
+          const __nv_bfloat16 h0 = __float2bfloat16_rn(hv[0]), h1 = __float2bfloat16_rn(hv[1]);
+          hi[q2] = bf16x2_bits(h0, h1);
+          lo[q2] = bf16x2_bits(__float2bfloat16_rn(hv[0] - __bfloat162float(h0)),
+                               __float2bfloat16_rn(hv[1] - __bfloat162float(h1)));
+        }
+        const size_t off = (size_t)kb * PTC_M * 16 + (size_t)tid * 16;
+        *reinterpret_cast<uint4 *>(sAhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4 *>(sAlo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    fence_async_smem();  // generic-proxy stores -> visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint64_t ad[3] = {adh, adh, adl}, bd[3] = {bdh, bdl, bdh};
+#pragma unroll
+      for (int pss = 0; pss < 3; ++pss)
+#pragma unroll
+        for (int kc = 0; kc < PTC_K / 16; ++kc)
+          umma_bf16(tmem, ad[pss] + (uint64_t)((2 * kc * PTC_M * 16) >> 4),
+                    bd[pss] + (uint64_t)((2 * kc * PTC_N * 16) >> 4), idesc, (pss | kc) ? 1u : 0u);
+      umma_commit(&bar);
+    }
+    bool ok = false;
+    for (uint32_t i = 0; i < PTC_WAIT && !ok; ++i) ok = mbar_try_wait(&bar, phase);
+    phase ^= 1u;
+    if (!ok) s_abort = 1;
+    tc_fence_after();
+    // layer 2's bias and GELU, then layer 3, 32 TMEM columns at a time (whole warps load)
+    float g = b3[0];
+#pragma unroll
+    for (int hh = 0; hh < PTC_N / 32; ++hh) {
+      float d[32];
+      tmem_ld32(tmem + (uint32_t)(32 * hh) + ((uint32_t)(warp * 32) << 16), d);
+#pragma unroll
+      for (int o = 0; o < 32; ++o) g += W3[32 * hh + o] * pair_gelu_as(d[o] + b2[32 * hh + o]);
+    }
+    float cx = 0.f, cy = 0.f;
+    if (j != ~0u) {
+      float w = 0.f;
+      if (win > 0.f) w = g * win;
+      if (a.flags & 2) {
+        const float qd = sqrtf(r * r + a.eps2);
+        const float q3 = qd * qd * qd;
+        const float a_mesh = -4.f * (1.f - u) * r * a.inv_ppe * a.inv_ppe / qd + (1.f - win) * r / q3;
+        w += r / q3 - a_mesh;
+      }
+      w *= mass[j] * mask[j];
+      cx = w * dx / r;
+      cy = w * dy / r;
+    }
+    for (int o = KP >> 1; o > 0; o >>= 1) {
+      cx += __shfl_xor_sync(0xffffffffu, cx, o);
+      cy += __shfl_xor_sync(0xffffffffu, cy, o);
+    }
+    if (live && (g_id & (KP - 1)) == 0) {
+      const uint32_t i = __float_as_uint(me.w);
+      acc[2 * (int64_t)i] = cx;
+      acc[2 * (int64_t)i + 1] = cy;
+    }
+    tc_fence_before();
+    __syncthreads();  // TMEM and the A rows are reused by the next tile
+    if (s_abort) break;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && s_abort) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, PTC_N);
+  }
+  (void)lane;
 }
 
 // ---------------------------------------------------------------------------------

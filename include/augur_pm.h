@@ -130,7 +130,9 @@ int augur_pm_reset_kernel(augur_pm_plan *plan, void *stream);
  * such body the knn (1..32) nearest other such bodies in the 3 x 3 cells around its own, with
  * r = sqrt(|d|^2 + 1e-8), give
  *   acc_out_i = sum_j w(r) m_j mask_j d / r,   w = g(r) (1 - u)^2 (+ prior),   u = min(r/ppe, 1)^2,
- * g = ppmlp(features(r)) in the kmlp layout of augur_pm_set_kernel_mlp (params NULL: g = 0),
+ * g = ppmlp(features(r)) in the kmlp layout of augur_pm_set_kernel_mlp (params NULL: g = 0;
+ * its 64 x 64 layer runs on the tensor cores as three BF16 products of a hi + lo split, ~2^-16
+ * relative, and its GELUs use erfc from Abramowitz & Stegun 7.1.26, |erf error| <= 1.5e-7),
  * features [r, log(r + 0.05)], or with AUGUR_KERNEL_CELL_UNITS [r/h, log(r/h + 0.1), log(0.5/h)]
  * (h = extent/grid), then the n_extra constants; AUGUR_KERNEL_PRIOR adds
  * r/q^3 - a_mesh, q = sqrt(r^2 + eps^2), a_mesh = -4 (1 - u) r / (ppe^2 q) + (1 - (1 - u)^2) r / q^3.
