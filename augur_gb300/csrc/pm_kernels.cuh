@@ -1053,8 +1053,7 @@ __global__ void __launch_bounds__(128) pair_weight_kernel(const float4 *__restri
 constexpr int PTC_M = 128, PTC_N = 64, PTC_K = 64;
 constexpr uint32_t PTC_WAIT = 1u << 20;
 constexpr size_t PTC_A_BYTES = (size_t)PTC_M * PTC_K * 2, PTC_B_BYTES = (size_t)PTC_N * PTC_K * 2;
-constexpr size_t PTC_SMEM = 2 * PTC_A_BYTES + 2 * PTC_B_BYTES +
-                            sizeof(float) * (KMLP_H * KMLP_MAXCOL + 3 * KMLP_H + 1);
+constexpr size_t PTC_SMEM = 2 * PTC_A_BYTES + 2 * PTC_B_BYTES + sizeof(float) * (4 * KMLP_H + 2 * KMLP_H + 4);
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
@@ -1071,21 +1070,32 @@ __global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__r
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sAhi = smem, *sAlo = smem + PTC_A_BYTES;
   unsigned char *sBhi = smem + 2 * PTC_A_BYTES, *sBlo = sBhi + PTC_B_BYTES;
-  float *sp = reinterpret_cast<float *>(sBlo + PTC_B_BYTES);  // W1 (64 x ncol), b1, b2, W3, b3
+  // per layer-1 output o: {W1[o][0], W1[o][1], b1[o] + the constant features' terms, 0};
+  // per layer-2 output o: {b2[o], W3[o]}; then b3
+  float4 *L1 = reinterpret_cast<float4 *>(sBlo + PTC_B_BYTES);
+  float2 *L2 = reinterpret_cast<float2 *>(L1 + KMLP_H);
+  float *b3 = reinterpret_cast<float *>(L2 + KMLP_H);
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncol = a.ncol;
-  float *W1 = sp, *b1 = W1 + KMLP_H * ncol, *b2 = b1 + KMLP_H, *W3 = b2 + KMLP_H, *b3 = W3 + KMLP_H;
   {
     const float *gW1 = params, *gb1 = gW1 + KMLP_H * ncol, *gW2 = gb1 + KMLP_H, *gb2 = gW2 + KMLP_H * KMLP_H;
     const float *gW3 = gb2 + KMLP_H, *gb3 = gW3 + KMLP_H;
-    for (int e = tid; e < KMLP_H * ncol; e += PTC_M) W1[e] = gW1[e];
-    for (int e = tid; e < KMLP_H; e += PTC_M) {
-      b1[e] = gb1[e];
-      b2[e] = gb2[e];
-      W3[e] = gW3[e];
+    // features 0 and 1 depend on r; the rest (log(0.5/h) in cell units, the extras) are constant
+    float fc[KMLP_MAXCOL];
+#pragma unroll
+    for (int e = 0; e < KMLP_MAXCOL; ++e) fc[e] = 0.f;
+    if (a.flags & 1) fc[2] = logf(0.5f / a.h);
+#pragma unroll
+    for (int e = 2; e < KMLP_MAXCOL; ++e)
+      if (e >= a.nbase && e < a.ncol) fc[e] = a.extra[e - a.nbase];
+    for (int o = tid; o < KMLP_H; o += PTC_M) {
+      float bc = gb1[o];
+      for (int e = 2; e < ncol; ++e) bc += gW1[o * ncol + e] * fc[e];
+      L1[o] = make_float4(gW1[o * ncol], gW1[o * ncol + 1], bc, 0.f);
+      L2[o] = make_float2(gb2[o], gW3[o]);
     }
     if (tid == 0) b3[0] = gb3[0];
     // B = W2 (n = output, k = input; torch's [out][in] is already K-major), split hi + lo
@@ -1136,18 +1146,8 @@ __global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__r
     }
     // layer 1 + GELU for this row, split into hi / lo BF16 rows of A (zero for empty rows)
     {
-      float f[KMLP_MAXCOL];
-      if (a.flags & 1) {
-        f[0] = r / a.h;
-        f[1] = logf(r / a.h + 0.1f);
-        f[2] = logf(0.5f / a.h);
-      } else {
-        f[0] = r;
-        f[1] = logf(r + 0.05f);
-      }
-#pragma unroll
-      for (int e = 2; e < KMLP_MAXCOL; ++e)
-        if (e >= a.nbase) f[e] = e < a.ncol ? a.extra[e - a.nbase] : 0.f;
+      const float f0 = (a.flags & 1) ? r / a.h : r;
+      const float f1 = (a.flags & 1) ? logf(r / a.h + 0.1f) : logf(r + 0.05f);
       const bool use = j != ~0u && win > 0.f;
 #pragma unroll
       for (int kb = 0; kb < PTC_K / 8; ++kb) {
@@ -1157,11 +1157,8 @@ __global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__r
           float hv[2];
 #pragma unroll
           for (int s2 = 0; s2 < 2; ++s2) {
-            const int o = kb * 8 + q2 * 2 + s2;
-            float z = b1[o];
-#pragma unroll
-            for (int e = 0; e < KMLP_MAXCOL; ++e)
-              if (e < ncol) z += W1[o * ncol + e] * f[e];
+            const float4 l1 = L1[kb * 8 + q2 * 2 + s2];
+            const float z = fmaf(l1.y, f1, fmaf(l1.x, f0, l1.z));
             hv[s2] = use ? pair_gelu_as(z) : 0.f;
           }
           const __nv_bfloat16 h0 = __float2bfloat16_rn(hv[0]), h1 = __float2bfloat16_rn(hv[1]);
@@ -1200,7 +1197,10 @@ __global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__r
       float d[32];
       tmem_ld32(tmem + (uint32_t)(32 * hh) + ((uint32_t)(warp * 32) << 16), d);
 #pragma unroll
-      for (int o = 0; o < 32; ++o) g += W3[32 * hh + o] * pair_gelu_as(d[o] + b2[32 * hh + o]);
+      for (int o = 0; o < 32; ++o) {
+        const float2 l2 = L2[32 * hh + o];
+        g = fmaf(l2.y, pair_gelu_as(d[o] + l2.x), g);
+      }
     }
     float cx = 0.f, cy = 0.f;
     if (j != ~0u) {
