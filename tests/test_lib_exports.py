@@ -80,3 +80,22 @@ def test_unet2d_param_count_matches_reference_layout(golden):
     g = golden["field2d"]
     n = sum(int(np.prod(g["w_" + k].shape)) for k in g["names"] if k.startswith("net."))
     assert _lib.load().augur_unet2d_param_count(6, 1, 32, 5) == n
+
+
+@pytest.mark.parametrize("lang", ("c", "c++"))
+def test_headers_compile_as_c_and_cxx(tmp_path, lang):
+    """include/*.h is the C ABI a C, C++ or FFI caller binds: every header compiles on its own
+    as C99 and as C++17 (no torch or CUDA types in the signatures)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip(f"no {lang} compiler")
+    heads = sorted(p.name for p in (ROOT / "include").glob("*.h"))
+    src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    src.write_text("".join(f'#include "{h}"\n' for h in heads) + "int main(void) { return 0; }\n")
+    std = ["-std=c99", "-pedantic"] if lang == "c" else ["-std=c++17"]
+    r = subprocess.run([cc, *std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
