@@ -31,7 +31,7 @@ def _ptr(t):
 class UNetScatterField:
     def __init__(self, grid: int = 128, extent: float = 64.0, dt: float = 0.1, width: int = 32, levels: int = 5,
                  pp: float = 2.0, knn: int = 16, split: bool = True, momfix: bool = True, in_scale: float = 1.0,
-                 eps: float = 0.5, device=None):
+                 eps: float = 0.5, device=None, graph: bool = False):
         self.lib = _lib.load()
         self.grid, self.extent, self.h = int(grid), float(extent), float(extent) / int(grid)
         self.dt, self.width, self.levels = float(dt), int(width), int(levels)
@@ -49,6 +49,10 @@ class UNetScatterField:
         self._wf = torch.empty(int(self.lib.augur_field2d_finish_work_bytes()), dtype=torch.uint8, device=dev)
         self._batch = 0
         self._buffers(1)
+        # graph=True: Verlet steps with a previous acceleration are captured once per input shape
+        # in a CUDA graph and replayed (the reference's "graph" option, scripts/scatter_field.py:567-589)
+        self.graph = bool(graph)
+        self._graphs: dict = {}
 
     def _buffers(self, B: int) -> None:
         """Per-batch buffers: input stacks (B, 6, G, G), acceleration grids (B, G, G, 4), U-Net work."""
@@ -180,6 +184,36 @@ class UNetScatterField:
     def step(self, pos, vel, mass, mask, field):
         """One velocity-Verlet step, ScatterField._step (:677-688): field = (potential, a_prev)."""
         self._check(pos, vel, mass, mask)
+        if self.graph and field[1] is not None and not torch.cuda.is_current_stream_capturing():
+            return self._graphed_step(pos, vel, mass, mask, field)
+        return self._step(pos, vel, mass, mask, field)
+
+    def _graphed_step(self, pos, vel, mass, mask, field):
+        f, a_prev = field
+        args = (pos, vel, mass, mask, f.to(self.device, torch.float32).contiguous(), a_prev.contiguous())
+        key = tuple((tuple(t.shape), t.dtype) for t in args)
+        ent = self._graphs.get(key)
+        if ent is None:
+            static = [t.clone() for t in args]
+            cur = torch.cuda.current_stream(self.device)
+            side = torch.cuda.Stream(self.device)
+            side.wait_stream(cur)
+            with torch.cuda.stream(side):  # warm-up: plan growth, scratch allocation, attribute opt-ins
+                for _ in range(2):
+                    self._step(*static[:4], (static[4], static[5]))
+            cur.wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                out = self._step(*static[:4], (static[4], static[5]))
+            ent = self._graphs[key] = (g, static, out)
+        g, static, out = ent
+        for dst, src in zip(static, args):
+            dst.copy_(src)
+        g.replay()
+        p, v, (fo, a), dv = out
+        return p.clone(), v.clone(), (fo.clone(), a.clone()), dv.clone()
+
+    def _step(self, pos, vel, mass, mask, field):
         f, a_prev = field
         if a_prev is None:
             a_prev, f = self.force(pos, vel, mass, mask, f)

@@ -701,6 +701,15 @@ def run_widened(args, world, rank, local):
         def bstep():
             bst["p"], bst["v"], bst["f"], _ = m.step(bst["p"], bst["v"], bm, bm, bst["f"])
         bms, _ = timed(bstep)
+        # the same batch with the step captured in a CUDA graph (graph=True)
+        mg = UNetScatterField(device=dev, graph=True)
+        mg.load_state_dict(seeded_field2d_state())
+        gst = {"p": bst["p"].clone(), "v": bst["v"].clone(), "f": mg.init_field(B)}
+
+        def gstep():
+            gst["p"], gst["v"], gst["f"], _ = mg.step(gst["p"], gst["v"], bm, bm, gst["f"])
+        gstep()  # the first step computes a_prev eagerly; the next ones replay the graph
+        gms, _ = timed(gstep)
         if rank:
             return
         print(json.dumps(_line(
@@ -714,7 +723,8 @@ def run_widened(args, world, rank, local):
                       "peak_kind": "nominal FP32; achieved counts the U-Net's flops over the whole step", "traffic": None},
             batch64={"scenes": B, "bodies_per_scene": nb, "ms_per_step": bms,
                      "value": world * B * nb / (bms * 1e-3), "unit": "body-steps/s",
-                     "what": "64 scenes stepped together: one U-Net launch sequence for the batch"},
+                     "what": "64 scenes stepped together: one U-Net launch sequence for the batch",
+                     "graph_ms_per_step": gms, "graph_value": world * B * nb / (gms * 1e-3)},
             cpu_baseline=None, cpu_note="the reference's own CPU path is timed in the build container (DESIGN.md)")),
             flush=True)
         return

@@ -91,3 +91,26 @@ def test_batch_equals_scenes(golden, model):
                              mask[b:b + 1].contiguous(), f0[b:b + 1])
         assert torch.equal(acc[b], a1[0]) and torch.equal(field[b], f1[0])
     assert torch.all(acc[1, 3] == 0)
+
+
+def test_graphed_steps_equal_eager_steps(golden):
+    """graph=True (the reference's "graph" option) captures the Verlet step once per shape and
+    replays it: the trajectory is the eager one bit for bit."""
+    g = golden["field2d"]
+    sd = {k: g["w_" + k].astype(np.float32) for k in g["names"]}
+    eager = UNetScatterField(device=DEV)
+    eager.load_state_dict(sd)
+    graphed = UNetScatterField(device=DEV, graph=True)
+    graphed.load_state_dict(sd)
+    p, v, m, k = _scene(g, 30)
+    pos, vel = torch.cat([p, p * 0.8]).contiguous(), torch.cat([v, -v]).contiguous()
+    mass, mask = torch.cat([m, m]).contiguous(), torch.cat([k, k]).contiguous()
+    s1 = (pos, vel, eager.init_field(2))
+    s2 = (pos.clone(), vel.clone(), graphed.init_field(2))
+    for _ in range(4):
+        a = eager.step(s1[0], s1[1], mass, mask, s1[2])
+        b = graphed.step(s2[0], s2[1], mass, mask, s2[2])
+        s1, s2 = (a[0], a[1], a[2]), (b[0], b[1], b[2])
+        assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
+        assert torch.equal(a[2][0], b[2][0]) and torch.equal(a[2][1], b[2][1])
+    assert len(graphed._graphs) == 1
