@@ -152,12 +152,69 @@ def cpu_baseline_run(n, G, dt, budget_s=20.0):
             "s_per_step": t1 / steps}
 
 
+def run_reference_widened(args, world):
+    """CPU reference arm of the widened workloads: the oracle's float64 restatement of the
+    reference's pair term, 2D model and large-N tick (oracle/pm_oracle.py, oracle/field2d_oracle.py)
+    on a bounded sample of the same workload, single-threaded numpy."""
+    from oracle import field2d_oracle as F
+    from oracle import pm_oracle as O
+
+    rng = np.random.default_rng(9100)
+    sd = {k: v.numpy().astype(np.float64) for k, v in seeded_field2d_state().items()}
+    t0 = time.time()
+    if args.workload == "pair":
+        n, q = args.bodies, 50
+        pos = rng.normal(0.0, 10.7, (n, 2))
+        params = np.concatenate([sd[f"ppmlp.{i}.{w}"].reshape(-1) for i in (0, 2, 4) for w in ("weight", "bias")])
+        params[-65:] = np.linspace(-0.2, 0.2, 65)
+        idx = np.arange(0, n, n // q)[:q]
+        O.pair_acc_2d(pos, np.ones(n), np.ones(n), params, 2, [], 0, 0.5, 0.5, 0.5, 16, queries=idx)
+        dt_s = time.time() - t0
+        value, unit, sample = q / dt_s, "bodies/s", f"{q} query bodies of the {n}-body scene (brute-force top-knn)"
+        metric = "pair-term bodies/s (knn 16, pair-weight MLP), 1e6 Gaussian bodies"
+    elif args.workload == "field2d":
+        n = args.bodies
+        m = F.Model2D(sd)
+        pos, vel = rng.uniform(-20, 20, (n, 2)), rng.normal(0, 1, (n, 2))
+        one = np.ones(n)
+        state = (np.zeros((1, 128, 128)), None)
+        pos, vel, state, _ = m.step(pos, vel, one, one, state)  # the first step computes a_prev
+        t0 = time.time()
+        m.step(pos, vel, one, one, state)
+        dt_s = time.time() - t0
+        value, unit, sample = n / dt_s, "body-steps/s", f"one Verlet step of the {n}-body scene"
+        metric = "body-steps/s of the production 2D model (U-Net, kernel and pair terms, Verlet)"
+    else:
+        n = 100_000
+        m = F.Model2D(sd, pair=False)
+        sim = F.Tick2D(m, n, c=10.0, dt=0.1, state_dtype=np.float16)
+        pos = np.clip(rng.normal(0, 8.0, (n, 2)), -29, 29).astype(np.float16)
+        mom = rng.normal(0, 3.0, (n, 2)).astype(np.float16)
+        pos, mom = sim.init_kick(pos, mom)
+        t0 = time.time()
+        sim.tick(pos, mom)
+        dt_s = time.time() - t0
+        value, unit, sample = n / dt_s, "body-ticks/s", f"one tick of a {n}-body sample of the scene, fp16 state"
+        metric = "body-ticks/s, 1e9-body 2D scene, fp16 state (chunked large-N tick)"
+    cb = {"value": value, "unit": unit, "cores": 1, "kind": "port",
+          "sample": sample + " (oracle float64 numpy restatement of the reference)"}
+    print(json.dumps({"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
+                      "steps": 1, "warmup": 0, "ms_per_step": dt_s * 1e3, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": args.workload, "bodies": args.bodies}, "cpu_baseline": cb,
+                      "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
+    if args.workload in ("pair", "field2d", "tick1e9"):
+        run_reference_widened(args, world)
+        return
     if args.workload != "pm":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm times the default 3M-body "
-                                                              "workload only"}), flush=True)
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm times the single-scene "
+                                                              "workloads only"}), flush=True)
         return
     n, G = args.bodies, args.grid
     cb = cpu_baseline_run(n, G, args.dt, budget_s=max(5.0, 60.0 / max(1, args.steps)))
