@@ -7,7 +7,7 @@ scripts/pm_baseline_force_error.py:88-92, turned into a training target). The ne
 the CIC density and PM potential grids and outputs a 3-channel correction field that is
 CIC-gathered at the bodies and added to the PM force.
 
-Plain PM is the fallback and the judge: FallbackMonitor reverts a scene to plain PM when its
+Plain PM is the fallback and the yardstick: FallbackMonitor reverts a scene to plain PM when its
 relative energy drift exceeds 5% or the predicted correction grows beyond a fraction of the
 PM force (the reference's energy drift diagnostic, scripts/scatter_field.py:759-765, :874).
 """
