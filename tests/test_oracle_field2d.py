@@ -63,3 +63,19 @@ def test_oracle_tick(golden, weights):
     for t in range(int(g["ticks"])):
         pos, mom = sim.tick(pos, mom)
         assert rel(pos, g["f32_pos"][t]) < 1e-5 and rel(mom, g["f32_mom"][t]) < 1e-5, t
+
+
+def test_oracle_tick_fp16_state(golden, weights):
+    """float16 state: the oracle rounds to float16 where the reference stores (pos after the drift,
+    momentum after the kick); most stored values are the reference's own."""
+    g = golden["tick2d"]
+    n = int(g["n"])
+    sim = F.Tick2D(F.Model2D(weights, pair=False), n, c=float(g["c"]), dt=float(g["dt"]), state_dtype=np.float16)
+    pos, mom = g["f16_pos0"].copy(), g["f16_mom0"].copy()
+    pos, mom = sim.init_kick(pos, mom)
+    assert np.mean(mom == g["f16_mom_ik"]) > 0.85
+    for t in range(int(g["ticks"])):
+        pos, mom = sim.tick(pos, mom)
+        for a, b in ((pos, g["f16_pos"][t]), (mom, g["f16_mom"][t])):
+            assert np.mean(a == b) > 0.85, t
+            assert rel(a, b) < 5e-4, t
