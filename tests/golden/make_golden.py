@@ -156,12 +156,13 @@ def kernel_acc_cases():
 
 def pair_acc_cases():
     """ScatterField.pp_acc (pair term: k nearest neighbours, windowed learned weight and prior,
-    scripts/scatter_field.py:291-300, 324-364, 500-521) with seeded ppmlp weights: dense mode
-    (N <= 512) and the cell-list mode, plain and cell-unit features."""
+    scripts/scatter_field.py:291-300, 324-471, 500-521) with seeded ppmlp weights: dense mode
+    (N <= 512), the cell-list mode (plain and cell-unit features) and the adaptive multilevel mode."""
     cases = [
         dict(name="dense", n=300, cu=False, cell=False, prior=True, epsin=False),
         dict(name="cell", n=3000, cu=False, cell=True, prior=True, epsin=False),
         dict(name="cell_cu", n=3000, cu=True, cell=True, prior=False, epsin=True),
+        dict(name="adapt", n=3000, cu=False, cell=False, prior=True, epsin=False, adapt=True),
     ]
     out = {}
     for i, c in enumerate(cases):
@@ -170,6 +171,8 @@ def pair_acc_cases():
                             cu=c["cu"], epsin=c["epsin"])
         if c["cell"]:
             m.opt = {"cell"}
+        if c.get("adapt"):
+            m.opt = {"adapt"}  # the adaptive multilevel cell list (pp_acc_adapt, :366-471)
         m.eps_cur = 0.8
         g = torch.Generator().manual_seed(9200 + i)
         with torch.no_grad():  # the output layer starts at zero: give it seeded values

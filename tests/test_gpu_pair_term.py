@@ -1,5 +1,6 @@
 """The pair term (ScatterField.pp_acc, scripts/scatter_field.py:291-300, 324-364, 500-521) on the
-GPU against the reference's own outputs (tests/golden/pair_acc.npz: dense and cell-list modes) and
+GPU against the reference's own outputs (tests/golden/pair_acc.npz: dense, cell-list and adaptive
+multilevel modes) and
 the oracle's float64 brute-force top-knn, plus the edge cases of its cell list: masked bodies,
 bodies outside the box (clamped cells), fewer than knn neighbours, a pair radius small enough
 that the cells are coarsened, and order independence."""
@@ -12,7 +13,7 @@ from oracle import pm_oracle as O
 
 pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda:0")
-CASES = ("dense", "cell", "cell_cu")
+CASES = ("dense", "cell", "cell_cu", "adapt")
 TOL = 1e-4  # fp32 distances, features and MLP against float64 / the reference's fp32
 
 

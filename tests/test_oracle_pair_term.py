@@ -1,12 +1,12 @@
 """The oracle's restatement of the pair term (ScatterField.pp_acc, scripts/scatter_field.py:291-300,
-324-364, 500-521) against the reference's own outputs (tests/golden/pair_acc.npz: dense mode and the
-cell-list mode, plain and cell-unit features). No GPU."""
+324-471, 500-521) against the reference's own outputs (tests/golden/pair_acc.npz: dense mode, the
+cell-list mode with plain and cell-unit features, and the adaptive multilevel mode). No GPU."""
 import numpy as np
 import pytest
 
 from oracle import pm_oracle as O
 
-CASES = ("dense", "cell", "cell_cu")
+CASES = ("dense", "cell", "cell_cu", "adapt")
 
 
 def _case(golden, case):
