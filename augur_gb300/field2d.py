@@ -31,12 +31,16 @@ def _ptr(t):
 class UNetScatterField:
     def __init__(self, grid: int = 128, extent: float = 64.0, dt: float = 0.1, width: int = 32, levels: int = 5,
                  pp: float = 2.0, knn: int = 16, split: bool = True, momfix: bool = True, in_scale: float = 1.0,
-                 eps: float = 0.5, device=None, graph: bool = False):
+                 eps: float = 0.5, device=None, graph: bool = False, prior: bool = False, cu: bool = False):
         self.lib = _lib.load()
         self.grid, self.extent, self.h = int(grid), float(extent), float(extent) / int(grid)
         self.dt, self.width, self.levels = float(dt), int(width), int(levels)
         self.pp, self.knn, self.split, self.momfix = float(pp), int(knn), bool(split), bool(momfix)
         self.in_scale, self.eps = float(in_scale), float(eps)
+        # variants: prior (kernel -(1 + K)/sqrt(r^2 + eps^2) and the pair prior) and cell units (cu:
+        # features in units of h, ppe = pp h / 0.5), scripts/scatter_field.py:138-151, 263-300
+        self.prior, self.cu = bool(prior), bool(cu)
+        self.ncol = 3 if self.cu else 2
         self.cf, self.cin = 1, 6  # potential field; inputs [m, m vx, m vy, k_x, k_y, field]
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         if self.grid % (1 << self.levels):
@@ -67,7 +71,7 @@ class UNetScatterField:
 
     # ---- parameters ------------------------------------------------------------------------
     def ppe(self) -> float:
-        return self.pp
+        return self.pp * self.h / 0.5 if self.cu else self.pp
 
     def load_state_dict(self, sd: dict) -> None:
         """Parameters under the reference's names (ppmlp.*, kmlp.*, net.*), any float dtype/device."""
@@ -98,7 +102,8 @@ class UNetScatterField:
                 self.plan.close()
             self.plan = PMPlan(2, self.grid, max(int(n), 1), "isolated", self.extent, eps=self.eps, device=self.device)
             if self.kparams is not None:
-                self.plan.set_kernel_mlp(self.kparams, 2, split=self.split, split_radius=self.ppe())
+                self.plan.set_kernel_mlp(self.kparams, self.ncol, cell_units=self.cu, prior=self.prior,
+                                         split=self.split, split_radius=self.ppe(), eps=self.eps)
         return self.plan
 
     def close(self) -> None:
@@ -157,7 +162,7 @@ class UNetScatterField:
             a_pair = None
             if self.pparams is not None:
                 a_pair = plan.pair_acc(pos[b], mass[b], mask[b], ppe=self.ppe(), knn=self.knn, params=self.pparams,
-                                       ncol=2)
+                                       ncol=self.ncol, cell_units=self.cu, prior=self.prior, eps=self.eps)
             self._call("augur_field2d_finish", a_grid.data_ptr(), _ptr(a_pair), mass[b].data_ptr(),
                        mask[b].data_ptr(), n, int(self.momfix), acc_out[b].data_ptr(), self._wf.data_ptr())
 

@@ -126,15 +126,18 @@ class Model2D:
     the split window at ppe = pp, zero kpad, pair term (dense top-knn), momentum fix, Verlet."""
 
     def __init__(self, sd, grid=128, extent=64.0, dt=0.1, pp=2.0, knn=16, eps=0.5, in_scale=1.0, levels=5,
-                 pair=True):
+                 pair=True, prior=False, cu=False):
         self.sd = {k: np.asarray(v, np.float64) for k, v in sd.items()}
         self.G, self.E, self.h, self.dt, self.pp, self.knn, self.eps = grid, extent, extent / grid, dt, pp, knn, eps
-        self.in_scale, self.levels, self.pair = in_scale, levels, pair
+        self.in_scale, self.levels, self.pair, self.prior, self.cu = in_scale, levels, pair, prior, cu
+        self.ncol = 3 if cu else 2
+        self.ppe = pp * self.h / 0.5 if cu else pp  # ScatterField.ppe (:138-139)
         self.kparams, self.pparams = _mlp_params(sd, "kmlp"), _mlp_params(sd, "ppmlp")
 
     def kernel_acc(self, rho):
-        """kernel_acc (:274-289): (2, G, G)."""
-        a = O.kernel_acc_2d(rho, self.kparams, 2, [], 4, self.pp, self.eps, self.E)
+        """kernel_acc (:274-289): (2, G, G); split window at ppe, optional prior and cell units."""
+        flags = 4 | (1 if self.cu else 0) | (2 if self.prior else 0)
+        a = O.kernel_acc_2d(rho, self.kparams, self.ncol, [], flags, self.ppe, self.eps, self.E)
         return np.moveaxis(a, -1, 0)
 
     def grid_force(self, x, field):
@@ -149,7 +152,9 @@ class Model2D:
         acc, field = self.grid_force(x, field)
         a = gather(acc, pos, self.E)
         if self.pair:
-            a = a + O.pair_acc_2d(pos, mass, mask, self.pparams, 2, [], 0, self.pp, self.eps, self.h, self.knn)
+            flags = (1 if self.cu else 0) | (2 if self.prior else 0)
+            a = a + O.pair_acc_2d(pos, mass, mask, self.pparams, self.ncol, [], flags, self.ppe, self.eps, self.h,
+                                  self.knn)
         mm = (np.asarray(mass, np.float64) * np.asarray(mask, np.float64))[:, None]
         a = a - (mm * a).sum(0, keepdims=True) / max(mm.sum(), 1e-9)
         return a * np.asarray(mask, np.float64)[:, None], field

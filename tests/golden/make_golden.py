@@ -272,6 +272,48 @@ def field2d_cases():
     np.savez_compressed(OUT / "field2d.npz", **out)
 
 
+def field2d_variant_cases():
+    """The production 2D model's prior + cell-unit variant (ScatterField(..., prior=True, cu=True),
+    the reference's ms_kp_pot_v_g128_prior / _cu family) at grid 64 (U-Net levels 4, width 16), in
+    float64 with seeded float16-exact weights: one force and two Verlet steps of 60 bodies."""
+    torch.manual_seed(4739)
+    m = sf.ScatterField(grid=64, extent=64.0, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
+                        potential=True, verlet=True, prior=True, cu=True, width=16)
+    g = torch.Generator().manual_seed(9400)
+    with torch.no_grad():
+        for mlp in (m.ppmlp, m.kmlp):
+            mlp[-1].weight.copy_(torch.randn(mlp[-1].weight.shape, generator=g) * 0.3)
+            mlp[-1].bias.copy_(torch.randn(1, generator=g) * 0.3)
+        m.net.out.weight.copy_(torch.randn(m.net.out.weight.shape, generator=g) * 1.0)
+        m.net.out.bias.copy_(torch.randn(1, generator=g) * 0.05)
+        for t in m.parameters():
+            t.copy_(t.half().float())
+    m = m.double().eval()
+    out = {"names": np.array([k for k, _ in m.named_parameters()]), "steps": np.int32(2),
+           "levels": np.int32(m.net.levels), "width": np.int32(16), "grid": np.int32(64)}
+    for k, t in m.named_parameters():
+        out["w_" + k] = t.detach().numpy().astype(np.float16)
+    rng = np.random.default_rng(4739)
+    n = 60
+    p0 = rng.uniform(-12.0, 12.0, (n, 2)).astype(np.float32)
+    v0 = rng.normal(0.0, 0.5, (n, 2))
+    v0 = (v0 - v0.mean(0)).astype(np.float32)
+    pos, vel = torch.tensor(p0, dtype=torch.float64)[None], torch.tensor(v0, dtype=torch.float64)[None]
+    mass, mask = torch.ones(1, n, dtype=torch.float64), torch.ones(1, n, dtype=torch.float64)
+    out["pos0"], out["vel0"] = p0, v0
+    with torch.no_grad():
+        field = m.init_field(1, "cpu", torch.float64)
+        a0, f1 = m.force(pos, vel, mass, mask, field[0])
+        out["acc0"], out["field1"] = a0[0].numpy(), f1[0, 0].numpy().astype(np.float32)
+        ps, vs = [], []
+        for _ in range(2):
+            pos, vel, field, _ = m.step(pos, vel, mass, mask, field)
+            ps.append(pos[0].numpy())
+            vs.append(vel[0].numpy())
+        out["pos"], out["vel"] = np.stack(ps), np.stack(vs)
+    np.savez_compressed(OUT / "field2d_variant.npz", **out)
+
+
 def tick2d_cases():
     """The reference's chunked large-N tick (scripts/scatter_bh_1b.py: make_ic :66-104, Sim
     :107-146) on the CPU: the production 2D model without its pair term (ops.no_pp), relativistic
@@ -314,7 +356,7 @@ def tick2d_cases():
 
 CASES = {"cell_index": cell_index_cases, "scatter_gather": scatter_gather_cases, "pm_acc": pm_acc_cases,
          "exact_acc": exact_acc_cases, "kernel_acc": kernel_acc_cases, "pair_acc": pair_acc_cases,
-         "field2d": field2d_cases, "tick2d": tick2d_cases}
+         "field2d": field2d_cases, "tick2d": tick2d_cases, "field2d_variant": field2d_variant_cases}
 
 if __name__ == "__main__":
     for name in (sys.argv[1:] or list(CASES)):

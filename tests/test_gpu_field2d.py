@@ -114,3 +114,23 @@ def test_graphed_steps_equal_eager_steps(golden):
         assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
         assert torch.equal(a[2][0], b[2][0]) and torch.equal(a[2][1], b[2][1])
     assert len(graphed._graphs) == 1
+
+
+def test_prior_cell_unit_variant_matches_reference(golden):
+    """ScatterField(..., prior=True, cu=True) at grid 64 (U-Net levels 4, width 16): one force and
+    two Verlet steps against the reference in float64 (tests/golden/field2d_variant.npz)."""
+    g = golden["field2d_variant"]
+    m = UNetScatterField(grid=64, extent=64.0, dt=0.1, width=int(g["width"]), levels=int(g["levels"]), pp=2.0,
+                         prior=True, cu=True, device=DEV)
+    m.load_state_dict({k: g["w_" + k].astype(np.float32) for k in g["names"]})
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=DEV)[None]
+    n = len(g["pos0"])
+    pos, vel, one = t(g["pos0"]), t(g["vel0"]), torch.ones(1, n, device=DEV)
+    acc, field = m.force(pos, vel, one, one, torch.zeros(1, 1, 64, 64, device=DEV))
+    assert rel(acc[0].cpu().numpy(), g["acc0"]) < 1e-4
+    assert rel(field[0, 0].cpu().numpy(), g["field1"]) < 1e-5
+    state = m.init_field(1)
+    for s in range(int(g["steps"])):
+        pos, vel, state, _ = m.step(pos, vel, one, one, state)
+        assert np.abs(pos[0].cpu().numpy() - g["pos"][s]).max() < 1e-4
+        assert np.abs(vel[0].cpu().numpy() - g["vel"][s]).max() < 1e-4

@@ -79,3 +79,19 @@ def test_oracle_tick_fp16_state(golden, weights):
         for a, b in ((pos, g["f16_pos"][t]), (mom, g["f16_mom"][t])):
             assert np.mean(a == b) > 0.85, t
             assert rel(a, b) < 5e-4, t
+
+
+def test_oracle_prior_cell_unit_variant(golden):
+    """The prior + cell-unit variant (grid 64, U-Net levels 4, width 16) against the reference."""
+    g = golden["field2d_variant"]
+    sd = {k: g["w_" + k].astype(np.float64) for k in g["names"]}
+    m = F.Model2D(sd, grid=64, extent=64.0, levels=int(g["levels"]), prior=True, cu=True)
+    pos, vel = g["pos0"].astype(np.float64), g["vel0"].astype(np.float64)
+    one = np.ones(len(pos))
+    a, f = m.force(pos, vel, one, one, np.zeros((1, 64, 64)))
+    assert rel(a, g["acc0"]) < 1e-9
+    assert rel(f[0], g["field1"]) < 1e-6
+    state = (np.zeros((1, 64, 64)), None)
+    for t in range(int(g["steps"])):
+        pos, vel, state, _ = m.step(pos, vel, one, one, state)
+        assert np.abs(pos - g["pos"][t]).max() < 1e-9 and np.abs(vel - g["vel"][t]).max() < 1e-9
