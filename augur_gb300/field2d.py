@@ -31,7 +31,8 @@ def _ptr(t):
 class UNetScatterField:
     def __init__(self, grid: int = 128, extent: float = 64.0, dt: float = 0.1, width: int = 32, levels: int = 5,
                  pp: float = 2.0, knn: int = 16, split: bool = True, momfix: bool = True, in_scale: float = 1.0,
-                 eps: float = 0.5, device=None, graph: bool = False, prior: bool = False, cu: bool = False):
+                 eps: float = 0.5, device=None, graph: bool = False, prior: bool = False, cu: bool = False,
+                 kpad: str = "zero"):
         self.lib = _lib.load()
         self.grid, self.extent, self.h = int(grid), float(extent), float(extent) / int(grid)
         self.dt, self.width, self.levels = float(dt), int(width), int(levels)
@@ -40,6 +41,9 @@ class UNetScatterField:
         # variants: prior (kernel -(1 + K)/sqrt(r^2 + eps^2) and the pair prior) and cell units (cu:
         # features in units of h, ppe = pp h / 0.5), scripts/scatter_field.py:138-151, 263-300
         self.prior, self.cu = bool(prior), bool(cu)
+        if kpad not in ("zero", "ext"):
+            raise ValueError("kpad: 'zero' or 'ext'")
+        self.kpad = kpad  # "ext": the kernel potential's central difference reads one cell beyond the grid
         self.ncol = 3 if self.cu else 2
         self.cf, self.cin = 1, 6  # potential field; inputs [m, m vx, m vy, k_x, k_y, field]
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
@@ -103,7 +107,8 @@ class UNetScatterField:
             self.plan = PMPlan(2, self.grid, max(int(n), 1), "isolated", self.extent, eps=self.eps, device=self.device)
             if self.kparams is not None:
                 self.plan.set_kernel_mlp(self.kparams, self.ncol, cell_units=self.cu, prior=self.prior,
-                                         split=self.split, split_radius=self.ppe(), eps=self.eps)
+                                         split=self.split, split_radius=self.ppe(), eps=self.eps,
+                                         pad_ext=self.kpad == "ext")
         return self.plan
 
     def close(self) -> None:

@@ -126,17 +126,18 @@ class Model2D:
     the split window at ppe = pp, zero kpad, pair term (dense top-knn), momentum fix, Verlet."""
 
     def __init__(self, sd, grid=128, extent=64.0, dt=0.1, pp=2.0, knn=16, eps=0.5, in_scale=1.0, levels=5,
-                 pair=True, prior=False, cu=False):
+                 pair=True, prior=False, cu=False, kpad="zero"):
         self.sd = {k: np.asarray(v, np.float64) for k, v in sd.items()}
         self.G, self.E, self.h, self.dt, self.pp, self.knn, self.eps = grid, extent, extent / grid, dt, pp, knn, eps
         self.in_scale, self.levels, self.pair, self.prior, self.cu = in_scale, levels, pair, prior, cu
         self.ncol = 3 if cu else 2
+        self.kpad = kpad
         self.ppe = pp * self.h / 0.5 if cu else pp  # ScatterField.ppe (:138-139)
         self.kparams, self.pparams = _mlp_params(sd, "kmlp"), _mlp_params(sd, "ppmlp")
 
     def kernel_acc(self, rho):
         """kernel_acc (:274-289): (2, G, G); split window at ppe, optional prior and cell units."""
-        flags = 4 | (1 if self.cu else 0) | (2 if self.prior else 0)
+        flags = 4 | (1 if self.cu else 0) | (2 if self.prior else 0) | (8 if self.kpad == "ext" else 0)
         a = O.kernel_acc_2d(rho, self.kparams, self.ncol, [], flags, self.ppe, self.eps, self.E)
         return np.moveaxis(a, -1, 0)
 

@@ -274,11 +274,13 @@ def field2d_cases():
 
 def field2d_variant_cases():
     """The production 2D model's prior + cell-unit variant (ScatterField(..., prior=True, cu=True),
-    the reference's ms_kp_pot_v_g128_prior / _cu family) at grid 64 (U-Net levels 4, width 16), in
-    float64 with seeded float16-exact weights: one force and two Verlet steps of 60 bodies."""
+    the reference's ms_kp_pot_v_g128_prior / _cu family) with kpad = "ext" (the large-N driver's
+    option) at grid 64 (U-Net levels 4, width 16), in float64 with seeded float16-exact weights:
+    one force and two Verlet steps of 60 bodies."""
     torch.manual_seed(4739)
     m = sf.ScatterField(grid=64, extent=64.0, net="unet", dt=0.1, kernel=True, pp=2.0, split=True,
                         potential=True, verlet=True, prior=True, cu=True, width=16)
+    m.kpad = "ext"
     g = torch.Generator().manual_seed(9400)
     with torch.no_grad():
         for mlp in (m.ppmlp, m.kmlp):

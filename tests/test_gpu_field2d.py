@@ -117,11 +117,11 @@ def test_graphed_steps_equal_eager_steps(golden):
 
 
 def test_prior_cell_unit_variant_matches_reference(golden):
-    """ScatterField(..., prior=True, cu=True) at grid 64 (U-Net levels 4, width 16): one force and
+    """ScatterField(..., prior=True, cu=True), kpad "ext", at grid 64 (U-Net levels 4, width 16): one force and
     two Verlet steps against the reference in float64 (tests/golden/field2d_variant.npz)."""
     g = golden["field2d_variant"]
     m = UNetScatterField(grid=64, extent=64.0, dt=0.1, width=int(g["width"]), levels=int(g["levels"]), pp=2.0,
-                         prior=True, cu=True, device=DEV)
+                         prior=True, cu=True, kpad="ext", device=DEV)
     m.load_state_dict({k: g["w_" + k].astype(np.float32) for k in g["names"]})
     t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32, device=DEV)[None]
     n = len(g["pos0"])

@@ -82,10 +82,10 @@ def test_oracle_tick_fp16_state(golden, weights):
 
 
 def test_oracle_prior_cell_unit_variant(golden):
-    """The prior + cell-unit variant (grid 64, U-Net levels 4, width 16) against the reference."""
+    """The prior + cell-unit variant with kpad "ext" (grid 64, U-Net levels 4, width 16) against the reference."""
     g = golden["field2d_variant"]
     sd = {k: g["w_" + k].astype(np.float64) for k in g["names"]}
-    m = F.Model2D(sd, grid=64, extent=64.0, levels=int(g["levels"]), prior=True, cu=True)
+    m = F.Model2D(sd, grid=64, extent=64.0, levels=int(g["levels"]), prior=True, cu=True, kpad="ext")
     pos, vel = g["pos0"].astype(np.float64), g["vel0"].astype(np.float64)
     one = np.ones(len(pos))
     a, f = m.force(pos, vel, one, one, np.zeros((1, 64, 64)))
