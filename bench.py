@@ -7,6 +7,11 @@ synthetic) are resident in HBM before the timed region; the per-step working set
 (~1.5 GB of traffic over ~0.8 GB of buffers) is larger than the 129 MB L2, so no flush.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload pm|batch64|pm1e9|pair|field2d|tick1e9]
+
+The default workload is the one above; --workload batch64 steps 64 uneven scenes in one CUDA
+graph, pm1e9 one 10^9-body scene on 1024^3, and pair / field2d / tick1e9 time the pair term,
+the production 2D model and its 10^9-body fp16-state tick.
 
 Prints one JSON line (rank 0). Under torchrun each rank runs an independent replica
 (scenes are independent; the PM step has no inter-GPU exchange) and value is the
