@@ -11,6 +11,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "../../include/augur_pm.h"
 
 #define AUGUR_ERRBIT_NONFINITE 1u
@@ -18,6 +22,39 @@
 #define AUGUR_ERRBIT_TIMEOUT 4u
 
 namespace augur {
+
+// ---------------------------------------------------------------------------------
+// host helpers shared by every translation unit
+// ---------------------------------------------------------------------------------
+// Opts `kernel` in to `bytes` of dynamic shared memory on the current device. The opt-in is a
+// per-device property of the kernel shared by every caller in the process, so it is recorded per
+// (device, kernel) under a lock and only ever raised.
+inline int raise_dyn_smem(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return AUGUR_ECUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cur = done[{dev, kernel}];
+  if (bytes <= cur) return AUGUR_OK;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return AUGUR_ECUDA;
+  }
+  cur = bytes;
+  return AUGUR_OK;
+}
+
+// Streaming multiprocessors of the current device (152 on GB300 if the query fails).
+inline int current_sm_count() {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) {
+    cudaGetLastError();
+    return 152;
+  }
+  return nsm;
+}
 
 // ---------------------------------------------------------------------------------
 // complex helpers (float2 = re, im)

@@ -934,9 +934,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   a.B = B;
   a.G = G;
   a.xseg = (G + CONV_M - 1) / CONV_M;
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nsm = current_sm_count();
   // y chunk: long enough to amortise the two halo rows, short enough to fill every SM
   const int columns = B * G * a.xseg;
   int yc = G;
@@ -951,13 +949,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   if (make_act_map<CIN>(&map, in, B, G) != AUGUR_OK) return AUGUR_ECUDA;
   constexpr int WBYTES = 27 * CIN * N * 2;
   const size_t smem = ((WBYTES + 127) / 128) * 128 + (size_t)RING * 3 * (CIN / 8) * SLAB_ROWS * 16;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(conv_tc_kernel<CIN, N, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return AUGUR_ECUDA;
-    attr = true;
-  }
+  if (raise_dyn_smem((const void *)conv_tc_kernel<CIN, N, EPI>, smem)) return AUGUR_ECUDA;
   const int grid = std::min(a.nunits, nsm);
   conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(map, (const bf16 *)wB, bias, resid,
                                                                 (const bf16 *)zprev, out0, (bf16 *)out1, a, err, stats);
@@ -970,9 +962,7 @@ int launch_conv_in_tc(const void *x, const void *wB, const float *bias, void *z0
   a.B = B;
   a.G = G;
   a.xseg = (G + CONV_M - 1) / CONV_M;
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nsm = current_sm_count();
   const int columns = B * G * a.xseg;
   int yc = G;
   while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
@@ -981,12 +971,7 @@ int launch_conv_in_tc(const void *x, const void *wB, const float *bias, void *z0
   a.nunits = columns * a.nyc;
   a.out_scale = 1.f;
   const size_t smem = (size_t)IN_KB * 32 * 16 + (size_t)IN_STAGES * IN_ABYTES;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(conv_in_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return AUGUR_ECUDA;
-    attr = true;
-  }
+  if (raise_dyn_smem((const void *)conv_in_tc_kernel, smem)) return AUGUR_ECUDA;
   const int grid = std::min(a.nunits, nsm);
   conv_in_tc_kernel<<<grid, IN_THREADS, smem, st>>>((const bf16 *)x, (const bf16 *)wB, bias, (bf16 *)z0, (bf16 *)h0,
                                                     a, err);
@@ -997,9 +982,7 @@ template <int CIN, int N, int DZF>
 int launch_wgrad(const void *h, const void *dz, int B, int G, float *partial, int max_parts, float *out,
                  cudaStream_t st) {
   const int nrows = B * G * G;
-  int dev = 0, nsm = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nsm = current_sm_count();
   int nparts = std::min(max_parts, std::min(nrows, nsm * 4));
   const int rows_per = (nrows + nparts - 1) / nparts;
   nparts = (nrows + rows_per - 1) / rows_per;

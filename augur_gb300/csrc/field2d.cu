@@ -289,14 +289,12 @@ __global__ void f2_prep_kernel(const float *__restrict__ W, const float *__restr
 
 template <int KS>
 int conv3_ks(const ConvSrc &s, const float *Wp, int cout, int H, int act, float *out, int batch, cudaStream_t st) {
-  static bool raised = false;  // opt in to the large shared-memory carve-out once per process
-  if (!raised) {
-    const int lim = (int)conv_smem(CIN_MAX);
-    if (cudaFuncSetAttribute(f2_conv3_kernel<A_SAME, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) ||
-        cudaFuncSetAttribute(f2_conv3_kernel<A_POOL, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) ||
-        cudaFuncSetAttribute(f2_conv3_kernel<A_UP, KS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))
+  {  // opt in to the large shared-memory carve-out (per device, only ever raised)
+    const size_t lim = conv_smem(CIN_MAX);
+    if (augur::raise_dyn_smem((const void *)f2_conv3_kernel<A_SAME, KS>, lim) ||
+        augur::raise_dyn_smem((const void *)f2_conv3_kernel<A_POOL, KS>, lim) ||
+        augur::raise_dyn_smem((const void *)f2_conv3_kernel<A_UP, KS>, lim))
       return AUGUR_ECUDA;
-    raised = true;
   }
   dim3 grid((H + CT - 1) / CT, (H + CT - 1) / CT, batch);
   // the partial-sum exchange reuses the staging region: (KS - 1) x 8 x 256 floats
@@ -919,13 +917,7 @@ int tick_launch(int what, void *pos, void *mom, int64_t n, TickArgs a, int drift
   if (what == 0) {  // scatter
     const size_t sm = (size_t)a.G * a.G * sizeof(unsigned long long);
     if (sm <= T2_SMEM_MAX) {
-      static bool raised = false;
-      if (!raised) {
-        if (cudaFuncSetAttribute(t2_scatter_kernel<TP, TM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)T2_SMEM_MAX))
-          return AUGUR_ECUDA;
-        raised = true;
-      }
+      if (augur::raise_dyn_smem((const void *)t2_scatter_kernel<TP, TM, true>, T2_SMEM_MAX)) return AUGUR_ECUDA;
       // persistent CTAs per channel (one per SM at this shared-memory size), each flushes once
       const unsigned per = (unsigned)std::max<int64_t>(1, std::min<int64_t>(101, (n + 1023) / 1024));
       t2_scatter_kernel<TP, TM, true><<<dim3(per, 3), 1024, sm, st>>>((const TP *)pos, (const TM *)mom, n, a, drift,

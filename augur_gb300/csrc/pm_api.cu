@@ -493,19 +493,7 @@ int alloc_deposit_tables(augur_pm_plan *p) {
 // another plan's launches rely on.
 template <typename K>
 int raise_smem(K *kernel, size_t bytes) {
-  static std::mutex mu;
-  static std::map<std::pair<int, const void *>, size_t> done;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  std::lock_guard<std::mutex> lock(mu);
-  size_t &cur = done[{dev, (const void *)kernel}];
-  if (bytes <= cur) return AUGUR_OK;
-  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
-    cudaGetLastError();
-    return AUGUR_ECUDA;
-  }
-  cur = bytes;
-  return AUGUR_OK;
+  return raise_dyn_smem((const void *)kernel, bytes);
 }
 
 int raise_smem_limits(const augur_pm_plan *p) {
@@ -1034,14 +1022,8 @@ int augur_pm_pair_acc(augur_pm_plan *p, const float *pos, const float *mass, con
   AUGUR_LAUNCH_CHECK(p);
   if (params) {
     // the MLP's 64 x 64 layer on the tensor cores; persistent CTAs over 128-row tiles
-    static bool raised = false;
-    if (!raised) {
-      if (cudaFuncSetAttribute(pair_weight_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PTC_SMEM))
-        return AUGUR_ECUDA;
-      raised = true;
-    }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    if (raise_dyn_smem((const void *)pair_weight_tc_kernel, PTC_SMEM)) return AUGUR_ECUDA;
+    const int sms = current_sm_count();
     const int64_t tiles = (n * KP + PTC_M - 1) / PTC_M;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, (int64_t)std::max(1, sms) * 4);
     pair_weight_tc_kernel<<<grid, PTC_M, PTC_SMEM, st>>>(p->pair_sorted, pos, mass, mask, n, KP, p->pair_nbj,

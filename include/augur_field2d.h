@@ -114,6 +114,10 @@ int augur_field2d_kick(const float *vel, const float *acc0, const float *acc1, i
  * alone. The scatter is deterministic: contributions are rounded to a fixed point bounded by
  * |v| < c and N, summed in int64 (one channel per CTA in shared memory for grid <= 160, then one
  * flush per CTA). fp32 arithmetic follows torch's operation order without contractions.
+ * Non-finite state (NaN or infinite positions or momenta) is outside the tick's contract: no
+ * error is reported, and such a body's fixed-point contribution is undefined (where the
+ * reference's float grid would turn NaN). Callers that can produce non-finite state check it
+ * themselves (for example with torch.isfinite on the state between ticks).
  * work: augur_tick2d_work_bytes(grid) bytes, 8-byte aligned.
  */
 #define AUGUR_DTYPE_F32  0

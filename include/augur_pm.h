@@ -298,7 +298,9 @@ int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t t
  * this library keeps until the process exits; t * dim must not exceed 2^19 (else
  * AUGUR_ERANGE). The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that call before any stream
- * capture. All calls share the array: calls whose kernels overlap on the GPU (for example
+ * capture. The address is kept for the life of the process: after cudaDeviceReset (or a
+ * release and re-creation of the device's primary context) it is stale, so the entry point
+ * must not be called again in that process. All calls share the array: calls whose kernels overlap on the GPU (for example
  * on two streams) race and give wrong results; serialise them on one stream. Results match
  * augur_direct_sum_fp64 up to the order of the per-chunk partial sums.
  */

@@ -480,6 +480,73 @@ def direct_sum_periodic(targets, sources, eps: float, box: float, mass=None, tar
     return out
 
 
+def ewald_table(n: int = 64):
+    """The Ewald correction for a unit mass in a unit box (periodic sum minus the nearest-image
+    Newtonian term) on an (n+1)^3 grid over the positive octant [0, 1/2]^3, indexed [z][y][x]:
+    the table the GPU's periodic direct sum interpolates. Zero at the origin."""
+    P = n + 1
+    g = 0.5 * np.arange(P) / n
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    X = np.stack([x.ravel(), y.ravel(), z.ravel()], -1)
+    a = ewald_unit(X)
+    r = np.linalg.norm(X, axis=-1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        newt = np.where(r[:, None] > 0, -X / np.maximum(r, 1e-300)[:, None] ** 3, 0.0)
+    corr = a - newt
+    corr[r == 0] = 0.0
+    return corr.reshape(P, P, P, 3)
+
+
+def ewald_interp(tab, u):
+    """Trilinear interpolation of ewald_table at unit-box displacements u (K,3) in [-1/2, 1/2]^3,
+    folded into the positive octant (the correction is odd in each component)."""
+    n = tab.shape[0] - 1
+    u = np.asarray(u, np.float64)
+    s = np.where(u < 0, -1.0, 1.0)
+    v = np.minimum(np.abs(u) * (2 * n), n)
+    i = np.minimum(v.astype(np.int64), n - 1)
+    f = v - i
+    out = np.zeros_like(u)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                w = (f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1]) * (f[:, 2] if dz else 1 - f[:, 2])
+                out += w[:, None] * tab[i[:, 2] + dz, i[:, 1] + dy, i[:, 0] + dx]
+    return s * out
+
+
+def direct_sum_periodic_tabulated(targets, sources, eps: float, box: float, tab, mass=None, target_index=None):
+    """direct_sum_periodic with the Ewald correction read from ewald_table by trilinear
+    interpolation instead of summed exactly: the arithmetic of the GPU's periodic direct sum."""
+    tg = np.asarray(targets, np.float64)
+    src = np.asarray(sources, np.float64)
+    m = np.ones(len(src)) if mass is None else np.asarray(mass, np.float64)
+    out = np.zeros_like(tg)
+    for t in range(len(tg)):
+        d = src - tg[t]
+        d -= box * np.rint(d / box)
+        r2 = (d ** 2).sum(-1)
+        keep = np.ones(len(src), bool)
+        if target_index is not None and target_index[t] >= 0:
+            keep[target_index[t]] = False
+        inv = (r2 + eps ** 2) ** -1.5
+        corr = ewald_interp(tab, -d / box) / box ** 2
+        out[t] = ((d * (inv * m)[:, None]) + corr * m[:, None])[keep].sum(0)
+    return out
+
+
+def energy_sums(vel, mass, mask, phi=None):
+    """float64 reference of the compensated reductions: kinetic energy sum m v^2 / 2, momentum
+    sum m v, mass sum m and potential energy sum m phi / 2, with m = mass * mask (fp32 product)."""
+    m = (np.asarray(mass, F32) * np.asarray(mask, F32)).astype(np.float64)
+    v = np.asarray(vel, np.float64)
+    out = {"ke": float(0.5 * (m * (v ** 2).sum(-1)).sum()), "momentum": (m[:, None] * v).sum(0).tolist(),
+           "mass": float(m.sum()), "pe": 0.0}
+    if phi is not None:
+        out["pe"] = float(0.5 * (m * np.asarray(phi, np.float64)).sum())
+    return out
+
+
 # ----------------------------------------------------------------------------------
 # integrators
 # ----------------------------------------------------------------------------------

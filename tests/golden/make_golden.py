@@ -1,7 +1,7 @@
 """Generates tests/golden/*.npz from the reference implementation itself.
 
-Run in a container where the reference (Faraday-dot-py/Augur) is checked out:
-    AUGUR_REF=/root/reference python tests/golden/make_golden.py
+Run where the reference (Faraday-dot-py/Augur) is checked out, with AUGUR_REF naming its root:
+    AUGUR_REF=<path to the reference checkout> python tests/golden/make_golden.py
 It imports the reference's own functions (ScatterField._corners / scatter / gather,
 pm_baseline_force_error.sample / pm_acc, scatter_scaling_ops.exact_acc), runs them on
 the CPU in float32/float64 exactly as the reference does, and stores inputs and outputs.
@@ -19,7 +19,9 @@ from pathlib import Path
 import numpy as np
 import torch
 
-REF = Path(os.environ.get("AUGUR_REF", "/root/reference"))
+if not os.environ.get("AUGUR_REF"):
+    raise SystemExit("set AUGUR_REF to the root of the reference checkout (Faraday-dot-py/Augur)")
+REF = Path(os.environ["AUGUR_REF"])
 OUT = Path(__file__).resolve().parent
 sys.dont_write_bytecode = True
 sys.path.insert(0, str(REF))
