@@ -75,7 +75,8 @@ SIGNATURES = {
     "augur_cnn_conv_tc": (_i32, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _f32, _vp, _vp, _vp]),
     "augur_cnn_conv_in": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     "augur_cnn_conv_in_tc": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
-    "augur_cnn_wgrad": (_i32, [_i32, _vp, _vp, _i32, _i32, _vp, _i32, _vp, _vp]),
+    "augur_cnn_wgrad": (_i32, [_i32, _vp, _vp, _i32, _i32, _vp, _i32, _vp, _vp, _vp]),
+    "augur_cnn_set_wait_budget": (C.c_uint, [C.c_uint]),
     "augur_cnn_prep_weights": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
     "augur_cnn_input": (_i32, [_vp, _vp, _i64, _f32, _f32, _vp, _vp]),
     "augur_cnn_adamw": (_i32, [_vp, _vp, _vp, _vp, _i32, _f32, _f32, _f32, _f32, _f32, _i32, _vp]),

@@ -176,20 +176,20 @@ class GridCNN:
             self._partial = torch.empty(4 * 152 * (W * 27 * W + W), dtype=torch.float32, device=self.device)
         parts = 4 * 152
         s = self.out_scale
-        # output layer: y = s (conv(h3) + b)
-        gw = torch.empty(4 * 27 * W + 4, dtype=torch.float32, device=self.device)
-        self._call("augur_cnn_wgrad", 1, h[3].data_ptr(), dfield4.data_ptr(), B, G, self._partial.data_ptr(), parts,
-                   gw.data_ptr())
-        self.gview["w_out"].copy_(gw[:3 * 27 * W].view(3, 27, W) * s)
-        self.gview["b_out"].copy_(gw[4 * 27 * W:4 * 27 * W + 3] * s)
+        # output layer: y = s (conv(h3) + b); dout16 = s dL/dy as bf16 feeds both of its gradients
         self._call("augur_cnn_pack_dout", dfield4.data_ptr(), nv, s, ws["dout16"].data_ptr())
+        gw = torch.empty(4 * 27 * W + 4, dtype=torch.float32, device=self.device)
+        self._call("augur_cnn_wgrad", 3, h[3].data_ptr(), ws["dout16"].data_ptr(), B, G, self._partial.data_ptr(),
+                   parts, gw.data_ptr(), self.err.data_ptr())
+        self.gview["w_out"].copy_(gw[:3 * 27 * W].view(3, 27, W))
+        self.gview["b_out"].copy_(gw[4 * 27 * W:4 * 27 * W + 3])
         self._call("augur_cnn_conv_tc", 3, ws["dout16"].data_ptr(), self.op_bwd_out.data_ptr(), None, None,
                    z[3].data_ptr(), dh[1].data_ptr(), dz[1].data_ptr(), B, G, 1.0, self.err.data_ptr(), None)
         cur = 1
         for i in (2, 1, 0):  # middle layer i maps h[i] -> h[i+1]
             gm = torch.empty(W * 27 * W + W, dtype=torch.float32, device=self.device)
             self._call("augur_cnn_wgrad", 0, h[i].data_ptr(), dz[cur].data_ptr(), B, G, self._partial.data_ptr(),
-                       parts, gm.data_ptr())
+                       parts, gm.data_ptr(), self.err.data_ptr())
             self.gview[f"w_mid{i}"].copy_(gm[:W * 27 * W].view(W, 27, W))
             self.gview[f"b_mid{i}"].copy_(gm[W * 27 * W:])
             nxt = 1 - cur
@@ -199,7 +199,7 @@ class GridCNN:
             cur = nxt
         gi = torch.empty(W * 27 * 2 + W, dtype=torch.float32, device=self.device)
         self._call("augur_cnn_wgrad", 2, self._x.data_ptr(), dz[cur].data_ptr(), B, G, self._partial.data_ptr(),
-                   parts, gi.data_ptr())
+                   parts, gi.data_ptr(), None)
         self.gview["w_in"].copy_(gi[:W * 27 * 2].view(W, 27, 2))
         self.gview["b_in"].copy_(gi[W * 27 * 2:])
 

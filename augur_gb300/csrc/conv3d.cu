@@ -27,6 +27,8 @@
 
 #include <mutex>
 
+#include <atomic>
+
 #include "augur_common.cuh"
 #include "tcgen05.cuh"
 
@@ -45,7 +47,11 @@ constexpr int EPI_WARPS = 8;
 constexpr int MMA_WARP = EPI_WARPS;
 constexpr int TMA_WARP = EPI_WARPS + 1;
 constexpr int CONV_THREADS = 32 * (EPI_WARPS + 2);
-constexpr uint32_t WAIT_BUDGET = 1u << 20;
+constexpr uint32_t WAIT_BUDGET = 1u << 20;  // default tries of a pipeline wait (augur_cnn_set_wait_budget)
+// Tries of a drain wait: before a CTA exits it waits, with this fixed bound and regardless of the
+// pipeline budget, for its own TMA copies and MMAs still in flight, so that nothing writes its
+// shared memory or TMEM after it has gone.
+constexpr uint32_t DRAIN_BUDGET = 1u << 22;
 
 enum { EPI_FWD = 0, EPI_OUT = 1, EPI_BWD = 2 };
 
@@ -56,13 +62,6 @@ __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.f + erff(x * 0.70710678118654752440f)) + x * phi;
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
-               : "memory");
-}
 // 5D tiled TMA load (c, x, y, z, b) into shared memory, completing bytes on mbar.
 __device__ __forceinline__ void tma_load5(uint32_t dst, const CUtensorMap *map, int c, int x, int y, int z, int b,
                                           uint64_t *mbar) {
@@ -80,6 +79,7 @@ struct ConvArgs {
   int nyc;           // ceil(G / yc)
   int nunits;        // B * G * xseg * nyc
   float out_scale;   // EPI_OUT: added field = out_scale * (acc + bias)
+  uint32_t budget;   // tries of a pipeline wait before the CTA gives up (AUGUR_ERRBIT_TIMEOUT)
 };
 
 struct ConvUnit {
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;
   unsigned char *sSlab = smem + WREGION;  // [RING][3 planes][CB][SLAB_ROWS][16 B]
-  __shared__ __align__(8) uint64_t full[RING], empty[RING], slot_full[RACC], slot_empty[RACC];
+  __shared__ __align__(8) uint64_t full[RING], empty[RING], slot_full[RACC], slot_empty[RACC], drained;
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
 
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
       mbar_init(&slot_full[i], 1);
       mbar_init(&slot_empty[i], EPI_WARPS);
     }
+    mbar_init(&drained, 1);
     s_abort = 0;
     mbar_fence_init();
   }
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
 
   // bounded wait; gives up early once another role has given up
   auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
-    for (uint32_t i = 0; i < WAIT_BUDGET; ++i) {
+    for (uint32_t i = 0; i < a.budget; ++i) {
       if (mbar_try_wait(bar, parity)) return true;
       if ((i & 255u) == 255u && *abort_flag) return false;
     }
@@ -237,11 +238,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
                         u.b, &full[slot]);
         }
       }
-      // tail: every slot's last fill has been consumed and released (no transfer or MMA
-      // still writes this CTA's shared memory when it exits)
+      // tail: the copies of the last RING fills have landed (no transfer still writes this
+      // CTA's shared memory when it exits), waited for even after an abort
       const uint32_t last = k;
       for (uint32_t r = (last > RING ? last - RING : 0); r < last; ++r)
-        if (!wait(&empty[r % RING], (r / RING) & 1u)) wait(&full[r % RING], (r / RING) & 1u);
+        if (!mbar_wait_bounded(&full[r % RING], (r / RING) & 1u, DRAIN_BUDGET)) *abort_flag = 1;
     }
   } else if (warp == MMA_WARP) {
     // ---- MMA issue, one input row at a time ---------------------------------------------------
@@ -292,6 +293,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
         k0 += u.ny + 2;
         T0 += u.ny;
       }
+      // drain: every MMA this thread issued (and the arrivals its commits make) has completed
+      // before the CTA frees TMEM and exits, on the normal path and after an abort alike
+      umma_commit(&drained);
+      if (!mbar_wait_bounded(&drained, 0u, DRAIN_BUDGET)) *abort_flag = 1;
     }
   } else {
     // ---- epilogue: warp w reads TMEM lane quarter w % 4 (voxels x0 + 32 (w % 4) + lane) and
@@ -449,7 +454,7 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;                   // [8 kb][32 n][16 B]
   unsigned char *sA = smem + IN_KB * N * 16;  // [IN_STAGES][8 kb][128 r][16 B]
-  __shared__ __align__(8) uint64_t full[IN_STAGES], empty[IN_STAGES], acc_full[NACC], acc_empty[NACC];
+  __shared__ __align__(8) uint64_t full[IN_STAGES], empty[IN_STAGES], acc_full[NACC], acc_empty[NACC], drained;
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
 
@@ -472,6 +477,7 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
       mbar_init(&acc_full[i], 1);
       mbar_init(&acc_empty[i], EPI_WARPS);
     }
+    mbar_init(&drained, 1);
     s_abort = 0;
     mbar_fence_init();
   }
@@ -487,7 +493,7 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
   const uint32_t a0 = smem_u32(sA);
   volatile int *abort_flag = &s_abort;
   auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
-    for (uint32_t i = 0; i < WAIT_BUDGET; ++i) {
+    for (uint32_t i = 0; i < a.budget; ++i) {
       if (mbar_try_wait(bar, parity)) return true;
       if ((i & 255u) == 255u && *abort_flag) return false;
     }
@@ -556,6 +562,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
           umma_commit(&empty[st]);
         }
       }
+      // drain: every MMA issued here (and its commits' arrivals) has completed before the CTA
+      // frees TMEM and exits, also after an abort
+      umma_commit(&drained);
+      if (!mbar_wait_bounded(&drained, 0u, DRAIN_BUDGET)) *abort_flag = 1;
     }
   } else {
     // ---- epilogue ------------------------------------------------------------------------------
@@ -597,14 +607,6 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
         if (lane == 0) mbar_arrive(&acc_empty[acc]);
       }
     }
-  }
-  // drain: every issued MMA has been waited for by the epilogue (acc_full); the empty commits
-  // of the last stages are waited here so no arrival targets this CTA after it exits
-  if (tid == 32 * (MMA_WARP + 1)) {
-    uint32_t total = 0;
-    for (int unit = blockIdx.x; unit < a.nunits; unit += gridDim.x) total += conv_unit(a, unit).ny;
-    for (uint32_t q = (total > IN_STAGES ? total - IN_STAGES : 0); q < total; ++q)
-      wait(&empty[q % IN_STAGES], (q / IN_STAGES) & 1u);
   }
   tc_fence_before();
   __syncthreads();
@@ -765,6 +767,205 @@ __global__ void __launch_bounds__(CIN * (N / NB) * XS) wgrad_kernel(const bf16 *
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Weight gradient on tcgen05: dW[n][tap][c] = sum_v dz[v][n] * h[v + tap][c] (zero padding) and
+// the bias gradient sum_v dz[v][n], for 32 input channels and NP = 16 or 32 gradient channels.
+//
+// GEMM: D[(plane, c)][n] += A[(plane, c)][x] * B[x][n] over K = the 128 voxels x of one dz row
+// (b, z, y, x0 .. x0+127), with A = the input rows of the nine (dz, dy) neighbour planes and B =
+// the dz row. Both operands sit in shared memory exactly as the TMA boxes land, channels-last
+// [8-channel block][voxel row][16 B], which for K = voxels is the MN-major no-swizzle layout: a
+// core matrix is 8 voxel rows of 8 channels (128 contiguous bytes); in this mode the descriptor's
+// leading byte offset is the distance between K-adjacent core matrices (128 B) and its stride
+// byte offset the distance between MN-adjacent ones (CBLK). The nine planes and a constant plane
+// of ones are stored back to back (plane stride 4 CBLK), so four consecutive planes x 32
+// channels are one M = 128 operand with a uniform channel-block stride, and the dx taps are
+// the same operand started 16 B (one voxel row) later. Per 16 voxels: 3 dx x 3 M tiles
+// (planes 0-3, 4-7, 6-9; planes 6 and 7 of the last tile repeat the second tile's and are
+// not read back) into nine TMEM accumulators of NP columns. The ones plane gives the bias
+// gradient (its rows are sum_x dz[x][n] for every c).
+//
+// Each CTA takes a contiguous range of dz rows (consecutive y, so the h rows are re-read
+// from L2), accumulates in TMEM for its whole range, and writes one partial of
+// NOUT * 27 * 32 + NOUT floats; partials are added in a fixed order afterwards.
+// Roles: warps 0-3 epilogue (TMEM lane quarters), warp 4 MMA issue, warp 5 TMA.
+// ---------------------------------------------------------------------------------------
+constexpr int WG_PLANES = 10;                    // nine (dz, dy) planes + the ones plane
+constexpr int WG_CBLK = SLAB_ROWS * 16;          // one 8-channel block of an input row
+constexpr int WG_PLANE = 4 * WG_CBLK;            // 32 channels
+constexpr int WG_DBLK = CONV_M * 16;             // one 8-channel block of the dz row
+constexpr int WG_STAGES = 2;
+constexpr int WG_THREADS = 6 * 32;
+constexpr int WG_TMEM_COLS = 512;
+
+struct WgArgs {
+  int B, G, xseg, nunits;
+  uint32_t budget;
+};
+
+template <int NP>
+constexpr int wg_stage_bytes() {
+  return WG_PLANES * WG_PLANE + (NP / 8) * WG_DBLK;
+}
+
+template <int NP, int NOUT>
+__global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(const __grid_constant__ CUtensorMap hmap,
+                                                                 const __grid_constant__ CUtensorMap dmap, WgArgs a,
+                                                                 float *__restrict__ partial,
+                                                                 unsigned *__restrict__ err) {
+  constexpr int STAGE = wg_stage_bytes<NP>();
+  constexpr uint32_t TX = 9u * 4u * SLAB * 16u + (uint32_t)(NP / 8) * CONV_M * 16u;
+  constexpr uint32_t IDESC = idesc_bf16_f32(CONV_M, NP) | (1u << 15) | (1u << 16);  // A and B MN-major
+  constexpr int LEN = NOUT * 27 * 32 + NOUT;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[WG_STAGES], empty[WG_STAGES], done;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int G = a.G;
+  // this CTA's contiguous range of dz rows (units), y fastest
+  const int u0 = (int)(((long long)a.nunits * blockIdx.x) / gridDim.x);
+  const int u1 = (int)(((long long)a.nunits * (blockIdx.x + 1)) / gridDim.x);
+  {  // the ones plane of every stage (bf16 1.0), never overwritten
+    const uint4 one = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+    for (int e = tid; e < WG_STAGES * (WG_PLANE / 16); e += WG_THREADS) {
+      const int st = e / (WG_PLANE / 16), r = e % (WG_PLANE / 16);
+      reinterpret_cast<uint4 *>(smem + (size_t)st * STAGE + 9 * WG_PLANE)[r] = one;
+    }
+  }
+  if (tid == 0) {
+    for (int i = 0; i < WG_STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&done, 1);
+    s_abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&s_tmem, WG_TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t base0 = smem_u32(smem);
+  volatile int *abort_flag = &s_abort;
+  auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+    for (uint32_t i = 0; i < a.budget; ++i) {
+      if (mbar_try_wait(bar, parity)) return true;
+      if ((i & 255u) == 255u && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    return false;
+  };
+  auto unit_coords = [&](int u, int &b, int &z, int &y, int &x0) {
+    const int xs = u % a.xseg;
+    int t = u / a.xseg;
+    y = t % G;
+    t /= G;
+    z = t % G;
+    b = t / G;
+    x0 = xs * CONV_M;
+  };
+
+  if (warp == 5) {
+    // ---- TMA: the nine neighbour rows (130 voxels from x0 - 1) and the dz row (128 voxels) ----
+    if (lane == 0) {
+      uint32_t issued = 0;
+      for (int u = u0; u < u1; ++u) {
+        const uint32_t i = (uint32_t)(u - u0), slot = i % WG_STAGES, n = i / WG_STAGES;
+        if (n > 0 && !wait(&empty[slot], (n - 1) & 1u)) break;
+        int b, z, y, x0;
+        unit_coords(u, b, z, y, x0);
+        const uint32_t dst = base0 + slot * STAGE;
+        mbar_expect_tx(&full[slot], TX);
+        for (int p = 0; p < 9; ++p)
+#pragma unroll
+          for (int cb = 0; cb < 4; ++cb)
+            tma_load5(dst + (uint32_t)(p * WG_PLANE + cb * WG_CBLK), &hmap, cb * 8, x0 - 1, y + p % 3 - 1,
+                      z + p / 3 - 1, b, &full[slot]);
+#pragma unroll
+        for (int nb = 0; nb < NP / 8; ++nb)
+          tma_load5(dst + (uint32_t)(WG_PLANES * WG_PLANE + nb * WG_DBLK), &dmap, nb * 8, x0, y, z, b, &full[slot]);
+        issued = i + 1;
+      }
+      // tail: the last copies have landed before the CTA can exit (also after an abort)
+      for (uint32_t r = (issued > WG_STAGES ? issued - WG_STAGES : 0); r < issued; ++r)
+        if (!mbar_wait_bounded(&full[r % WG_STAGES], (r / WG_STAGES) & 1u, DRAIN_BUDGET)) *abort_flag = 1;
+    }
+  } else if (warp == 4) {
+    // ---- MMA issue ---------------------------------------------------------------------------
+    if (lane == 0) {
+      bool first = true;
+      for (int u = u0; u < u1; ++u) {
+        const uint32_t i = (uint32_t)(u - u0), slot = i % WG_STAGES;
+        if (!wait(&full[slot], (i / WG_STAGES) & 1u)) break;
+        tc_fence_after();
+        int b, z, y, x0;
+        unit_coords(u, b, z, y, x0);
+        const int ks_n = (min(CONV_M, G - x0) + 15) / 16;
+        const uint32_t sb = base0 + slot * STAGE;
+        for (int ks = 0; ks < ks_n; ++ks) {
+          const uint64_t bd = smem_desc(sb + (uint32_t)(WG_PLANES * WG_PLANE + ks * 256), 128, WG_DBLK);
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+              const int p0 = t == 0 ? 0 : (t == 1 ? 4 : 6);
+              const uint64_t ad = smem_desc(sb + (uint32_t)(p0 * WG_PLANE + (ks * 16 + dx) * 16), 128, WG_CBLK);
+              umma_bf16(tmem + (uint32_t)((t * 3 + dx) * NP), ad, bd, IDESC, first ? 0u : 1u);
+            }
+          first = false;
+        }
+        umma_commit(&empty[slot]);
+      }
+      // every MMA (and every commit's arrival) completes before the epilogue reads TMEM and
+      // before the CTA exits, also after an abort
+      umma_commit(&done);
+      if (!mbar_wait_bounded(&done, 0u, DRAIN_BUDGET)) *abort_flag = 1;
+    }
+  } else {
+    // ---- epilogue: warp q reads TMEM lanes 32q .. 32q + 31 = plane p0 + q, channel = lane ----------
+    const int q = warp;
+    const bool ok = wait(&done, 0u);
+    tc_fence_after();
+    float *out = partial + (size_t)blockIdx.x * LEN;
+    const bool any = u1 > u0 && ok;  // accumulators hold this CTA's sums (else write zeros)
+    for (int t = 0; t < 3; ++t) {
+      const int p = (t == 0 ? 0 : (t == 1 ? 4 : 6)) + q;
+      if (t == 2 && q < 2) continue;  // planes 6 and 7 again
+      for (int dx = 0; dx < 3; ++dx) {
+        if (p == 9 && dx != 1) continue;
+        float v[NP];
+        const uint32_t ta = tmem + (uint32_t)((t * 3 + dx) * NP) + ((uint32_t)(q * 32) << 16);
+        if (any) {
+          if constexpr (NP == 32) tmem_ld32(ta, v);
+          else tmem_ld16(ta, v);
+        }
+        if (p == 9) {
+          if (lane == 0)
+#pragma unroll
+            for (int n = 0; n < NOUT; ++n) out[NOUT * 27 * 32 + n] = any ? v[n] : 0.f;
+        } else {
+          const int tap = (p / 3) * 9 + (p % 3) * 3 + dx;
+#pragma unroll
+          for (int n = 0; n < NOUT; ++n) out[(n * 27 + tap) * 32 + lane] = any ? v[n] : 0.f;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && *abort_flag) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, WG_TMEM_COLS);
+  }
+}
+
 __global__ void reduce_partials_kernel(const float *__restrict__ partial, int nparts, int len,
                                        float *__restrict__ out) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -895,6 +1096,9 @@ using namespace augur;
 
 namespace {
 
+// tries of a pipeline wait in the tensor-core kernels (augur_cnn_set_wait_budget)
+std::atomic<uint32_t> g_wait_budget{WAIT_BUDGET};
+
 // cuTensorMapEncodeTiled through the runtime's driver entry-point query (no link against
 // libcuda); resolved once.
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -943,6 +1147,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   a.nyc = (G + yc - 1) / yc;
   a.nunits = columns * a.nyc;
   a.out_scale = out_scale;
+  a.budget = g_wait_budget.load();
   // input activations [B][G][G][G][CIN] bf16 as a 5D tensor (c, x, y, z, b); box = 8 channels x
   // SLAB voxels of one row; outside the grid the box reads zeros (the convolution's padding)
   CUtensorMap map;
@@ -970,11 +1175,52 @@ int launch_conv_in_tc(const void *x, const void *wB, const float *bias, void *z0
   a.nyc = (G + yc - 1) / yc;
   a.nunits = columns * a.nyc;
   a.out_scale = 1.f;
+  a.budget = g_wait_budget.load();
   const size_t smem = (size_t)IN_KB * 32 * 16 + (size_t)IN_STAGES * IN_ABYTES;
   if (raise_dyn_smem((const void *)conv_in_tc_kernel, smem)) return AUGUR_ECUDA;
   const int grid = std::min(a.nunits, nsm);
   conv_in_tc_kernel<<<grid, IN_THREADS, smem, st>>>((const bf16 *)x, (const bf16 *)wB, bias, (bf16 *)z0, (bf16 *)h0,
                                                     a, err);
+  return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
+}
+
+// (B, G, G, G, C) bf16 channels-last as a 5D tensor (c, x, y, z, b) with a box of 8 channels x
+// boxx voxels of one row; out-of-range boxes read zeros.
+int make_rows_map(CUtensorMap *map, const void *ptr, int C, int B, int G, int boxx) {
+  auto fn = encode_fn();
+  if (!fn || (reinterpret_cast<uintptr_t>(ptr) & 15) != 0 || C % 8 != 0) return AUGUR_EINVAL;
+  const cuuint64_t dim[5] = {(cuuint64_t)C, (cuuint64_t)G, (cuuint64_t)G, (cuuint64_t)G, (cuuint64_t)B};
+  const cuuint64_t stride[4] = {(cuuint64_t)C * 2, (cuuint64_t)G * C * 2, (cuuint64_t)G * G * C * 2,
+                                (cuuint64_t)G * G * G * C * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)boxx, 1, 1, 1};
+  const cuuint32_t estride[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(ptr), dim, stride, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? AUGUR_OK : AUGUR_EINVAL;
+}
+
+// weight gradient on tcgen05: h (B, G^3, 32) bf16, dz (B, G^3, NP) bf16; NOUT gradient channels
+// are written (out: NOUT * 27 * 32 weights, then NOUT biases)
+template <int NP, int NOUT>
+int launch_wgrad_tc(const void *h, const void *dz, int B, int G, float *partial, int max_parts, float *out,
+                    unsigned *err, cudaStream_t st) {
+  if (G < 3 || !err) return AUGUR_EINVAL;
+  WgArgs a;
+  a.B = B;
+  a.G = G;
+  a.xseg = (G + CONV_M - 1) / CONV_M;
+  a.nunits = B * G * G * a.xseg;
+  a.budget = g_wait_budget.load();
+  CUtensorMap hmap, dmap;
+  if (make_rows_map(&hmap, h, 32, B, G, SLAB) != AUGUR_OK || make_rows_map(&dmap, dz, NP, B, G, CONV_M) != AUGUR_OK)
+    return AUGUR_EINVAL;
+  const int nparts = std::min(std::min(max_parts, current_sm_count()), a.nunits);
+  const size_t smem = (size_t)WG_STAGES * wg_stage_bytes<NP>();
+  if (raise_dyn_smem((const void *)wgrad_tc_kernel<NP, NOUT>, smem)) return AUGUR_ECUDA;
+  wgrad_tc_kernel<NP, NOUT><<<nparts, WG_THREADS, smem, st>>>(hmap, dmap, a, partial, err);
+  const int len = NOUT * 27 * 32 + NOUT;
+  reduce_partials_kernel<<<(len + 255) / 256, 256, 0, st>>>(partial, nparts, len, out);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
 }
 
@@ -994,7 +1240,7 @@ int launch_wgrad(const void *h, const void *dz, int B, int G, float *partial, in
   const size_t smem = std::max(((size_t)9 * (G + 2) * CIN + (size_t)G * N) * 4,
                                XS > 1 ? (size_t)XS * CIN * N * 28 * 4 : 0);
   if (smem > 227 * 1024) return AUGUR_EINVAL;
-  cudaFuncSetAttribute(wgrad_kernel<CIN, N, DZF, XS, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (raise_dyn_smem((const void *)wgrad_kernel<CIN, N, DZF, XS, NB>, smem)) return AUGUR_ECUDA;
   wgrad_kernel<CIN, N, DZF, XS, NB><<<nparts, CIN * (N / NB) * XS, smem, st>>>((const bf16 *)h, dz, B, G, rows_per,
                                                                               partial);
   const int len = N * 27 * CIN + N;
@@ -1040,20 +1286,26 @@ int augur_cnn_conv_in_tc(const void *x, const void *w_umma, const float *bias, i
   return launch_conv_in_tc(x, w_umma, bias, z0, h0, batch, grid, err, (cudaStream_t)stream);
 }
 
-// kind: 0 = 32 -> 32 (dz bf16), 1 = output layer 32 -> 3 (dz = output gradient, fp32 float4
-// grid), 2 = input layer 2 -> 32 (dz bf16). out: N*27*CIN weight gradients then N bias
-// gradients; partial: scratch of max_parts * (N*27*CIN + N) floats.
+// kind: 0 = 32 -> 32 (dz bf16, tcgen05), 1 = output layer 32 -> 3 (dz = output gradient, fp32
+// float4 grid, CUDA cores), 2 = input layer 2 -> 32 (dz bf16, CUDA cores), 3 = output layer from
+// the 16-channel bf16 gradient of augur_cnn_pack_dout (tcgen05), 4 = 32 -> 32 on the CUDA cores.
+// out: N*27*CIN weight gradients then N bias gradients (N = 4 for the output layer); partial:
+// scratch of max_parts * (N*27*CIN + N) floats. err: the error word of the tcgen05 kinds.
 int augur_cnn_wgrad(int kind, const void *h, const void *dz, int batch, int grid, float *partial, int max_parts,
-                    float *out, void *stream) {
-  if (!h || !dz || !partial || !out || max_parts < 1) return AUGUR_EINVAL;
+                    float *out, unsigned *err, void *stream) {
+  if (!h || !dz || !partial || !out || max_parts < 1 || batch < 1 || grid < 3) return AUGUR_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
   switch (kind) {
-    case 0: return launch_wgrad<32, 32, 0>(h, dz, batch, grid, partial, max_parts, out, st);
+    case 0: return launch_wgrad_tc<32, 32>(h, dz, batch, grid, partial, max_parts, out, err, st);
     case 1: return launch_wgrad<32, 4, 1>(h, dz, batch, grid, partial, max_parts, out, st);
     case 2: return launch_wgrad<2, 32, 0>(h, dz, batch, grid, partial, max_parts, out, st);
+    case 3: return launch_wgrad_tc<16, 4>(h, dz, batch, grid, partial, max_parts, out, err, st);
+    case 4: return launch_wgrad<32, 32, 0>(h, dz, batch, grid, partial, max_parts, out, st);
     default: return AUGUR_EINVAL;
   }
 }
+
+unsigned augur_cnn_set_wait_budget(unsigned tries) { return g_wait_budget.exchange(tries); }
 
 int augur_cnn_prep_weights(const float *w, int n_out, int c_in, int cin_pad, int n_pad, int flip, void *out,
                            void *stream) {

@@ -132,10 +132,13 @@ unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 constexpr int DEP_CHUNK_MIN = 2048;
 constexpr int DEP_THREADS = 256;
-// bodies per deposit work item: at least the plan's minimum, and at most ~1024 chunks
+// bodies per deposit work item: at least the plan's minimum, ~1024 chunks for large inputs, and
+// at most DEP_ITEM_MAX (the bound under which a work item's 32-bit shared sums cannot overflow),
+// so that any n < 2^31 takes at most DEP_NCH_MAX chunks
+constexpr int64_t DEP_NCH_MAX = 4096;
 uint32_t dep_chunk(const augur_pm_plan *p, int64_t n) {
   int64_t c = (n + 1023) / 1024;
-  return (uint32_t)std::max<int64_t>(p->dep_chunk_min, c);
+  return (uint32_t)std::min<int64_t>(DEP_ITEM_MAX, std::max<int64_t>(p->dep_chunk_min, c));
 }
 int64_t dep_nchunks(const augur_pm_plan *p, int64_t n) { return (n + dep_chunk(p, n) - 1) / dep_chunk(p, n); }
 
@@ -424,7 +427,7 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   const int RY = t->deposit_rows_y, RZ = t->deposit_rows_z;
   if (RY < 1 || RY > G || G % RY != 0) return AUGUR_EINVAL;
   if (d3 ? (RZ < 1 || RZ > 15 || G % RZ != 0) : RZ != 1) return AUGUR_EINVAL;
-  if (t->deposit_chunk < 1024 || t->deposit_chunk > (1 << 24)) return AUGUR_EINVAL;
+  if (t->deposit_chunk < 1024 || t->deposit_chunk > DEP_ITEM_MAX) return AUGUR_EINVAL;
   if (!(t->green_tile_y == 8 || t->green_tile_y == 16) || G % t->green_tile_y != 0) return AUGUR_EINVAL;
   const int RB = t->c2r_rows;
   if (RB < 1 || RB > 32 || (RB & (RB - 1)) != 0) return AUGUR_EINVAL;
@@ -470,9 +473,11 @@ int alloc_deposit_tables(augur_pm_plan *p) {
   const size_t bytes0 = p->bytes;
   const int G = p->G;
   p->nblk = (p->dim == 3) ? (G / p->dep_RY) * (G / p->dep_RZ) : G / p->dep_RY;
-  // chunks of any n <= max_n: ceil(n / max(chunk_min, ceil(n / 1024))) <= min(ceil(max_n / chunk_min), 1024)
-  const int64_t nch = std::min<int64_t>((p->max_n + p->dep_chunk_min - 1) / p->dep_chunk_min, 1024);
-  p->dep_slots = (size_t)8 * (size_t)nch + 1;
+  // chunks of any n <= max_n: ceil(n / dep_chunk) <= min(ceil(max_n / chunk_min), DEP_NCH_MAX)
+  const int64_t nch = std::min<int64_t>((p->max_n + p->dep_chunk_min - 1) / p->dep_chunk_min, DEP_NCH_MAX);
+  // one 64-bit accumulator tile per row block split over several work items: a split block has
+  // at least two items, and there are at most nblk + 4 nch items, so at most min(nblk, 4 nch)
+  p->dep_slots = (size_t)std::min<int64_t>(p->nblk, 4 * nch) + 1;
   p->dep_items_max = (size_t)p->nblk + 4 * (size_t)nch + 1;
   int rc = AUGUR_OK;
   rc |= dalloc(p, &p->dep_nch, (size_t)p->nblk);
@@ -485,6 +490,10 @@ int alloc_deposit_tables(augur_pm_plan *p) {
   p->dep_bytes = p->bytes - bytes0;
   if (rc != AUGUR_OK) return AUGUR_ENOMEM;
   if (cudaMemset(p->dep_counters, 0, sizeof(uint32_t) * p->nblk) != cudaSuccess) return AUGUR_ECUDA;
+  // the split blocks' accumulator tiles start at zero; the last work item of a block clears its
+  // tile after reading it, so they are zero again at the start of every deposit
+  if (cudaMemset(p->dep_scratch, 0, p->dep_slots * (size_t)p->dep_RY * p->dep_RZ * G * 8) != cudaSuccess)
+    return AUGUR_ECUDA;
   return AUGUR_OK;
 }
 

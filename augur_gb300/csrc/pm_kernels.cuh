@@ -315,9 +315,13 @@ __device__ __forceinline__ void block_segments(const DepositArgs &a, int b, cons
 
 // Work items: every row block gets max(1, ceil(bodies / chunk)) items. One CTA records each
 // block's body segments (seg_tab[b] = {first body, prefix count} pairs), scans the per-block
-// item counts into item_off (nblk + 1 entries) and slot_off (partial-tile slots of blocks
-// split over more than one item), and lists the block of every item in item_blk.
+// item counts into item_off (nblk + 1 entries) and slot_off (the 64-bit accumulator tile of each
+// block split over more than one item), and lists the block of every item in item_blk.
 constexpr int MAXSEGB = 32;  // segments per row block: 2 * (RZ + 1) with RZ <= 15
+// Bodies per deposit work item at most: a work item adds each contribution q < 2^26 to a cell
+// as two 13-bit halves in 32-bit shared accumulators, which cannot overflow for fewer than 2^19
+// contributions per cell (one per body visit).
+constexpr int64_t DEP_ITEM_MAX = (int64_t)1 << 19;
 
 // One thread per row block (many CTAs): the block's body segments and its item count.
 template <int D>
@@ -359,7 +363,7 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
   for (int b = b0; b < b1; ++b) {
     uint32_t c = nch[b];
     si += c;
-    ss += c > 1 ? c : 0;
+    ss += c > 1 ? 1u : 0u;
   }
   const int lane = tid & 31, warp = tid >> 5;
   uint32_t ii = si, is = ss;
@@ -398,25 +402,35 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
     slot_off[b] = rs;
     for (uint32_t j = 0; j < c; ++j) item_blk[ri + j] = (uint32_t)b;
     ri += c;
-    rs += c > 1 ? c : 0;
+    rs += c > 1 ? 1u : 0u;
   }
   if (tid == nt - 1) item_off[nb] = ri;
 }
 
 // ---------------------------------------------------------------------------------
-// K2 (+K3a): deterministic CIC deposit of one block of grid rows, accumulated in
-// 64-bit fixed point in shared memory with warp-aggregated atomics (integer sums are
-// associative, so the result is independent of body order and scheduling), then
+// K2 (+K3a): deterministic CIC deposit of one block of grid rows in fixed point (integer
+// sums are associative, so the result is independent of body order and scheduling), then
 // either written as float32 density rows (MODE 0) or transformed along x in shared
 // memory (R2C, MODE 1) and written to the half spectrum spec[kx][row] (MODE 2: both).
 //
 // Block = RY consecutive y rows x RZ consecutive z planes (2D: RZ = 1). Bodies that
 // touch the block are those whose base row lies in [y0-1, y0+RY-1] x [z0-1, z0+RZ-1];
 // with the state sorted by base row they form at most 2*(RZ+1) contiguous segments.
+// Each contribution q < 2^26 is added to its cell as two 13-bit halves (q & 8191, q >> 13)
+// with 32-bit shared-memory reductions: on this part a 32-bit shared atomic add issues many
+// times faster than a 64-bit one, and the halves cannot overflow (at most DEP_ITEM_MAX
+// contributions per cell per work item); the cell's sum is hi * 2^13 + lo.
 // A block with more than `chunk` bodies is split over several CTAs (work items); each
-// writes its fixed-point tile to scratch and the CTA that finishes last (counter +
-// threadfence, no waiting) adds the others' tiles before converting.
+// adds its nonzero sums into the block's 64-bit tile in global memory (L2 reductions), and
+// the CTA that finishes last (counter + threadfence, no waiting) reads the tile, clears it
+// for the next call, and converts.
 // ---------------------------------------------------------------------------------
+// adds q < 2^31 to cell c of the split accumulators (lo gets the low 13 bits, hi the rest)
+__device__ __forceinline__ void dep_add(uint32_t *lo, uint32_t *hi, int c, uint32_t q) {
+  if (q & 8191u) atomicAdd(&lo[c], q & 8191u);
+  if (q >> 13) atomicAdd(&hi[c], q >> 13);
+}
+
 template <int D, int MODE, bool AGG>
 __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restrict__ pos4,
                                                       const unsigned *__restrict__ mmax_bits, DepositArgs a,
@@ -449,8 +463,9 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   const int PS = fft_row_stride(G / 2);       // padded transform rows
   const size_t region = (size_t)RR * 2 * PS * 8;  // >= RR * G * 8: accumulator, then transform scratch
 
-  // [accumulator / transform scratch: region][fp32 rows: RR*RS*4][twiddles]
-  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem);
+  // [accumulator halves lo, hi / transform scratch: region][fp32 rows: RR*RS*4][twiddles]
+  uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem);
+  uint32_t *acc_hi = acc_lo + (size_t)RR * G;
   float *rows = reinterpret_cast<float *>(smem + region);
   float2 *tw = reinterpret_cast<float2 *>(smem + region + (size_t)RR * RS * 4);
 
@@ -466,7 +481,7 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
       s_row[tid - 1] = t.z;
     }
   }
-  for (int e = tid; e < RR * G; e += nt) acc[e] = 0ull;
+  for (int e = tid; e < RR * G / 2; e += nt) reinterpret_cast<uint4 *>(acc_lo)[e] = make_uint4(0u, 0u, 0u, 0u);
   if (MODE != 0)
     for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
   __syncthreads();
@@ -577,16 +592,16 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
           if (agg) {
             const unsigned peers = __match_any_sync(0xffffffffu, key);
             if (key != 0xffffffffu) {
-              const uint32_t s0q = __reduce_add_sync(peers, q0);
+              const uint32_t s0q = __reduce_add_sync(peers, q0);  // < 32 * 2^26
               const uint32_t s1q = __reduce_add_sync(peers, q1);
               if (lane == __ffs(peers) - 1) {
-                if (s0q) atomicAdd(&acc[c0], (unsigned long long)s0q);
-                if (s1q) atomicAdd(&acc[c1], (unsigned long long)s1q);
+                dep_add(acc_lo, acc_hi, c0, s0q);
+                dep_add(acc_lo, acc_hi, c1, s1q);
               }
             }
           } else if (key != 0xffffffffu) {
-            if (q0) atomicAdd(&acc[c0], (unsigned long long)q0);
-            if (q1) atomicAdd(&acc[c1], (unsigned long long)q1);
+            dep_add(acc_lo, acc_hi, c0, q0);
+            dep_add(acc_lo, acc_hi, c1, q1);
           }
         }
       }
@@ -594,24 +609,21 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   }
   __syncthreads();
 
+  unsigned long long *gtile = nullptr;
   if (nparts > 1) {
-    // publish this part's tile, then let the last part to arrive sum all of them
-    const size_t tile = (size_t)RR * G;
-    unsigned long long *mine = scratch + (size_t)(slot_off[blk] + part) * tile;
-    for (int e = tid; e < RR * G; e += nt) mine[e] = acc[e];
+    // add this part's sums into the block's 64-bit tile; the last part to arrive converts it
+    gtile = scratch + (size_t)slot_off[blk] * ((size_t)RR * G);
+    for (int e = tid; e < RR * G; e += nt) {
+      const unsigned long long v = ((unsigned long long)acc_hi[e] << 13) + acc_lo[e];
+      if (v) atomicAdd(&gtile[e], v);
+    }
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = (atomicAdd(&counters[blk], 1u) == nparts - 1) ? 1 : 0;
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    for (uint32_t o = 0; o < nparts; ++o) {
-      if (o == part) continue;
-      const unsigned long long *other = scratch + (size_t)(slot_off[blk] + o) * tile;
-      for (int e = tid; e < RR * G; e += nt) acc[e] += __ldcg(&other[e]);
-    }
     if (tid == 0) counters[blk] = 0u;
-    __syncthreads();
   }
 
   // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
@@ -619,7 +631,13 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
     int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
     // u64 -> f32 rounds correctly either way; the 32-bit conversion is a fast FP32-pipe
     // instruction, the 64-bit one is not on this part and is only needed for sums >= 2^32
-    const unsigned long long q = acc[e];
+    unsigned long long q;
+    if (gtile) {  // the split block's total, and the tile cleared for the next call
+      q = __ldcg(&gtile[e]);
+      gtile[e] = 0ull;
+    } else {
+      q = ((unsigned long long)acc_hi[e] << 13) + acc_lo[e];
+    }
     const float fq = (q >> 32) ? __ull2float_rn(q) : __uint2float_rn((unsigned)q);
     float v = __fmul_rn(fq, qs.outscale);
     if (MODE != 1) {

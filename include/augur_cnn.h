@@ -54,16 +54,31 @@ int augur_cnn_conv_in_tc(const void *x, const void *w_umma, const float *bias, i
                          void *h0, unsigned *err, void *stream);
 
 /*
- * Weight and bias gradients (fixed-order reduction of per-CTA partial sums):
- *   kind 0: 32 -> 32 layer, h (bf16, 32 ch) and dz (bf16, 32 ch)
- *   kind 1: output layer, h3 (bf16, 32 ch) and the output gradient as a float4 grid (4 channels,
- *           the 4th must be zero)
- *   kind 2: input layer, x (bf16, 2 ch) and dz0 (bf16, 32 ch)
- * out receives N*27*CIN weight gradients in w[n][tap][c] order, then N bias gradients.
- * partial: scratch of max_parts * (N*27*CIN + N) floats.
+ * Weight and bias gradients (fixed-order reduction of per-CTA partial sums; the reference's
+ * autograd through nn.Conv3d, scripts/train_scatter_field.py:224-228):
+ *   kind 0: 32 -> 32 layer on tcgen05, h (bf16, 32 ch) and dz (bf16, 32 ch)
+ *   kind 1: output layer on the CUDA cores, h3 (bf16, 32 ch) and the output gradient as a float4
+ *           grid (4 channels, the 4th must be zero)
+ *   kind 2: input layer on the CUDA cores, x (bf16, 2 ch) and dz0 (bf16, 32 ch)
+ *   kind 3: output layer on tcgen05, h3 (bf16, 32 ch) and the 16-channel bf16 output gradient
+ *           written by augur_cnn_pack_dout (channels 3..15 zero)
+ *   kind 4: kind 0 on the CUDA cores (the same sums in another order)
+ * out receives N*27*CIN weight gradients in w[n][tap][c] order, then N bias gradients (N = 4 for
+ * the output layer, whose 4th channel is zero). partial: scratch of max_parts * (N*27*CIN + N)
+ * floats. err: error word of the tensor-core kinds (bit 4: a bounded wait ran out), may be NULL
+ * for kinds 1, 2 and 4.
  */
 int augur_cnn_wgrad(int kind, const void *h, const void *dz, int batch, int grid, float *partial, int max_parts,
-                    float *out, void *stream);
+                    float *out, unsigned *err, void *stream);
+
+/*
+ * Tries of every bounded pipeline wait in the tensor-core kernels launched after this call
+ * (process-wide; the default is 2^20 = 1048576). Returns the previous value, so a caller can
+ * restore it. A kernel whose wait runs out leaves its loops, waits (with a fixed bound) for its
+ * own copies and MMAs in flight, frees its TMEM and raises bit 4 of its error word; with 0 tries
+ * every pipeline wait gives up at once, which exercises that path. No counterpart in the reference.
+ */
+unsigned augur_cnn_set_wait_budget(unsigned tries);
 
 /*
  * fp32 w[n][tap][c] (n < n_out, c < c_in) -> bf16 tensor-core operand with cin_pad

@@ -76,7 +76,7 @@ int64_t augur_pm_plan_workspace_bytes(const augur_pm_plan *plan);
 typedef struct augur_pm_tiles {
   int deposit_rows_y; /* y rows per deposit row block; divides grid */
   int deposit_rows_z; /* z planes per deposit row block; 3D: 1..15 dividing grid, 2D: 1 */
-  int deposit_chunk;  /* minimum bodies per deposit work item, 1024 .. 2^24 */
+  int deposit_chunk;  /* minimum bodies per deposit work item, 1024 .. 2^19 */
   int green_tile_y;   /* y columns per z-transform + Green block: 8 or 16, divides grid */
   int c2r_rows;       /* x rows per C2R block: power of two <= 32 */
   int fft_rows;       /* rows per y-transform block: 1..256 */

@@ -174,3 +174,84 @@ def test_tensor_core_input_layer_matches_cuda_core_layer(B, G):
     net._call("augur_cnn_conv_in_tc", xd.data_ptr(), net.op_in.data_ptr(), net.view["b_in"].data_ptr(), B, G,
               None, h2.data_ptr(), net.err.data_ptr())
     assert torch.equal(h2, h_tc)
+
+
+def _wgrad(net, kind, h, dz, B, G, nout):
+    parts = 4 * 152
+    partial = torch.empty(parts * (nout * 27 * 32 + nout), dtype=torch.float32, device=DEV)
+    out = torch.empty(nout * 27 * 32 + nout, dtype=torch.float32, device=DEV)
+    net._call("augur_cnn_wgrad", kind, h.data_ptr(), dz.data_ptr(), B, G, partial.data_ptr(), parts, out.data_ptr(),
+              net.err.data_ptr())
+    net.check()
+    return out
+
+
+@pytest.mark.parametrize("B,G", [(1, 16), (2, 20), (1, 130)])
+def test_wgrad_tensor_cores_match_cuda_cores_and_float64(B, G):
+    """Weight and bias gradients of a 32 -> 32 layer on tcgen05 (kind 0) against the CUDA-core kernel
+    (kind 4, the same fp32 sums of exact bf16 products in another order) and, at the small grid,
+    against a float64 restatement dW[n][tap][c] = sum_v dz[v][n] h[v + tap][c]."""
+    net = make_net(seed=21)
+    g = torch.Generator().manual_seed(B * 100 + G)
+    nv = B * G ** 3
+    h = torch.randn(nv * 32, generator=g).to(torch.bfloat16).to(DEV)
+    dz = (torch.randn(nv * 32, generator=g) * 0.1).to(torch.bfloat16).to(DEV)
+    tc = _wgrad(net, 0, h, dz, B, G, 32).cpu().double()
+    cc = _wgrad(net, 4, h, dz, B, G, 32).cpu().double()
+    assert rel_rms(tc, cc) < 1e-4  # fp32 sums over up to 2.2M voxels in two orders
+    if G <= 20:
+        hh = h.cpu().double().view(B, G, G, G, 32)
+        dd = dz.cpu().double().view(B, G, G, G, 32)
+        hp = F.pad(hh.permute(0, 4, 1, 2, 3), (1, 1, 1, 1, 1, 1)).permute(0, 2, 3, 4, 1)
+        ref = torch.empty(32, 27, 32, dtype=torch.float64)
+        for tap in range(27):
+            oz, oy, ox = tap // 9, (tap // 3) % 3, tap % 3
+            sh = hp[:, oz:oz + G, oy:oy + G, ox:ox + G, :]
+            ref[:, tap, :] = torch.einsum("bzyxn,bzyxc->nc", dd, sh)
+        ref = torch.cat([ref.reshape(-1), dd.sum((0, 1, 2, 3))])
+        assert rel_rms(tc, ref) < 1e-5
+
+
+@pytest.mark.parametrize("B,G", [(1, 16), (1, 130)])
+def test_wgrad_output_layer_tensor_cores(B, G):
+    """Output-layer gradients on tcgen05 from the packed 16-channel bf16 gradient (kind 3) against the
+    CUDA-core kernel on the same bf16-rounded values as an fp32 float4 grid (kind 1)."""
+    net = make_net(seed=22)
+    g = torch.Generator().manual_seed(G)
+    nv = B * G ** 3
+    h = torch.randn(nv * 32, generator=g).to(torch.bfloat16).to(DEV)
+    d4 = torch.zeros(nv, 4)
+    d4[:, :3] = torch.randn(nv, 3, generator=g)
+    d4 = d4.to(DEV)
+    d16 = torch.empty(nv * 16, dtype=torch.bfloat16, device=DEV)
+    net._call("augur_cnn_pack_dout", d4.data_ptr(), nv, 1.0, d16.data_ptr())
+    d4r = torch.zeros(nv, 4, device=DEV)
+    d4r[:, :3] = d16.view(nv, 16)[:, :3].float()
+    tc = _wgrad(net, 3, h, d16, B, G, 4).cpu().double()
+    cc = _wgrad(net, 1, h, d4r, B, G, 4).cpu().double()
+    assert rel_rms(tc, cc) < 1e-4  # fp32 sums over up to 2.2M voxels in two orders
+    assert float(tc[3 * 27 * 32:4 * 27 * 32].abs().max()) == 0.0 and float(tc[-1]) == 0.0
+
+
+def test_wait_budget_expiry_is_reported_and_recovers():
+    """With a wait budget of zero every pipeline wait of the tensor-core kernels gives up at once: the
+    kernels leave their loops, drain their own copies and MMAs, free TMEM and raise the timeout bit,
+    which GridCNN.check() reports. The next launches with the default budget are unaffected."""
+    net = make_net(seed=23)
+    B, G = 1, 24
+    x, xd = inputs(B, G, seed=6)
+    good = torch.zeros(B * G ** 3 * 4, device=DEV)
+    net.forward(xd, B, G, good)
+    net.check()
+    prev = net.lib.augur_cnn_set_wait_budget(0)
+    try:
+        field = torch.zeros_like(good)
+        net.forward(xd, B, G, field)
+        with pytest.raises(RuntimeError, match="ran out of its budget"):
+            net.check()
+    finally:
+        net.lib.augur_cnn_set_wait_budget(prev)
+    again = torch.zeros_like(good)
+    net.forward(xd, B, G, again)
+    net.check()
+    assert torch.equal(again, good)
