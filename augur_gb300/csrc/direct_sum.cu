@@ -5,8 +5,9 @@
 //   a_t = sum_j m_j (x_j - x_t) * (|x_j - x_t|^2 + eps^2)^-1.5 , self pair excluded.
 // Periodic (box > 0, D = 3): minimum-image softened Newtonian pair force plus the Ewald
 // correction (periodic sum minus the nearest-image Newtonian term) for a unit mass,
-// tabulated once per device on a 65^3 grid over the positive octant of [0, 1/2]^3 and
-// interpolated trilinearly (the correction is odd in each displacement component).
+// tabulated once per device (FP64 sums, stored as fp32) on a 65^3 grid over the positive octant
+// of [0, 1/2]^3 and interpolated trilinearly in fp32 (the correction is odd in each displacement
+// component); the Newtonian pair sum is FP64 throughout.
 // The Ewald sum uses alpha = 2, real-space images |n_i| <= 2, k-space |h|^2 <= 10
 // (Hernquist, Bouchet & Suto 1991, ApJS 75, 231).
 //
@@ -27,7 +28,9 @@ constexpr int DS_TILE = 512;
 constexpr int EW_N = 64;  // intervals per axis of the correction table over [0, 1/2]
 constexpr int EW_P = EW_N + 1;
 
-__device__ __forceinline__ double wrap_min_image(double d, double box) { return d - box * rint(d / box); }
+__device__ __forceinline__ double wrap_min_image(double d, double box, double inv_box) {
+  return d - box * rint(d * inv_box);
+}
 
 // Ewald correction for a unit mass at the origin, unit box, displacement x in [0, 1/2]^3.
 __global__ void ewald_table_kernel(double *__restrict__ tab) {
@@ -71,41 +74,50 @@ __global__ void ewald_table_kernel(double *__restrict__ tab) {
   for (int c = 0; c < 3; ++c) tab[(size_t)e * 3 + c] = a[c];
 }
 
-__device__ __forceinline__ void ewald_corr(const double *__restrict__ tab, const double d[3], double box, double out[3]) {
+// The Ewald correction is interpolated in fp32 from an fp32 copy of the table: it is a small part
+// of the force (its size relative to the Newtonian sum is below ~1e-1 in these scenes), so fp32's
+// relative rounding (~1e-7) moves the total by ~1e-8, below the table's own interpolation error
+// (~1e-6), while FP64 arithmetic on this part runs several times slower.
+__device__ __forceinline__ void ewald_corr(const float *__restrict__ tab, const double d[3], double inv_box,
+                                           double out[3]) {
   // d is the minimum-image displacement source - target: the acceleration of the
   // target is the unit-box correction evaluated at u = (target - source)/box, scaled by 1/box^2
-  double u[3], s[3];
+  float u[3], s[3];
   for (int c = 0; c < 3; ++c) {
-    double t = -d[c] / box;
-    s[c] = t < 0.0 ? -1.0 : 1.0;
-    u[c] = fabs(t) * (2.0 * EW_N);
-    if (u[c] > EW_N) u[c] = EW_N;
+    const float t = (float)(-d[c] * inv_box);
+    s[c] = t < 0.f ? -1.f : 1.f;
+    u[c] = fminf(fabsf(t) * (2.f * EW_N), (float)EW_N);
   }
   int i[3];
-  double f[3];
+  float f[3];
   for (int c = 0; c < 3; ++c) {
     int k = (int)u[c];
     if (k >= EW_N) k = EW_N - 1;
     i[c] = k;
-    f[c] = u[c] - k;
+    f[c] = u[c] - (float)k;
   }
-  double r[3] = {0.0, 0.0, 0.0};
+  float r[3] = {0.f, 0.f, 0.f};
   for (int dz = 0; dz < 2; ++dz)
     for (int dy = 0; dy < 2; ++dy)
       for (int dx = 0; dx < 2; ++dx) {
-        double w = (dx ? f[0] : 1.0 - f[0]) * (dy ? f[1] : 1.0 - f[1]) * (dz ? f[2] : 1.0 - f[2]);
-        size_t e = ((size_t)(i[2] + dz) * EW_P + (i[1] + dy)) * EW_P + (i[0] + dx);
-        for (int c = 0; c < 3; ++c) r[c] += w * tab[e * 3 + c];
+        const float w = (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) * (dz ? f[2] : 1.f - f[2]);
+        const size_t e = ((size_t)(i[2] + dz) * EW_P + (i[1] + dy)) * EW_P + (i[0] + dx);
+        for (int c = 0; c < 3; ++c) r[c] += w * __ldg(&tab[e * 3 + c]);
       }
-  const double inv_b2 = 1.0 / (box * box);
-  for (int c = 0; c < 3; ++c) out[c] = s[c] * r[c] * inv_b2;
+  const double inv_b2 = inv_box * inv_box;
+  for (int c = 0; c < 3; ++c) out[c] = (double)(s[c] * r[c]) * inv_b2;
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ in, int n, float *__restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) out[e] = (float)in[e];
 }
 
 template <int D, bool PERIODIC>
 __global__ void __launch_bounds__(DS_THREADS) direct_sum_partial_kernel(
     const double *__restrict__ tg, const int64_t *__restrict__ tidx, int64_t T, const double *__restrict__ src,
     const double *__restrict__ mass, int64_t N, int64_t chunk, double eps2, double box,
-    const double *__restrict__ ewtab, double *__restrict__ partial) {
+    const float *__restrict__ ewtab, double *__restrict__ partial) {
   __shared__ double sp[DS_TILE][4];
   const int64_t t = (int64_t)blockIdx.x * DS_THREADS + threadIdx.x;
   const int64_t s0 = (int64_t)blockIdx.y * chunk;
@@ -117,6 +129,7 @@ __global__ void __launch_bounds__(DS_THREADS) direct_sum_partial_kernel(
     if (tidx) self = tidx[t];
   }
   double a[3] = {0.0, 0.0, 0.0};
+  const double inv_box = PERIODIC ? 1.0 / box : 0.0;
   for (int64_t b = s0; b < s1; b += DS_TILE) {
     const int nb = (int)min((int64_t)DS_TILE, s1 - b);
     __syncthreads();
@@ -131,14 +144,14 @@ __global__ void __launch_bounds__(DS_THREADS) direct_sum_partial_kernel(
         double d[3];
         for (int c = 0; c < 3; ++c) d[c] = sp[k][c] - x[c];
         if (PERIODIC)
-          for (int c = 0; c < 3; ++c) d[c] = wrap_min_image(d[c], box);
+          for (int c = 0; c < 3; ++c) d[c] = wrap_min_image(d[c], box, inv_box);
         double r2 = d[0] * d[0] + d[1] * d[1] + (D == 3 ? d[2] * d[2] : 0.0) + eps2;
         double inv = rsqrt(r2);
         double f = sp[k][3] * inv * inv * inv;
         for (int c = 0; c < D; ++c) a[c] += d[c] * f;
         if (PERIODIC) {
           double cr[3];
-          ewald_corr(ewtab, d, box, cr);
+          ewald_corr(ewtab, d, inv_box, cr);
           for (int c = 0; c < 3; ++c) a[c] += sp[k][3] * cr[c];
         }
       }
@@ -156,23 +169,33 @@ __global__ void sum_partials_kernel(const double *__restrict__ partial, int spli
   out[e] = s;
 }
 
-double *g_ewald[64] = {nullptr};
+float *g_ewald[64] = {nullptr};
 std::mutex g_ewald_mu;
 
-int ewald_table(double **out) {
+// The correction table of the current device (fp32 copy of the FP64-evaluated sums), built once
+// per device; a device reset in the process makes the cached pointer stale.
+int ewald_table(float **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return AUGUR_ECUDA;
   std::lock_guard<std::mutex> lk(g_ewald_mu);
   if (!g_ewald[dev]) {
+    const int n = EW_P * EW_P * EW_P;
     double *t = nullptr;
-    if (cudaMalloc(&t, sizeof(double) * 3 * EW_P * EW_P * EW_P) != cudaSuccess) return AUGUR_ENOMEM;
-    int n = EW_P * EW_P * EW_P;
-    ewald_table_kernel<<<(n + 127) / 128, 128>>>(t);
-    if (cudaDeviceSynchronize() != cudaSuccess) {
+    float *t32 = nullptr;
+    if (cudaMalloc(&t, sizeof(double) * 3 * n) != cudaSuccess) return AUGUR_ENOMEM;
+    if (cudaMalloc(&t32, sizeof(float) * 3 * n) != cudaSuccess) {
       cudaFree(t);
+      return AUGUR_ENOMEM;
+    }
+    ewald_table_kernel<<<(n + 127) / 128, 128>>>(t);
+    to_f32_kernel<<<(3 * n + 255) / 256, 256>>>(t, 3 * n, t32);
+    const bool ok = cudaDeviceSynchronize() == cudaSuccess;
+    cudaFree(t);
+    if (!ok) {
+      cudaFree(t32);
       return AUGUR_ECUDA;
     }
-    g_ewald[dev] = t;
+    g_ewald[dev] = t32;
   }
   *out = g_ewald[dev];
   return AUGUR_OK;
@@ -339,9 +362,9 @@ int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t T
   if (T == 0) return AUGUR_OK;
   if (!targets || !acc_out || (N > 0 && !sources)) return AUGUR_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
-  const double *ewtab = nullptr;
+  const float *ewtab = nullptr;
   if (box > 0.0) {
-    double *t = nullptr;
+    float *t = nullptr;
     int rc = ewald_table(&t);
     if (rc) return rc;
     ewtab = t;

@@ -251,35 +251,34 @@ int deposit_rho(augur_pm_plan *p, float *rho, cudaStream_t st) {
   return p->dim == 3 ? launch_deposit<3, 0>(p, rho, nullptr, st) : launch_deposit<2, 0>(p, rho, nullptr, st);
 }
 
+size_t rowst_smem(const augur_pm_plan *p) {
+  return 128 + (size_t)ROWST_STAGES * p->rows_RB * p->L * 8 +
+         (size_t)(fft_nstages(p->L) > 2 ? 2 : 1) * p->rows_RB * fft_row_stride(p->L) * 8 + (size_t)p->Lt * 8;
+}
+
 int fft_rows(augur_pm_plan *p, float2 *data, int64_t nrows, bool inverse, cudaStream_t st) {
   const int L = p->L;
   const int RB = p->rows_RB;
+  // persistent bulk-copy form: multi-stage lengths, 16-byte aligned rows
+  if (L >= 32 && (reinterpret_cast<uintptr_t>(data) & 15) == 0 && rowst_smem(p) <= p->smem_max &&
+      !raise_dyn_smem((const void *)rows_tma_kernel, rowst_smem(p))) {
+    const int64_t nbatch = (nrows + RB - 1) / RB;
+    const int per_sm = rowst_smem(p) * 2 + 4096 <= p->smem_max + 1024 ? 2 : 1;  // 228 KB per SM
+    const int grid = (int)std::min<int64_t>(nbatch, (int64_t)per_sm * current_sm_count());
+    rows_tma_kernel<<<grid, 256, rowst_smem(p), st>>>(data, nrows, RB, L, p->Lt / L, p->Lt, p->tw, inverse ? 1 : 0,
+                                                      p->d_err);
+    AUGUR_LAUNCH_CHECK(p);
+    return AUGUR_OK;
+  }
   fft_rows_kernel<<<blocks_for(nrows, RB), 256, p->smem_rows, st>>>(data, nrows, RB, L, make_fastdiv(L), p->Lt / L,
                                                                      p->Lt, p->tw, inverse ? 1 : 0);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
 
-// periodic 3D: spec (after R2C along x) -> F4 force grid
-int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
+// x C2R of ncomp gradient spectra (spec3) into the float4 force grid
+int launch_c2r(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   const int G = p->G, M = p->M;
-  int rc = fft_rows(p, p->spec, (int64_t)(M + 1) * G, false, st);
-  if (rc) return rc;
-  GreenArgs ga;
-  ga.G = G;
-  ga.TY = p->green_TY;
-  ga.ncomp = ncomp;
-  ga.Lt = p->Lt;
-  ga.fsh = p->sh_L;
-  ga.kfund = (float)(2.0 * M_PI / p->extent);
-  ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
-  if (p->green_TY == 16)
-    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
-  else
-    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
-  AUGUR_LAUNCH_CHECK(p);
-  rc = fft_rows(p, p->spec3, (int64_t)ncomp * (M + 1) * G, true, st);
-  if (rc) return rc;
   C2RArgs ca{};
   ca.L = G;
   ca.nrows = G * G;
@@ -298,6 +297,35 @@ int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
                                                                                  reinterpret_cast<float *>(F4));
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
+}
+
+// z transform + Green's function + spectral gradient of spec into ncomp spectra (spec3)
+int launch_green(augur_pm_plan *p, int ncomp, cudaStream_t st) {
+  const int G = p->G, M = p->M;
+  GreenArgs ga;
+  ga.G = G;
+  ga.TY = p->green_TY;
+  ga.ncomp = ncomp;
+  ga.Lt = p->Lt;
+  ga.fsh = p->sh_L;
+  ga.kfund = (float)(2.0 * M_PI / p->extent);
+  ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
+  if (p->green_TY == 16)
+    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+  else
+    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+// periodic 3D: spec (after R2C along x) -> F4 force grid
+int periodic_tail(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
+  const int G = p->G, M = p->M;
+  int rc = fft_rows(p, p->spec, (int64_t)(M + 1) * G, false, st);
+  if (!rc) rc = launch_green(p, ncomp, st);
+  if (!rc) rc = fft_rows(p, p->spec3, (int64_t)ncomp * (M + 1) * G, true, st);
+  if (!rc) rc = launch_c2r(p, ncomp, F4, st);
+  return rc;
 }
 
 int r2c_rows(augur_pm_plan *p, const float *in, int Lin, int nin, int nout, float2 *out, cudaStream_t st) {
@@ -1129,46 +1157,11 @@ int augur_pm_run_profile(augur_pm_plan *p, int k, float *stage_ms, int nstage, v
     cudaEventRecord(ev[2], st);
     if (!rc) rc = fft_rows(p, p->spec, (int64_t)(M + 1) * G, false, st);
     cudaEventRecord(ev[3], st);
-    if (!rc) {
-      GreenArgs ga;
-      ga.G = G;
-      ga.TY = p->green_TY;
-      ga.ncomp = 3;
-      ga.Lt = p->Lt;
-      ga.fsh = p->sh_L;
-      ga.kfund = (float)(2.0 * M_PI / p->extent);
-      ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
-      if (p->green_TY == 16)
-        fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
-                                                                                          p->spec3);
-      else
-        fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw,
-                                                                                         p->spec3);
-    }
+    if (!rc) rc = launch_green(p, 3, st);
     cudaEventRecord(ev[4], st);
     if (!rc) rc = fft_rows(p, p->spec3, (int64_t)3 * (M + 1) * G, true, st);
     cudaEventRecord(ev[5], st);
-    if (!rc) {
-      C2RArgs ca{};
-      ca.L = G;
-      ca.nrows = G * G;
-      ca.RB = p->c2r_RB;
-      ca.ncomp = 3;
-      ca.Lt = p->Lt;
-      ca.nkeep = G * G;
-      ca.Lkeep = G;
-      ca.scale = 1.f;
-      ca.fsh = p->sh_M;
-      ca.twmul = p->Lt / M;
-      ca.fdRB = make_fastdiv(ca.RB);
-      ca.fdM = make_fastdiv(ca.L / 2);
-      ca.fdL = make_fastdiv(ca.L);
-  ca.fdRB = make_fastdiv(ca.RB);
-  ca.fdM = make_fastdiv(ca.L / 2);
-  ca.fdL = make_fastdiv(ca.L);
-      c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, p->smem_c2r, st>>>(
-          p->spec3, ca, p->tw, reinterpret_cast<float *>(p->F4));
-    }
+    if (!rc) rc = launch_c2r(p, 3, p->F4, st);
     cudaEventRecord(ev[6], st);
     if (!rc) rc = run_gather(p, p->run_dt, 1, nullptr, st);
     cudaEventRecord(ev[7], st);

@@ -17,6 +17,23 @@
 namespace augur {
 
 constexpr int SCAN_TILE = 4096;  // rows per local scan tile (1024 threads x 4)
+// tries of a bounded mbarrier wait in the TMA-fed kernels, and of the wait for a CTA's own copies
+// in flight before it exits after giving up
+constexpr uint32_t PM_WAIT_BUDGET = 1u << 20;
+constexpr uint32_t PM_DRAIN_BUDGET = 1u << 22;
+
+// The dynamic shared memory of the TMA-fed kernels, rounded up to a 128-byte boundary in the shared
+// window (their launches request 128 bytes more than they use).
+__device__ __forceinline__ unsigned char *smem_align128(unsigned char *p) {
+  const uint32_t a = smem_u32(p);
+  return p + (((a + 127u) & ~127u) - a);
+}
+// Checks a copy's addresses before it is issued: the shared destination or source 128-byte aligned
+// (16 for plain bulk copies), the global address and byte count 16-byte aligned. A copy that fails
+// is not issued; the caller raises AUGUR_ERRBIT_RANGE and gives up (its waits would never end).
+__device__ __forceinline__ bool copy_ok(uint32_t s_addr, uint32_t s_align, const void *g, uint32_t bytes) {
+  return (s_addr & (s_align - 1u)) == 0u && (reinterpret_cast<uintptr_t>(g) & 15u) == 0u && (bytes & 15u) == 0u;
+}
 constexpr int MAXSEG = 64;
 
 struct GridParams {
@@ -762,6 +779,85 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data
   auto ld = [&](int b, int e) -> float2 { return base[(size_t)b * L + e]; };
   auto st = [&](int b, int e, float2 v) { base[(size_t)b * L + e] = v; };
   AUGUR_FFT_IO(L, 0, nr, ld, st, A, B, LS, tw, twmul, inverse != 0);
+}
+
+// Row transforms (fft_rows_kernel) as a persistent kernel fed by bulk copies: the CTA takes row
+// batches blockIdx.x, + gridDim.x, ...; thread 0 keeps two batches' rows (contiguous, RB * L
+// complex) in flight into a two-slot ring, the first stage reads them from the slot, the last
+// stage writes the transformed rows back to global memory in place. Needs a multi-stage length
+// (L >= 32). Bounded waits as c2r_tma_kernel.
+constexpr int ROWST_STAGES = 2;
+__global__ void __launch_bounds__(256, 2) rows_tma_kernel(float2 *__restrict__ data, int64_t nrows, int RB, int L,
+                                                          int twmul, int Lt, const float2 *__restrict__ twg,
+                                                          int inverse, unsigned *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *smem = smem_align128(smem_raw);
+  __shared__ __align__(8) uint64_t full[ROWST_STAGES];
+  __shared__ int s_issued, s_bad;  // copies thread 0 has issued; a copy that failed copy_ok()
+  const int LS = fft_row_stride(L);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const size_t slot_elems = (size_t)RB * L;
+  float2 *ring = reinterpret_cast<float2 *>(smem);
+  float2 *A = ring + ROWST_STAGES * slot_elems;  // transforms of two stages only use B
+  float2 *B = A + (fft_nstages(L) > 2 ? (size_t)RB * LS : 0);
+  float2 *tw = B + (size_t)RB * LS;
+  const int64_t nbatch = (nrows + RB - 1) / RB;
+  const int nmine = (int64_t)blockIdx.x < nbatch ? (int)((nbatch - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  auto rows_of = [&](int i, int64_t &r0) {
+    r0 = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * RB;
+    return (int)min((int64_t)RB, nrows - r0);
+  };
+  auto issue = [&](int i) {  // thread 0: batch i into its slot, unless its addresses fail the check
+    int64_t r0;
+    const int nr = rows_of(i, r0);
+    const int slot = i % ROWST_STAGES;
+    const uint32_t bytes = (uint32_t)nr * L * 8u;
+    const uint32_t dst = smem_u32(ring + slot * slot_elems);
+    if (!copy_ok(dst, 16u, data + r0 * L, bytes)) {
+      s_bad = 1;
+      return;
+    }
+    mbar_expect_tx(&full[slot], bytes);
+    bulk_load(dst, data + r0 * L, bytes, &full[slot]);
+    s_issued = i + 1;
+  };
+  if (tid == 0) {
+    for (int i = 0; i < ROWST_STAGES; ++i) mbar_init(&full[i], 1);
+    s_issued = 0;
+    s_bad = 0;
+    mbar_fence_init();
+    for (int i = 0; i < min(nmine, ROWST_STAGES) && !s_bad; ++i) issue(i);
+  }
+  for (int e = tid; e < Lt; e += nt) tw[e] = twg[e];
+  __syncthreads();
+  int i = 0;
+  bool abort = false;
+  for (; i < nmine; ++i) {
+    const int slot = i % ROWST_STAGES;
+    int64_t r0;
+    const int nr = rows_of(i, r0);
+    const bool ok = i < s_issued && mbar_wait_bounded(&full[slot], (uint32_t)(i / ROWST_STAGES) & 1u, PM_WAIT_BUDGET);
+    if (__syncthreads_or(!ok)) {
+      abort = true;
+      break;
+    }
+    const float2 *S = ring + slot * slot_elems;
+    float2 *base = data + r0 * L;
+    auto ld = [&](int b, int e) -> float2 { return S[(size_t)b * L + e]; };
+    auto st = [&](int b, int e, float2 v) { base[(size_t)b * L + e] = v; };
+    AUGUR_FFT_IO(L, 0, nr, ld, st, A, B, LS, tw, twmul, inverse != 0);
+    // the slot was read by the first stage (a barrier ago): hand it to the copy engine again
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0 && i + ROWST_STAGES < nmine && !s_bad) issue(i + ROWST_STAGES);
+  }
+  if (tid == 0) {
+    for (int r = i; r < s_issued; ++r)  // every copy issued lands before the CTA exits
+      if (!mbar_wait_bounded(&full[r % ROWST_STAGES], (uint32_t)(r / ROWST_STAGES) & 1u, PM_DRAIN_BUDGET))
+        abort = true;
+    if (s_bad) atomicOr(err, AUGUR_ERRBIT_RANGE);
+    else if (abort) atomicOr(err, AUGUR_ERRBIT_TIMEOUT);
+  }
 }
 
 // 2D isolated, kpad = "ext" (scripts/scatter_field.py:286-288): the central difference reads the

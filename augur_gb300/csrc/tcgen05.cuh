@@ -164,37 +164,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
 }
 
 // ---- TMA and bulk copies --------------------------------------------------------------------
-// 3D tiled load into shared memory (coordinates innermost first), completing bytes on mbar. The
-// innermost coordinate times the element size must be a multiple of 16 bytes.
-__device__ __forceinline__ void tma_load3(uint32_t dst, const void *map, int c0, int c1, int c2, uint64_t *mbar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(mbar))
-      : "memory");
-}
-// 3D tiled store from shared memory (bulk group); coordinates must be in range and non-negative.
-__device__ __forceinline__ void tma_store3(const void *map, int c0, int c1, int c2, uint32_t src) {
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
-                   reinterpret_cast<uint64_t>(map)),
-               "r"(c0), "r"(c1), "r"(c2), "r"(src)
-               : "memory");
-}
-// Contiguous copies between shared and global memory: both addresses 16-byte aligned, bytes a
-// multiple of 16.
+// Contiguous copy from global to shared memory, completing bytes on mbar: both addresses 16-byte
+// aligned, bytes a multiple of 16.
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint64_t *mbar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                "l"(src), "r"(bytes), "r"(smem_u32(mbar))
                : "memory");
 }
-__device__ __forceinline__ void bulk_store(void *dst, uint32_t src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// the shared-memory sources of this thread's committed bulk stores have been read
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-// this thread's committed bulk stores are complete
-__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 }  // namespace augur

@@ -14,6 +14,9 @@ PM force (the reference's energy drift diagnostic, scripts/scatter_field.py:759-
 from __future__ import annotations
 
 import math
+import os
+import signal
+import threading
 import time
 
 import numpy as np
@@ -49,6 +52,63 @@ def make_snapshot(plan: PMPlan, net: GridCNN, kind: str, n: int, seed: int, n_ta
             "label": (truth - pm.double()).float()}
 
 
+def _scene_job(args):
+    kind, n, seed = args
+    pos, _, mass = scenes.make_scene(kind, n, seed=seed)
+    return pos, mass
+
+
+def make_truth(n: int, count: int, seed0: int, device, kinds=scenes.SCENES, n_targets: int = 8192,
+               eps: float = 1.0 / 256, workers: int = 0, log=None) -> list:
+    """The grid-independent half of a dataset: seeded scenes (kind i % len(kinds), seed seed0 + i)
+    kept on the device, the sampled target indices and the FP64 periodic direct-sum force at them.
+    label_snapshots() adds a grid's PM force and CNN input, so one truth serves every grid.
+    workers > 0 samples the scenes on that many host processes (spawned; no CUDA in them)."""
+    jobs = [(kinds[i % len(kinds)], n, seed0 + i) for i in range(count)]
+    if workers > 0:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+
+        ex = ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"))
+        it = ex.map(_scene_job, jobs, chunksize=4)
+    else:
+        ex, it = None, map(_scene_job, jobs)
+    out = []
+    t0 = time.time()
+    try:
+        for i, ((kind, _, seed), (pos, mass)) in enumerate(zip(jobs, it)):
+            p = torch.from_numpy(pos).to(device)
+            m = torch.from_numpy(mass).to(device)
+            rng = np.random.default_rng(seed + 17)
+            idx = torch.from_numpy(rng.choice(n, size=min(n_targets, n), replace=False)).to(device)
+            src = p.double()
+            truth = direct_sum_fp64(src[idx].contiguous(), src, m.double(), eps=eps, box=1.0,
+                                    target_index=idx.contiguous())
+            out.append({"kind": kind, "seed": seed, "pos": p, "mass": m, "idx": idx, "truth64": truth})
+            if log and (i + 1) % max(1, count // 10) == 0:
+                log(f"truth {i + 1}/{count} ({time.time() - t0:.1f} s)")
+    finally:
+        if ex is not None:
+            ex.shutdown()
+    return out
+
+
+def label_snapshots(plan: PMPlan, net: GridCNN, truths: list) -> list:
+    """Snapshots on plan's grid from make_truth() entries: CNN input, target positions, PM force and
+    the (FP64 direct sum - PM) label, as make_snapshot() returns them."""
+    out = []
+    for t in truths:
+        p, m = t["pos"], t["mass"]
+        ones = torch.ones(p.shape[0], device=p.device)
+        rho = plan.deposit(p, m, ones)
+        F4 = plan.poisson(rho)
+        tpos = p[t["idx"]].contiguous()
+        pm, _ = plan.gather(F4, tpos)
+        out.append({"kind": t["kind"], "seed": t["seed"], "x": net.input(rho, F4), "tpos": tpos, "pm": pm,
+                    "truth": t["truth64"].float(), "label": (t["truth64"] - pm.double()).float()})
+    return out
+
+
 def make_dataset(plan, net, n, count, seed0, kinds=scenes.SCENES, n_targets=8192, eps=1.0 / 256, log=None):
     out = []
     t0 = time.time()
@@ -68,12 +128,54 @@ def _predict(plan: PMPlan, field: torch.Tensor, B: int, snaps) -> list:
     return [plan.gather(f[b], s["tpos"])[0] for b, s in enumerate(snaps)]
 
 
+def save_checkpoint(path: str, state: dict) -> None:
+    """Writes state with torch.save to path + '.tmp' and renames it over path, so a reader (or a
+    resumed run) sees the previous checkpoint or the new one, never a partial file
+    (save_atomic, scripts/train_scatter_field.py:132-134)."""
+    tmp = str(path) + ".tmp"
+    torch.save(state, tmp)
+    os.replace(tmp, path)
+
+
+def load_checkpoint(path: str):
+    """The state save_checkpoint wrote, or None when there is none."""
+    if not path or not os.path.exists(path):
+        return None
+    return torch.load(path, map_location="cpu", weights_only=False)
+
+
+class _StopFlag:
+    """Set by SIGTERM while installed (main thread only): the loop saves and returns."""
+
+    def __init__(self):
+        self.set = False
+        self._prev = None
+
+    def __enter__(self):
+        if threading.current_thread() is threading.main_thread():
+            self._prev = signal.signal(signal.SIGTERM, self._handler)
+        return self
+
+    def _handler(self, signum, frame):
+        self.set = True
+
+    def __exit__(self, *exc):
+        if self._prev is not None:
+            signal.signal(signal.SIGTERM, self._prev)
+        return False
+
+
 def train(net: GridCNN, plan: PMPlan, data: list, steps: int, batch: int = 4, lr: float = 3e-4,
           weight_decay: float = 0.01, seed: int = 4738, log=None, log_every: int = 100, clip: float = 1.0,
-          warmup: int = 50) -> list:
+          warmup: int = 50, checkpoint: str | None = None, checkpoint_every: int = 1000) -> list:
     """AdamW on loss = mean over the batch's snapshots of sum |pred - label|^2 / sum |label|^2, with
     linear warm-up then cosine decay of the learning rate, gradient-norm clipping and skipping
-    of non-finite steps (scripts/train_scatter_field.py:190, :228-235)."""
+    of non-finite steps (scripts/train_scatter_field.py:190, :228-235).
+
+    checkpoint: a path; every checkpoint_every steps, at the end, and on SIGTERM the parameters,
+    AdamW moments, step counter, batch sampler state and loss history are written there atomically,
+    and a run that finds the file resumes from it (scripts/train_scatter_field.py:132-134,
+    :165-168). On SIGTERM the function returns after saving, with hist[-1]["stopped"] set."""
     G = plan.grid
     rng = np.random.default_rng(seed)
     hist = []
@@ -81,41 +183,71 @@ def train(net: GridCNN, plan: PMPlan, data: list, steps: int, batch: int = 4, lr
     dfield = torch.zeros_like(field)
     t0 = time.time()
     window, skipped = [], 0
-    for it in range(1, steps + 1):
-        pick = rng.choice(len(data), size=batch, replace=len(data) < batch)
-        snaps = [data[i] for i in pick]
-        x = torch.cat([s["x"] for s in snaps])
-        field.zero_()
-        net.forward(x, batch, G, field, train=True)
-        preds = _predict(plan, field, batch, snaps)
-        loss = 0.0
-        dfield.zero_()
-        d4 = dfield.view(batch, G ** 3 * 4)
-        for b, (s, pr) in enumerate(zip(snaps, preds)):
-            # each snapshot normalised by its own residual energy, so that scenes with small
-            # forces (a uniform box) weigh as much as concentrated ones
-            den = batch * max(float((s["label"] ** 2).sum()), 1e-30)
-            diff = pr - s["label"]
-            loss += float((diff ** 2).sum()) / den
-            g = (2.0 / den) * diff
-            net._call("augur_cnn_gather_transpose", s["tpos"].data_ptr(), g.contiguous().data_ptr(),
-                      s["tpos"].shape[0], G, plan.extent, d4[b].data_ptr())
-        net.backward(dfield, batch, G)
-        gn = net.clip_grad_norm(clip)
-        if not (math.isfinite(loss) and math.isfinite(gn)):
-            skipped += 1
-            continue
-        sched = min(1.0, it / max(1, warmup)) * (0.55 + 0.45 * math.cos(math.pi * it / steps))
-        net.adamw(lr=lr * sched, weight_decay=weight_decay)
-        window.append(loss)
-        if it % log_every == 0 or it == steps:
-            net.check()
-            hist.append({"step": it, "loss": float(np.mean(window)), "grad_norm": gn, "skipped": skipped,
-                         "s": time.time() - t0})
-            window = []
-            if log:
-                log(f"step {it} loss {hist[-1]['loss']:.4f} |g| {gn:.3g} ({time.time() - t0:.1f} s)")
+    start = 1
+    ck = load_checkpoint(checkpoint) if checkpoint else None
+    if ck is not None:
+        net.load_state_dict(ck["net"])
+        rng.bit_generator.state = ck["rng"]
+        hist, skipped, start = list(ck["hist"]), int(ck["skipped"]), int(ck["it"]) + 1
+        if log:
+            log(f"resumed from {checkpoint} at step {start - 1}")
+
+    def state(it):
+        return {"net": net.state_dict(), "rng": rng.bit_generator.state, "hist": hist, "skipped": skipped, "it": it,
+                "steps": steps}
+
+    with _StopFlag() as stop:
+        for it in range(start, steps + 1):
+            loss, gn = _train_step(net, plan, data, batch, G, rng, field, dfield, clip)
+            if loss is None:  # non-finite loss or gradient: no update
+                skipped += 1
+            else:
+                sched = min(1.0, it / max(1, warmup)) * (0.55 + 0.45 * math.cos(math.pi * it / steps))
+                net.adamw(lr=lr * sched, weight_decay=weight_decay)
+                window.append(loss)
+            if it % log_every == 0 or it == steps:
+                net.check()
+                hist.append({"step": it, "loss": float(np.mean(window)) if window else float("nan"),
+                             "grad_norm": gn, "skipped": skipped, "s": time.time() - t0})
+                window = []
+                if log:
+                    log(f"step {it} loss {hist[-1]['loss']:.4f} |g| {gn:.3g} ({time.time() - t0:.1f} s)")
+            if checkpoint and (it % checkpoint_every == 0 or it == steps or stop.set):
+                save_checkpoint(checkpoint, state(it))
+            if stop.set:
+                hist.append({"step": it, "stopped": True, "s": time.time() - t0})
+                if log:
+                    log(f"SIGTERM: saved at step {it}")
+                return hist
     return hist
+
+
+def _train_step(net, plan, data, batch, G, rng, field, dfield, clip):
+    """Forward, loss and backward of one batch with gradient-norm clipping; returns (loss, |g|), or
+    (None, |g|) when the loss or the gradient is not finite (the caller then skips the update)."""
+    pick = rng.choice(len(data), size=batch, replace=len(data) < batch)
+    snaps = [data[i] for i in pick]
+    x = torch.cat([s["x"] for s in snaps])
+    field.zero_()
+    net.forward(x, batch, G, field, train=True)
+    preds = _predict(plan, field, batch, snaps)
+    loss = 0.0
+    dfield.zero_()
+    d4 = dfield.view(batch, G ** 3 * 4)
+    for b, (s, pr) in enumerate(zip(snaps, preds)):
+        # each snapshot normalised by its own residual energy, so that scenes with small
+        # forces (a uniform box) weigh as much as concentrated ones
+        den = batch * max(float((s["label"] ** 2).sum()), 1e-30)
+        diff = pr - s["label"]
+        loss += float((diff ** 2).sum()) / den
+        g = (2.0 / den) * diff
+        net._call("augur_cnn_gather_transpose", s["tpos"].data_ptr(), g.contiguous().data_ptr(),
+                  s["tpos"].shape[0], G, plan.extent, d4[b].data_ptr())
+    net.backward(dfield, batch, G)
+    gn = net.clip_grad_norm(clip)
+    if not (math.isfinite(loss) and math.isfinite(gn)):
+        return None, gn
+    return loss, gn
 
 
 # ---------------------------------------------------------------------------------------------

@@ -268,8 +268,10 @@ def force_error(a, truth):
 
 
 def cnn_form(args, pos, vel, mass, dev, idx, truth, st):
-    """The CNN-corrected step at 128^3 (trained weights) on the same bodies: body-steps/s and
-    force error, beside plain PM at 128^3."""
+    """The CNN-corrected step at 128^3 (trained weights) on the same bodies: body-steps/s, the
+    network's share of the step against the tensor-pipe roofline, an end-to-end rate through the
+    public API with pinned host buffers, and the force error at t = 0 and after the timed steps,
+    beside plain PM at 128^3."""
     from augur_gb300 import PMPlan
     from augur_gb300.cnn import GridCNN
     from augur_gb300.learned import CorrectedPM, FallbackMonitor
@@ -285,17 +287,38 @@ def cnn_form(args, pos, vel, mass, dev, idx, truth, st):
     net.load_state_dict(d["net"])
     p, v, m = (torch.from_numpy(x).to(dev) for x in (pos, vel, mass))
     ones = torch.ones(n, device=dev)
-    # accuracy: PM on this grid with and without the correction, at the truth's bodies
-    rho = plan.deposit(p, m, ones)
-    F4 = plan.poisson(rho)
-    tp = p[idx].contiguous()
-    pm, _ = plan.gather(F4, tp)
+
+    def accuracy(pp, tgt, tr):
+        rho = plan.deposit(pp, m, ones)
+        F4 = plan.poisson(rho)
+        tp = pp[tgt].contiguous()
+        pm, _ = plan.gather(F4, tp)
+        field = torch.zeros(G ** 3 * 4, device=dev)
+        net.forward(net.input(rho, F4), 1, G, field)
+        corr, _ = plan.gather(field.view(G, G, G, 4), tp)
+        return force_error(pm + corr, tr), force_error(pm, tr), (rho, F4)
+
+    acc0, pm0, (rho, F4) = accuracy(p, idx, truth)
+    # the network alone on this grid (CUDA events), for its tensor-pipe roofline
+    x = net.input(rho, F4)
     field = torch.zeros(G ** 3 * 4, device=dev)
-    net.forward(net.input(rho, F4), 1, G, field)
-    corr, _ = plan.gather(field.view(G, G, G, 4), tp)
+    for _ in range(3):
+        net.forward(x, 1, G, field)
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(st)
+    for _ in range(10):
+        net.forward(x, 1, G, field)
+    a1.record(st)
+    torch.cuda.synchronize(dev)
+    net_ms = a0.elapsed_time(a1) / 10
+    flop = 174528.0 * G ** 3  # forward flops per voxel x voxels (2 x 27 x (2*32 + 3*32*32 + 32*3))
+    pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak_s, peak_b = float(pk.get("bf16_tflops_sustained", 1700.0)), float(pk.get("bf16_tflops", 1900.0))
+    tflops = flop / (net_ms * 1e-3) / 1e12
     # throughput of the corrected leapfrog (monitor checks every 10 steps)
     sim = CorrectedPM(plan, net, FallbackMonitor(), check_every=10)
-    sim.begin(p, v, m, ones, dt=args.dt)
+    pe, ve = p.clone(), v.clone()
+    sim.begin(pe, ve, m, ones, dt=args.dt)
     sim.steps(3)
     torch.cuda.synchronize(dev)
     k = max(10, min(200, args.steps // 5))
@@ -305,11 +328,46 @@ def cnn_form(args, pos, vel, mass, dev, idx, truth, st):
     e1.record(st)
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1) / k
-    sim.end(p, v)
+    sim.end(pe, ve)
     net.check()
+    # accuracy after the timed steps, against a fresh FP64 truth at the evolved positions
+    idx1, truth1 = fp64_truth(pe, m, n, seed=9101)
+    acc1, pm1, _ = accuracy(pe, idx1, truth1)
+    # end to end through the public API: one corrected step per call on caller tensors copied in from
+    # and out to pinned host memory (CorrectedPM.begin / steps(1) / end)
+    h_pos, h_vel = torch.from_numpy(pos).pin_memory(), torch.from_numpy(vel).pin_memory()
+    d_pos, d_vel = torch.empty_like(p), torch.empty_like(v)
+    sim2 = CorrectedPM(plan, net, FallbackMonitor(), check_every=10)
+
+    def e2e_step():
+        d_pos.copy_(h_pos, non_blocking=True)
+        d_vel.copy_(h_vel, non_blocking=True)
+        sim2.begin(d_pos, d_vel, m, ones, dt=args.dt)
+        sim2.steps(1)
+        sim2.end(d_pos, d_vel)
+        h_pos.copy_(d_pos, non_blocking=True)
+        h_vel.copy_(d_vel, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize(dev)
+    ke = 5
+    e0.record(st)
+    for _ in range(ke):
+        e2e_step()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / ke
     return {"form": "CNN-corrected PM", "grid": G, "value": n / (ms * 1e-3), "unit": "body-steps/s",
             "ms_per_step": ms, "steps": k, "monitor_check_every": 10, "reverted_to_plain_pm": sim.monitor.reverted,
-            "accuracy": force_error(pm + corr, truth), "plain_pm_same_grid_accuracy": force_error(pm, truth),
+            "roofline": {"bound": "tensor", "kernel": "GridCNN.forward (5 tcgen05 conv layers)", "achieved": tflops,
+                         "peak": peak_s, "unit": "TFLOP/s", "frac": tflops / peak_s, "peak_kind": "measured sustained",
+                         "frac_of_burst": tflops / peak_b, "forward_ms": net_ms, "flop_per_forward": flop,
+                         "share_of_step": net_ms / ms, "traffic": None},
+            "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "body-steps/s", "h2d_bytes_per_step": 24 * n,
+                    "d2h_bytes_per_step": 24 * n,
+                    "api": "augur_gb300.learned.CorrectedPM begin / steps(1) / end on pinned host buffers"},
+            "accuracy": acc0, "plain_pm_same_grid_accuracy": pm0,
+            "accuracy_after_steps": {"steps": k + 3, "cnn": acc1, "plain_pm_same_grid": pm1},
             "weights": str(ck.relative_to(ROOT)), "trained": {k2: d.get(k2) for k2 in ("bodies", "grid", "eps")}}
 
 
@@ -503,19 +561,22 @@ def run_batch(args, world, rank, local):
 
     # CNN-corrected form on the scenes whose grid has trained weights
     cnn = None
-    ck = ROOT / "augur_gb300" / "weights" / "scatter_cnn_g128.pt"
-    if ck.exists() and not args.no_cnn:
+    nets = {}
+    for ck in sorted((ROOT / "augur_gb300" / "weights").glob("scatter_cnn_g*.pt")):
         d = torch.load(ck, map_location="cpu", weights_only=False)
         net = GridCNN(dev)
         net.load_state_dict(d["net"])
-        simc = BatchedPM(batch, dt=args.dt, nets={int(d["grid"]): net}, streams=args.streams, check_every=10)
+        nets[int(d["grid"])] = net
+    if nets and not args.no_cnn:
+        simc = BatchedPM(batch, dt=args.dt, nets=nets, streams=args.streams, check_every=10)
         simc.begin()
         simc.steps(W)
         cms = timed(lambda: simc.steps(K)) / K
         simc.end()
         errs = simc.force_errors(ntarget=1024) if not args.no_accuracy else None
         ncnn = sum(1 for s in simc.scenes if s["monitor"] is not None)
-        cnn = {"form": "CNN-corrected PM on the 128^3 scenes, plain PM on the others (no weights for 64^3/96^3)",
+        cnn = {"form": "CNN-corrected PM on the scenes whose grid has trained weights "
+                       f"({sorted(nets)}), plain PM on the others",
                "value": bodies / (cms * 1e-3), "unit": "body-steps/s", "ms_per_step": cms,
                "cnn_scenes": ncnn, "reverted_to_plain_pm": sum(1 for s in simc.scenes if s["monitor"] is not None
                                                                 and s["monitor"].reverted),

@@ -282,7 +282,10 @@ int augur_pm_check(augur_pm_plan *plan, void *stream);
  * target is not a source). targets (T, D) f64, sources (N, D) f64, mass (N,) f64 or
  * NULL for unit masses. acc_out (T, D) f64.
  * If box > 0 the sum is periodic (Ewald; box side = box, minimum image plus a tabulated
- * Ewald correction), else isolated.
+ * Ewald correction), else isolated. The Newtonian pair sum is FP64; the Ewald correction is read
+ * from a 65^3 table (FP64 sums stored as fp32) and interpolated trilinearly in fp32, a part of the
+ * force whose fp32 rounding moves the total by ~1e-8, below the table's interpolation error
+ * (about 1e-6 relative RMS on 2048-body scenes).
  */
 int augur_direct_sum_fp64(const double *targets, const int64_t *t_idx, int64_t t,
                           const double *sources, const double *mass, int64_t n,

@@ -7,7 +7,8 @@ import torch
 
 from augur_gb300 import PMPlan, energy_fp64, scenes
 from augur_gb300.cnn import GridCNN
-from augur_gb300.learned import CorrectedPM, FallbackMonitor, evaluate, make_dataset, train
+from augur_gb300.learned import (CorrectedPM, FallbackMonitor, evaluate, label_snapshots, make_dataset, make_truth,
+                                 train)
 
 pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda:0")
@@ -31,6 +32,44 @@ def test_training_reduces_force_error_on_held_out_snapshots():
         bound = 1.05 if kind == "uniform" else 1.0
         assert r["cnn"]["rel_rms"] < bound * r["plain_pm"]["rel_rms"], (kind, r)
     assert after["cnn"]["rel_rms"] < 0.85 * after["plain_pm"]["rel_rms"], after
+
+
+def test_training_resumes_from_a_sigterm_checkpoint(tmp_path):
+    """Six AdamW steps in one run against three steps stopped by SIGTERM (saved atomically) plus a
+    fresh run that resumes from the checkpoint: the same parameters, AdamW state and step count (up
+    to the fp32 atomics of the gather transpose)."""
+    import os
+    import signal
+
+    G, n = 32, 20000
+    plan = PMPlan(3, G, n, "periodic", 1.0, device=DEV)
+    net0 = GridCNN(DEV, seed=4738, phi_scale=0.1)
+    truth = make_truth(n, 8, 4738, DEV, n_targets=1024, eps=1.0 / 64)
+    data = label_snapshots(plan, net0, truth)
+    scale = float(torch.cat([d["label"] for d in data]).pow(2).sum(1).mean().sqrt())
+
+    def fresh():
+        net = GridCNN(DEV, seed=4738, phi_scale=0.1, out_scale=scale)
+        net.view["w_out"].normal_(0.0, 1e-3)  # non-zero output layer: every parameter moves
+        net.prepare()
+        return net
+
+    a = fresh()
+    train(a, plan, data, steps=6, batch=2, lr=1e-3, log_every=3)
+    a2 = fresh()
+    train(a2, plan, data, steps=6, batch=2, lr=1e-3, log_every=3)
+    floor = float((a2.params - a.params).norm() / a.params.norm())  # run-to-run spread
+    ck = str(tmp_path / "g32.ckpt")
+    b = fresh()
+    kill = lambda m: os.kill(os.getpid(), signal.SIGTERM) if m.startswith("step 3 ") else None  # noqa: E731
+    hist = train(b, plan, data, steps=6, batch=2, lr=1e-3, log_every=3, log=kill, checkpoint=ck)
+    assert hist[-1].get("stopped") and hist[-1]["step"] == 3 and b.adam_step == 3
+    c = fresh()
+    hist = train(c, plan, data, steps=6, batch=2, lr=1e-3, log_every=3, checkpoint=ck)
+    assert c.adam_step == 6 and [h["step"] for h in hist if "loss" in h] == [3, 6]
+    rel = float((c.params - a.params).norm() / a.params.norm())
+    print(f"resumed vs straight {rel:.3e}, straight vs straight {floor:.3e}")
+    assert rel < 1e-5 + 3.0 * floor, (rel, floor)
 
 
 def test_split_run_loop_equals_run():
