@@ -38,6 +38,10 @@ SIGNATURES = {
     "augur_pm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp]),
     "augur_pm_run_begin": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),
     "augur_pm_run_steps": (_i32, [_vp, _i32, _vp]),
+    "augur_pm_batch_create": (_i32, [C.POINTER(_vp), _vp, _i32]),
+    "augur_pm_batch_run_steps": (_i32, [_vp, _i32, _vp]),
+    "augur_pm_batch_size": (_i32, [_vp]),
+    "augur_pm_batch_destroy": (_i32, [_vp]),
     "augur_pm_run_end": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "augur_pm_run_profile": (_i32, [_vp, _i32, _vp, _i32, _vp]),
     "augur_pm_run_load": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),

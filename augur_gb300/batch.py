@@ -15,15 +15,21 @@ correction's size needs the grid before and after the network and is not made.)
 
 A step swaps each plan's two body buffers, so the graph holds an even number of steps
 and replays leave the plans' host state unchanged.
+
+fused=True (plain PM only) steps all scenes with one launch per stage instead of one plan per
+graph branch: augur_pm_batch_run_steps deals each stage's blocks to the scenes by a table of
+block offsets, so a step is 11 launches whatever the number of scenes, bit-identical to the
+per-scene steps.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 
 import numpy as np
 import torch
 
-from . import autotune, scenes
+from . import _lib, autotune, scenes
 from .learned import FallbackMonitor
 from .pm import PMPlan, direct_sum_fp64
 
@@ -59,9 +65,14 @@ class BatchedPM:
     """
 
     def __init__(self, batch: list, dt: float = 5e-4, nets: dict | None = None, streams: int = 16,
-                 tiles="cache", check_every: int = 10, device=None, extent: float = 1.0, drift_max: float = 0.05):
+                 tiles="cache", check_every: int = 10, device=None, extent: float = 1.0, drift_max: float = 0.05,
+                 fused: bool = False):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.dt, self.nets, self.check_every = float(dt), dict(nets or {}), int(check_every)
+        if fused and self.nets:
+            raise ValueError("fused stepping covers plain PM batches (no nets)")
+        self.fused = bool(fused)
+        self._batch = None
         self.scenes = []
         cache = autotune.load_cache() if tiles == "cache" else None
         for sc in batch:
@@ -146,6 +157,30 @@ class BatchedPM:
     # ---- public -------------------------------------------------------------------------
     def begin(self):
         """Load every scene, apply the opening half kick and capture the two-step graph."""
+        if self.fused:
+            # one launch per stage needs one z-transform tile and one deposit variant for all plans
+            ty = 16 if all(s["grid"] % 16 == 0 for s in self.scenes) else 8
+            for s in self.scenes:
+                t = s["plan"].tiles
+                if t["green_tile_y"] != ty or t["deposit_aggregate"] != 0:
+                    s["plan"].set_tiles({"green_tile_y": ty, "deposit_aggregate": 0})
+                s["plan"].bind_force_grid(None)
+                s["plan"].run_begin(s["pos"], s["vel"], s["mass"], s["mask"], dt=self.dt)
+            lib = _lib.load()
+            arr = (C.c_void_p * len(self.scenes))(*[s["plan"]._p for s in self.scenes])
+            h = C.c_void_p()
+            with torch.cuda.device(self.device):
+                rc = lib.augur_pm_batch_create(C.byref(h), arr, len(self.scenes))
+            _lib.check(rc, "augur_pm_batch_create")
+            self._batch = h
+            self.groups = {}
+            torch.cuda.synchronize(self.device)
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                st = torch.cuda.current_stream(self.device).cuda_stream
+                _lib.check(lib.augur_pm_batch_run_steps(self._batch, 2, st), "augur_pm_batch_run_steps")
+            torch.cuda.synchronize(self.device)
+            return
         self._build_groups()
         for s in self.scenes:
             if not s["cnn"]:
@@ -211,6 +246,12 @@ class BatchedPM:
     def end(self):
         """Closing half kick; writes every scene's positions and velocities back (scene order)."""
         torch.cuda.synchronize(self.device)
+        if self.fused:
+            for s in self.scenes:
+                s["plan"].run_end(s["pos"], s["vel"])
+            self._free_batch()
+            torch.cuda.synchronize(self.device)
+            return [(s["pos"], s["vel"]) for s in self.scenes]
         for s in self.scenes:
             p = s["plan"]
             if s["cnn"]:
@@ -229,8 +270,15 @@ class BatchedPM:
         torch.cuda.synchronize(self.device)
         return [(s["pos"], s["vel"]) for s in self.scenes]
 
+    def _free_batch(self):
+        if self._batch is not None:
+            self.graph = None
+            _lib.load().augur_pm_batch_destroy(self._batch)
+            self._batch = None
+
     def close(self):
         self.graph = None
+        self._free_batch()
         for s in self.scenes:
             s["plan"].close()
 

@@ -464,7 +464,7 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   if (t->deposit_aggregate != 0 && t->deposit_aggregate != 1) return AUGUR_EINVAL;
   // shared memory of each kernel (layouts in pm_kernels.cuh; transform rows padded by fft_row_stride)
   const size_t PM = (size_t)fft_row_stride(M), PL = (size_t)fft_row_stride(L);
-  const size_t s_dep = (size_t)RY * RZ * (2 * PM * 8 + (size_t)(G + 2) * 4) + (size_t)Lt * 8;
+  const size_t s_dep = (size_t)RY * RZ * (2 * PM * 8 + std::max((size_t)(G + 2) * 4, PM * 8)) + (size_t)Lt * 8;
   const size_t s_green = (size_t)3 * G * t->green_tile_y * 8 + (size_t)Lt * 8;
   const size_t s_c2r = (size_t)2 * RB * PM * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 + (size_t)Lt * 8;
   const size_t s_rows = (size_t)2 * t->fft_rows * PL * 8 + (size_t)Lt * 8;
@@ -1223,5 +1223,244 @@ int augur_pm_check(augur_pm_plan *p, void *stream) {
   if (e & AUGUR_ERRBIT_TIMEOUT) return AUGUR_ETIMEDOUT;
   return AUGUR_OK;
 }
+
+}  // extern "C"
+
+// =====================================================================================
+// Batches of scenes: one launch per stage for every scene of the batch
+// =====================================================================================
+struct augur_pm_batch {
+  int ns;
+  std::vector<augur_pm_plan *> plans;
+  int parity;  // steps taken mod 2: pack set in use
+  int green_ty, agg;
+  size_t smem_dep, smem_rows, smem_green, smem_c2r;
+  int tot_scan, tot_scatter, tot_depcount, tot_dep, tot_rows_f, tot_rows_i, tot_green, tot_c2r, tot_gather;
+  int *boff;  // device: 9 tables of ns + 1 block offsets, stage after stage
+  ScanPack *scan;
+  ScatterPack *scatter;   // [2][ns]
+  DepPlanPack *depplan;   // [2][ns] (the plan tables do not depend on the parity; both equal)
+  DepPack *dep;           // [2][ns]
+  RowsPack *rows_f, *rows_i;
+  GreenPack *green;
+  C2RPack *c2r;
+  GatherPack *gather;     // [2][ns]
+  unsigned *d_err;        // not used: every scene reports through its own plan's error word
+};
+
+namespace {
+
+enum { BS_SCAN, BS_SCATTER, BS_DEPCOUNT, BS_DEP, BS_ROWS_F, BS_GREEN, BS_ROWS_I, BS_C2R, BS_GATHER, BS_N };
+
+template <typename T>
+int batch_upload(T **dst, const std::vector<T> &v) {
+  if (cudaMalloc(dst, sizeof(T) * std::max<size_t>(1, v.size())) != cudaSuccess) return AUGUR_ENOMEM;
+  if (!v.empty() && cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return AUGUR_ECUDA;
+  return AUGUR_OK;
+}
+
+void batch_free(augur_pm_batch *b) {
+  void *q[] = {b->boff, b->scan, b->scatter, b->depplan, b->dep, b->rows_f, b->rows_i, b->green, b->c2r, b->gather};
+  for (void *x : q)
+    if (x) cudaFree(x);
+}
+
+}  // namespace
+
+extern "C" {
+
+int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int nplans) {
+  if (!out || !plans || nplans < 1) return AUGUR_EINVAL;
+  *out = nullptr;
+  augur_pm_batch *b = new (std::nothrow) augur_pm_batch();
+  if (!b) return AUGUR_ENOMEM;
+  b->ns = nplans;
+  b->plans.assign(plans, plans + nplans);
+  const int ns = nplans;
+  std::vector<int> boff((size_t)BS_N * (ns + 1), 0);
+  std::vector<ScanPack> scan(ns);
+  std::vector<ScatterPack> scatter(2 * ns);
+  std::vector<DepPlanPack> depplan(ns);
+  std::vector<DepPack> dep(2 * ns);
+  std::vector<RowsPack> rows_f(ns), rows_i(ns);
+  std::vector<GreenPack> green(ns);
+  std::vector<C2RPack> c2r(ns);
+  std::vector<GatherPack> gather(2 * ns);
+  int rc = AUGUR_OK;
+  for (int i = 0; i < ns && rc == AUGUR_OK; ++i) {
+    augur_pm_plan *p = plans[i];
+    if (!p || p->mode != AUGUR_MODE_PERIODIC || p->dim != 3 || p->run_active != 1) {
+      rc = AUGUR_EINVAL;
+      break;
+    }
+    if (i == 0) {
+      b->green_ty = p->green_TY;
+      b->agg = p->dep_agg;
+    } else if (p->green_TY != b->green_ty || p->dep_agg != b->agg) {
+      rc = AUGUR_EINVAL;  // one z-transform tile and one deposit variant per batch
+      break;
+    }
+    const int G = p->G, M = p->M;
+    const int64_t n = p->run_n;
+    int cnt[BS_N];
+    cnt[BS_SCAN] = p->ntiles;
+    cnt[BS_SCATTER] = (int)blocks_for(n, 256);
+    cnt[BS_DEPCOUNT] = (int)blocks_for(p->nblk, 256);
+    const int64_t items = (int64_t)p->nblk + 4 * dep_nchunks(p, n) + 1;
+    if ((size_t)items > p->dep_items_max) {
+      rc = AUGUR_ERANGE;
+      break;
+    }
+    cnt[BS_DEP] = (int)items;
+    cnt[BS_ROWS_F] = (int)blocks_for((int64_t)(M + 1) * G, p->rows_RB);
+    cnt[BS_GREEN] = (M + 1) * (G / p->green_TY);
+    cnt[BS_ROWS_I] = (int)blocks_for((int64_t)3 * (M + 1) * G, p->rows_RB);
+    cnt[BS_C2R] = G * G / p->c2r_RB;
+    cnt[BS_GATHER] = (int)blocks_for(n, 256);
+    for (int st = 0; st < BS_N; ++st) boff[(size_t)st * (ns + 1) + i + 1] = boff[(size_t)st * (ns + 1) + i] + cnt[st];
+    b->smem_dep = std::max(b->smem_dep, p->smem_dep);
+    b->smem_rows = std::max(b->smem_rows, p->smem_rows);
+    b->smem_green = std::max(b->smem_green, p->smem_green);
+    b->smem_c2r = std::max(b->smem_c2r, p->smem_c2r);
+
+    scan[i] = {p->row_count, p->row_start, p->tile_sum, p->tile_off, p->nrow, p->ntiles};
+    const DepositArgs da = dep_args(p);
+    depplan[i] = {p->row_start, p->tile_off, da, p->dep_nch, p->dep_item_off, p->dep_slot_off, p->dep_item_blk,
+                  p->dep_seg_tab, p->d_err};
+    RowsPack rp{};
+    rp.data = p->spec;
+    rp.nrows = (int64_t)(M + 1) * G;
+    rp.RB = p->rows_RB;
+    rp.L = p->L;
+    rp.twmul = p->Lt / p->L;
+    rp.Lt = p->Lt;
+    rp.inverse = 0;
+    rp.fdL = make_fastdiv(p->L);
+    rp.tw = p->tw;
+    rows_f[i] = rp;
+    rp.data = p->spec3;
+    rp.nrows = (int64_t)3 * (M + 1) * G;
+    rp.inverse = 1;
+    rows_i[i] = rp;
+    GreenArgs ga;
+    ga.G = G;
+    ga.TY = p->green_TY;
+    ga.ncomp = 3;
+    ga.Lt = p->Lt;
+    ga.fsh = p->sh_L;
+    ga.kfund = (float)(2.0 * M_PI / p->extent);
+    ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
+    green[i] = {p->spec, ga, p->tw, p->spec3};
+    C2RArgs ca{};
+    ca.L = G;
+    ca.nrows = G * G;
+    ca.RB = p->c2r_RB;
+    ca.ncomp = 3;
+    ca.Lt = p->Lt;
+    ca.nkeep = G * G;
+    ca.Lkeep = G;
+    ca.scale = 1.f;
+    ca.fsh = p->sh_M;
+    ca.twmul = p->Lt / M;
+    ca.fdRB = make_fastdiv(ca.RB);
+    ca.fdM = make_fastdiv(ca.L / 2);
+    ca.fdL = make_fastdiv(ca.L);
+    c2r[i] = {p->spec3, ca, p->tw, reinterpret_cast<float *>(p->F4)};
+    const GatherArgs ga2 = gather_args(p, p->run_dt, p->run_dt, 1);
+    for (int par = 0; par < 2; ++par) {
+      const int c = p->cur ^ par;  // state buffers before this step's re-sort
+      scatter[(size_t)par * ns + i] = {p->pos4[c], p->vel4[c], n, p->key, p->slot, p->row_start, p->tile_off,
+                                       p->pos4[c ^ 1], p->vel4[c ^ 1]};
+      dep[(size_t)par * ns + i] = {p->pos4[c ^ 1], p->d_mmax, da, p->tw, p->spec, p->d_err, p->dep_item_off,
+                                   p->dep_slot_off, p->dep_item_blk, p->dep_seg_tab, p->dep_scratch,
+                                   p->dep_counters};
+      gather[(size_t)par * ns + i] = {p->F4, p->pos4[c ^ 1], p->vel4[c ^ 1], n, ga2, p->key, p->slot, p->row_count,
+                                      p->d_err};
+    }
+  }
+  if (rc == AUGUR_OK) {
+    b->tot_scan = boff[(size_t)BS_SCAN * (ns + 1) + ns];
+    b->tot_scatter = boff[(size_t)BS_SCATTER * (ns + 1) + ns];
+    b->tot_depcount = boff[(size_t)BS_DEPCOUNT * (ns + 1) + ns];
+    b->tot_dep = boff[(size_t)BS_DEP * (ns + 1) + ns];
+    b->tot_rows_f = boff[(size_t)BS_ROWS_F * (ns + 1) + ns];
+    b->tot_green = boff[(size_t)BS_GREEN * (ns + 1) + ns];
+    b->tot_rows_i = boff[(size_t)BS_ROWS_I * (ns + 1) + ns];
+    b->tot_c2r = boff[(size_t)BS_C2R * (ns + 1) + ns];
+    b->tot_gather = boff[(size_t)BS_GATHER * (ns + 1) + ns];
+    rc |= batch_upload(&b->boff, boff);
+    rc |= batch_upload(&b->scan, scan);
+    rc |= batch_upload(&b->scatter, scatter);
+    rc |= batch_upload(&b->depplan, depplan);
+    rc |= batch_upload(&b->dep, dep);
+    rc |= batch_upload(&b->rows_f, rows_f);
+    rc |= batch_upload(&b->rows_i, rows_i);
+    rc |= batch_upload(&b->green, green);
+    rc |= batch_upload(&b->c2r, c2r);
+    rc |= batch_upload(&b->gather, gather);
+    if (rc) rc = AUGUR_ENOMEM;
+  }
+  if (rc == AUGUR_OK) {
+    rc |= raise_smem(b->agg ? deposit_multi<true> : deposit_multi<false>, b->smem_dep);
+    rc |= raise_smem(fft_rows_multi, b->smem_rows);
+    rc |= raise_smem(b->green_ty == 16 ? green_multi<16> : green_multi<8>, b->smem_green);
+    rc |= raise_smem(c2r_multi, b->smem_c2r);
+    if (rc) rc = AUGUR_ECUDA;
+  }
+  if (rc != AUGUR_OK) {
+    batch_free(b);
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return AUGUR_OK;
+}
+
+int augur_pm_batch_destroy(augur_pm_batch *b) {
+  if (!b) return AUGUR_OK;
+  batch_free(b);
+  delete b;
+  return AUGUR_OK;
+}
+
+int augur_pm_batch_run_steps(augur_pm_batch *b, int k, void *stream) {
+  if (!b || k < 0) return AUGUR_EINVAL;
+  for (augur_pm_plan *p : b->plans)
+    if (p->run_active != 1) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  const int ns = b->ns;
+  const int *bo = b->boff;
+  auto off = [&](int stage) { return bo + (size_t)stage * (ns + 1); };
+  for (int s = 0; s < k; ++s) {
+    const int par = b->parity;
+    if (b->tot_scan) scan_local_multi<<<b->tot_scan, 1024, 0, st>>>(b->scan, off(BS_SCAN), ns);
+    scan_tiles_multi<<<ns, 1024, 0, st>>>(b->scan);
+    if (b->tot_scatter)
+      scatter_sorted_multi<<<b->tot_scatter, 256, 0, st>>>(b->scatter + (size_t)par * ns, off(BS_SCATTER), ns);
+    if (b->tot_depcount) deposit_count_multi<<<b->tot_depcount, 256, 0, st>>>(b->depplan, off(BS_DEPCOUNT), ns);
+    deposit_plan_multi<<<ns, 1024, 0, st>>>(b->depplan);
+    if (b->agg)
+      deposit_multi<true><<<b->tot_dep, DEP_THREADS, b->smem_dep, st>>>(b->dep + (size_t)par * ns, off(BS_DEP), ns);
+    else
+      deposit_multi<false><<<b->tot_dep, DEP_THREADS, b->smem_dep, st>>>(b->dep + (size_t)par * ns, off(BS_DEP), ns);
+    fft_rows_multi<<<b->tot_rows_f, 256, b->smem_rows, st>>>(b->rows_f, off(BS_ROWS_F), ns);
+    if (b->green_ty == 16)
+      green_multi<16><<<b->tot_green, 512, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+    else
+      green_multi<8><<<b->tot_green, 512, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+    fft_rows_multi<<<b->tot_rows_i, 256, b->smem_rows, st>>>(b->rows_i, off(BS_ROWS_I), ns);
+    c2r_multi<<<b->tot_c2r, 512, b->smem_c2r, st>>>(b->c2r, off(BS_C2R), ns);
+    if (b->tot_gather)
+      gather_multi<<<b->tot_gather, 256, 0, st>>>(b->gather + (size_t)par * ns, off(BS_GATHER), ns);
+    if (cudaGetLastError() != cudaSuccess) return AUGUR_ECUDA;
+    b->parity ^= 1;
+    for (augur_pm_plan *p : b->plans)
+      if (p->run_n > 0) p->cur ^= 1;
+  }
+  return AUGUR_OK;
+}
+
+int augur_pm_batch_size(const augur_pm_batch *b) { return b ? b->ns : 0; }
 
 }  // extern "C"

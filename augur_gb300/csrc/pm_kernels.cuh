@@ -159,10 +159,10 @@ __global__ void __launch_bounds__(256) keys_hist_aos_kernel(float *__restrict__ 
 // counters are cleared for the next histogram), then one block scans the tile totals.
 // row_begin(r) = tile_off[r / 4096] + start[r] for any r <= nrow.
 // ---------------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) scan_local_kernel(uint32_t *__restrict__ count, uint32_t *__restrict__ start,
-                                                          uint32_t *__restrict__ tile_sum, int nrow) {
+__device__ __forceinline__ void scan_local_kernel_body(uint32_t *__restrict__ count, uint32_t *__restrict__ start,
+                                                          uint32_t *__restrict__ tile_sum, int nrow, const int bx) {
   __shared__ uint32_t wsum[32];
-  const int tile = blockIdx.x;
+  const int tile = bx;
   const int base = tile * SCAN_TILE + threadIdx.x * 4;
   uint32_t v[4];
 #pragma unroll
@@ -202,8 +202,13 @@ __global__ void __launch_bounds__(1024) scan_local_kernel(uint32_t *__restrict__
   }
 }
 
-__global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t *__restrict__ tile_sum,
-                                                          uint32_t *__restrict__ tile_off, int ntiles) {
+__global__ void __launch_bounds__(1024) scan_local_kernel(uint32_t *__restrict__ count, uint32_t *__restrict__ start,
+                                                          uint32_t *__restrict__ tile_sum, int nrow) {
+  scan_local_kernel_body(count, start, tile_sum, nrow, (int)blockIdx.x);
+}
+
+__device__ __forceinline__ void scan_tiles_kernel_body(const uint32_t *__restrict__ tile_sum,
+                                                          uint32_t *__restrict__ tile_off, int ntiles, const int bx) {
   __shared__ uint32_t wsum[32];
   __shared__ uint32_t carry;
   if (threadIdx.x == 0) carry = 0;
@@ -239,6 +244,11 @@ __global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t *__rest
   if (threadIdx.x == 0) tile_off[ntiles] = carry;
 }
 
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t *__restrict__ tile_sum,
+                                                          uint32_t *__restrict__ tile_off, int ntiles) {
+  scan_tiles_kernel_body(tile_sum, tile_off, ntiles, (int)blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------------
 // Scatter bodies to their sorted slot. From caller AoS arrays (FROM_AOS) or from the
 // previous sorted state (run loop).
@@ -268,6 +278,20 @@ __global__ void __launch_bounds__(256) scatter_aos_kernel(const float *__restric
   vel4[dst] = v;
 }
 
+__device__ __forceinline__ void scatter_sorted_kernel_body(const float4 *__restrict__ pos_in,
+                                                             const float4 *__restrict__ vel_in, int64_t n,
+                                                             const uint32_t *__restrict__ key,
+                                                             const uint32_t *__restrict__ slot,
+                                                             const uint32_t *__restrict__ start,
+                                                             const uint32_t *__restrict__ tile_off,
+                                                             float4 *__restrict__ pos_out, float4 *__restrict__ vel_out, const int bx) {
+  const int64_t i = (int64_t)bx * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t dst = row_begin(start, tile_off, key[i]) + slot[i];
+  pos_out[dst] = pos_in[i];
+  vel_out[dst] = vel_in[i];
+}
+
 __global__ void __launch_bounds__(256) scatter_sorted_kernel(const float4 *__restrict__ pos_in,
                                                              const float4 *__restrict__ vel_in, int64_t n,
                                                              const uint32_t *__restrict__ key,
@@ -275,11 +299,7 @@ __global__ void __launch_bounds__(256) scatter_sorted_kernel(const float4 *__res
                                                              const uint32_t *__restrict__ start,
                                                              const uint32_t *__restrict__ tile_off,
                                                              float4 *__restrict__ pos_out, float4 *__restrict__ vel_out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t dst = row_begin(start, tile_off, key[i]) + slot[i];
-  pos_out[dst] = pos_in[i];
-  vel_out[dst] = vel_in[i];
+  scatter_sorted_kernel_body(pos_in, vel_in, n, key, slot, start, tile_off, pos_out, vel_out, (int)blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -342,11 +362,11 @@ constexpr int64_t DEP_ITEM_MAX = (int64_t)1 << 19;
 
 // One thread per row block (many CTAs): the block's body segments and its item count.
 template <int D>
-__global__ void __launch_bounds__(256) deposit_count_kernel(const uint32_t *__restrict__ start,
+__device__ __forceinline__ void deposit_count_kernel_body(const uint32_t *__restrict__ start,
                                                             const uint32_t *__restrict__ tile_off, DepositArgs a,
                                                             uint32_t *__restrict__ nch, uint4 *__restrict__ seg_tab,
-                                                            unsigned *__restrict__ err) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+                                                            unsigned *__restrict__ err, const int bx) {
+  const int b = bx * blockDim.x + threadIdx.x;
   if (b >= a.nblk) return;
   uint32_t cnt = 0;
   int ns = 0;
@@ -364,14 +384,22 @@ __global__ void __launch_bounds__(256) deposit_count_kernel(const uint32_t *__re
   nch[b] = cnt == 0 ? 1u : (cnt + a.chunk - 1) / a.chunk;
 }
 
+template <int D>
+__global__ void __launch_bounds__(256) deposit_count_kernel(const uint32_t *__restrict__ start,
+                                                            const uint32_t *__restrict__ tile_off, DepositArgs a,
+                                                            uint32_t *__restrict__ nch, uint4 *__restrict__ seg_tab,
+                                                            unsigned *__restrict__ err) {
+  deposit_count_kernel_body<D>(start, tile_off, a, nch, seg_tab, err, (int)blockIdx.x);
+}
+
 // One CTA: scan of the item counts into item_off and slot_off, and the block of every item.
 template <int D>
-__global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__restrict__ start,
+__device__ __forceinline__ void deposit_plan_kernel_body(const uint32_t *__restrict__ start,
                                                             const uint32_t *__restrict__ tile_off, DepositArgs a,
                                                             uint32_t *__restrict__ nch, uint32_t *__restrict__ item_off,
                                                             uint32_t *__restrict__ slot_off,
                                                             uint4 *__restrict__ seg_tab, uint32_t *__restrict__ item_blk,
-                                                            unsigned *__restrict__ err) {
+                                                            unsigned *__restrict__ err, const int bx) {
   __shared__ uint32_t wsum[2][32];
   const int nb = a.nblk, tid = threadIdx.x, nt = blockDim.x;
   const int per = (nb + nt - 1) / nt;
@@ -424,6 +452,16 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
   if (tid == nt - 1) item_off[nb] = ri;
 }
 
+template <int D>
+__global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__restrict__ start,
+                                                            const uint32_t *__restrict__ tile_off, DepositArgs a,
+                                                            uint32_t *__restrict__ nch, uint32_t *__restrict__ item_off,
+                                                            uint32_t *__restrict__ slot_off,
+                                                            uint4 *__restrict__ seg_tab, uint32_t *__restrict__ item_blk,
+                                                            unsigned *__restrict__ err) {
+  deposit_plan_kernel_body<D>(start, tile_off, a, nch, item_off, slot_off, seg_tab, item_blk, err, (int)blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------------
 // K2 (+K3a): deterministic CIC deposit of one block of grid rows in fixed point (integer
 // sums are associative, so the result is independent of body order and scheduling), then
@@ -442,6 +480,28 @@ __global__ void __launch_bounds__(1024) deposit_plan_kernel(const uint32_t *__re
 // the CTA that finishes last (counter + threadfence, no waiting) reads the tile, clears it
 // for the next call, and converts.
 // ---------------------------------------------------------------------------------
+// R2C post-process of a row block's M-point transforms Z (row stride MS) into the half spectrum:
+// X_k = (Z_k + conj Z_{M-k})/2 - i/2 W^k (Z_k - conj Z_{M-k}), k = 0..M, at spec[kx][row].
+template <int D>
+__device__ __forceinline__ void deposit_r2c_post(const float2 *Z, int MS, int M, int RR, int G, int RY, int z0, int y0,
+                                                 const DepositArgs &a, const float2 *tw, float2 *__restrict__ spec_out) {
+  const int tstep = a.Lt / G;
+  const size_t plane = (size_t)(D == 3 ? G : 1) * G;  // rows per kx plane
+  for (int e = threadIdx.x; e < (M + 1) * RR; e += blockDim.x) {
+    int kx = (int)fdiv(e, a.fdRR), rr = e - kx * RR;
+    float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
+    float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
+    float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+    float2 od = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y - zc.y));
+    float2 w = tw[kx * tstep];
+    float2 t = cmul(w, od);
+    float2 X = make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
+    int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
+    size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
+    spec_out[(size_t)kx * plane + row] = X;
+  }
+}
+
 // adds q < 2^31 to cell c of the split accumulators (lo gets the low 13 bits, hi the rest)
 __device__ __forceinline__ void dep_add(uint32_t *lo, uint32_t *hi, int c, uint32_t q) {
   if (q & 8191u) atomicAdd(&lo[c], q & 8191u);
@@ -449,7 +509,7 @@ __device__ __forceinline__ void dep_add(uint32_t *lo, uint32_t *hi, int c, uint3
 }
 
 template <int D, int MODE, bool AGG>
-__global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restrict__ pos4,
+__device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ pos4,
                                                       const unsigned *__restrict__ mmax_bits, DepositArgs a,
                                                       const float2 *__restrict__ twg, float *__restrict__ rho_out,
                                                       float2 *__restrict__ spec_out, unsigned *__restrict__ err,
@@ -458,7 +518,7 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
                                                       const uint4 *__restrict__ seg_tab,
                                                       const uint32_t *__restrict__ item_blk,
                                                       unsigned long long *__restrict__ scratch,
-                                                      unsigned *__restrict__ counters) {
+                                                      unsigned *__restrict__ counters, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ long long s_beg[MAXSEGB];
   __shared__ long long s_pre[MAXSEGB + 1];
@@ -468,7 +528,7 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   const GridParams &g = a.g;
   const int G = g.G, RY = a.RY, RZ = a.RZ, RR = RY * RZ;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const uint32_t item = blockIdx.x;
+  const uint32_t item = bx;
   if (item >= item_off[a.nblk]) return;  // uniform across the CTA
   const int blk = (int)item_blk[item];
   const uint32_t part = item - item_off[blk];
@@ -484,7 +544,9 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem);
   uint32_t *acc_hi = acc_lo + (size_t)RR * G;
   float *rows = reinterpret_cast<float *>(smem + region);
-  float2 *tw = reinterpret_cast<float2 *>(smem + region + (size_t)RR * RS * 4);
+  // the fp32 rows, or (fused spectrum path) the transform's scratch rows
+  const size_t rows_bytes = (size_t)RR * max(RS * 4, PS * 8);
+  float2 *tw = reinterpret_cast<float2 *>(smem + region + rows_bytes);
 
   const uint4 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
   if (tid <= MAXSEGB) {
@@ -643,6 +705,39 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
     if (tid == 0) counters[blk] = 0u;
   }
 
+  if constexpr (MODE == 1) {
+    // spectrum only, two-stage row transforms (G = 64 .. 512 except 3-smooth lengths of three
+    // stages): the fixed-point sums are converted on the transform's first load, so there is no
+    // separate conversion pass. Stage 0 reads the accumulators (or the split block's tile) and
+    // writes the scratch rows; stage 1 writes the transformed rows over the accumulator area.
+    const int M = G / 2, MS = M + 1;
+    if (fft_nstages(M) == 2) {
+      auto conv = [&](int c) -> float {
+        unsigned long long q;
+        if (gtile) {  // the split block's total, and the tile cleared for the next call
+          q = __ldcg(&gtile[c]);
+          gtile[c] = 0ull;
+        } else {
+          q = ((unsigned long long)acc_hi[c] << 13) + acc_lo[c];
+        }
+        const float fq = (q >> 32) ? __ull2float_rn(q) : __uint2float_rn((unsigned)q);
+        return __fmul_rn(fq, qs.outscale);
+      };
+      float2 *Zt = reinterpret_cast<float2 *>(smem);  // transformed rows, stride MS
+      float2 *Sb = reinterpret_cast<float2 *>(rows);  // stage-0 output, padded rows of PS
+      {
+        auto ld = [&](int b, int e) -> float2 {
+          const int c = b * G + 2 * e;
+          return make_float2(conv(c), conv(c + 1));
+        };
+        auto st = [&](int b, int e, float2 v) { Zt[b * MS + e] = v; };
+        AUGUR_FFT_IO(M, 0, RR, ld, st, Zt, Sb, PS, tw, a.twmul, false);
+      }
+      deposit_r2c_post<D>(Zt, MS, M, RR, G, RY, z0, y0, a, tw, spec_out);
+      return;
+    }
+  }
+
   // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
   for (int e = tid; e < RR * G; e += nt) {
     int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
@@ -679,22 +774,21 @@ __global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restric
     auto st = [&](int b, int e, float2 v) { Z[b * MS + e] = v; };
     AUGUR_FFT_IO(M, 0, RR, ld, st, TA, TB, PS, tw, a.twmul, false);
   }
-  // post-process X_k = (Z_k + conj Z_{M-k})/2 - i/2 W^k (Z_k - conj Z_{M-k}), k = 0..M
-  const int tstep = a.Lt / G;
-  const size_t plane = (size_t)(D == 3 ? G : 1) * G;  // rows per kx plane
-  for (int e = tid; e < (M + 1) * RR; e += nt) {
-    int kx = (int)fdiv(e, a.fdRR), rr = e - kx * RR;
-    float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
-    float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
-    float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
-    float2 od = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y - zc.y));
-    float2 w = tw[kx * tstep];
-    float2 t = cmul(w, od);
-    float2 X = make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
-    int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
-    size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
-    spec_out[(size_t)kx * plane + row] = X;
-  }
+  deposit_r2c_post<D>(Z, MS, M, RR, G, RY, z0, y0, a, tw, spec_out);
+}
+
+template <int D, int MODE, bool AGG>
+__global__ void __launch_bounds__(256, 4) deposit_kernel(const float4 *__restrict__ pos4,
+                                                      const unsigned *__restrict__ mmax_bits, DepositArgs a,
+                                                      const float2 *__restrict__ twg, float *__restrict__ rho_out,
+                                                      float2 *__restrict__ spec_out, unsigned *__restrict__ err,
+                                                      const uint32_t *__restrict__ item_off,
+                                                      const uint32_t *__restrict__ slot_off,
+                                                      const uint4 *__restrict__ seg_tab,
+                                                      const uint32_t *__restrict__ item_blk,
+                                                      unsigned long long *__restrict__ scratch,
+                                                      unsigned *__restrict__ counters) {
+  deposit_kernel_body<D, MODE, AGG>(pos4, mmax_bits, a, twg, rho_out, spec_out, err, item_off, slot_off, seg_tab, item_blk, scratch, counters, (int)blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -751,16 +845,16 @@ __global__ void __launch_bounds__(256) r2c_rows_kernel(const float *__restrict__
 
 // In-place FFT of contiguous complex rows of length L (rows = lines along y): the first
 // stage reads HBM, the last writes HBM, the stages between go through shared memory.
-__global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data, int64_t nrows, int RB, int L,
+__device__ __forceinline__ void fft_rows_kernel_body(float2 *__restrict__ data, int64_t nrows, int RB, int L,
                                                        FastDiv fdL, int twmul, int Lt,
-                                                       const float2 *__restrict__ twg, int inverse) {
+                                                       const float2 *__restrict__ twg, int inverse, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int LS = fft_row_stride(L);
   float2 *A = reinterpret_cast<float2 *>(smem);
   float2 *B = A + (size_t)RB * LS;
   float2 *tw = B + (size_t)RB * LS;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int64_t r0 = (int64_t)blockIdx.x * RB;
+  const int64_t r0 = (int64_t)bx * RB;
   const int nr = (int)min((int64_t)RB, nrows - r0);
   for (int e = tid; e < Lt; e += nt) tw[e] = twg[e];
   float2 *base = data + r0 * L;
@@ -779,6 +873,12 @@ __global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data
   auto ld = [&](int b, int e) -> float2 { return base[(size_t)b * L + e]; };
   auto st = [&](int b, int e, float2 v) { base[(size_t)b * L + e] = v; };
   AUGUR_FFT_IO(L, 0, nr, ld, st, A, B, LS, tw, twmul, inverse != 0);
+}
+
+__global__ void __launch_bounds__(256) fft_rows_kernel(float2 *__restrict__ data, int64_t nrows, int RB, int L,
+                                                       FastDiv fdL, int twmul, int Lt,
+                                                       const float2 *__restrict__ twg, int inverse) {
+  fft_rows_kernel_body(data, nrows, RB, L, fdL, twmul, Lt, twg, inverse, (int)blockIdx.x);
 }
 
 // Row transforms (fft_rows_kernel) as a persistent kernel fed by bulk copies: the CTA takes row
@@ -1368,14 +1468,14 @@ struct GreenArgs {
 };
 
 template <int TY>
-__global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
+__device__ __forceinline__ void fft_z_green_kernel_body(const float2 *__restrict__ spec, GreenArgs a,
                                                           const float2 *__restrict__ twg,
-                                                          float2 *__restrict__ out) {
+                                                          float2 *__restrict__ out, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int G = a.G, M = G / 2;
   const int nyt = G / TY;
-  const int kx = blockIdx.x / nyt;
-  const int y0 = (blockIdx.x % nyt) * TY;
+  const int kx = bx / nyt;
+  const int y0 = (bx % nyt) * TY;
   const int tid = threadIdx.x, nt = blockDim.x;
   const size_t plane = (size_t)G * G;
   const size_t cstride = (size_t)(M + 1) * plane;
@@ -1418,6 +1518,13 @@ __global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restri
   }
 }
 
+template <int TY>
+__global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
+                                                          const float2 *__restrict__ twg,
+                                                          float2 *__restrict__ out) {
+  fft_z_green_kernel_body<TY>(spec, a, twg, out, (int)blockIdx.x);
+}
+
 // 2D isolated: pointwise product with the kernel spectrum (complex), spec[kx][ky].
 __global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict__ khat, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1429,6 +1536,7 @@ __global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict_
 // of every component. OUT4: writes F4[r][x] = (c0, c1, c2, c3 or 0) for x < L.
 // Otherwise writes component 0 as real rows out[r][x] for r < nkeep, x < Lkeep (times scale).
 // ---------------------------------------------------------------------------------
+constexpr int C2R_LU = 5;  // C2R input loads per thread in flight
 struct C2RArgs {
   int L, nrows, RB, ncomp, Lt;
   int nkeep, Lkeep;
@@ -1440,13 +1548,13 @@ struct C2RArgs {
 };
 
 template <bool OUT4>
-__global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
-                                                       const float2 *__restrict__ twg, float *__restrict__ out) {
+__device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ in, C2RArgs a,
+                                                       const float2 *__restrict__ twg, float *__restrict__ out, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int L = a.L, M = L / 2, RB = a.RB;
   const int MS = fft_row_stride(M);  // X holds the loaded rows (M + 1 values), then serves as transform scratch
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int r0 = blockIdx.x * RB;
+  const int r0 = bx * RB;
   float2 *X = reinterpret_cast<float2 *>(smem);
   float2 *Y = X + (size_t)RB * MS;
   float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [ncomp][RB][L]
@@ -1457,12 +1565,29 @@ __global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restri
   const int nc = OUT4 ? a.ncomp : 1;
   for (int c = 0; c < nc; ++c) {
     const float2 *src = in + c * cstride;
-    for (int e = tid; e < (M + 1) * RB; e += nt) {
-      int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
-      int r = r0 + rr;
-      float2 v = (r < a.nrows) ? src[(size_t)kx * a.nrows + r] : make_float2(0.f, 0.f);
-      if (kx == 0 || kx == M) v.y = 0.f;  // imaginary part of DC and Nyquist is ignored
-      X[rr * MS + kx] = v;
+    // C2R_LU loads per thread in flight before any is stored (the loads, 128-byte row pieces
+    // spread over M + 1 kx planes, are latency-bound one at a time)
+    for (int e0 = tid; e0 < (M + 1) * RB; e0 += nt * C2R_LU) {
+      float2 v[C2R_LU];
+#pragma unroll
+      for (int u = 0; u < C2R_LU; ++u) {
+        const int e = e0 + u * nt;
+        v[u] = make_float2(0.f, 0.f);
+        if (e < (M + 1) * RB) {
+          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
+          if (r0 + rr < a.nrows) v[u] = __ldcs(&src[(size_t)kx * a.nrows + r0 + rr]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < C2R_LU; ++u) {
+        const int e = e0 + u * nt;
+        if (e < (M + 1) * RB) {
+          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
+          float2 w = v[u];
+          if (kx == 0 || kx == M) w.y = 0.f;  // imaginary part of DC and Nyquist is ignored
+          X[rr * MS + kx] = w;
+        }
+      }
     }
     __syncthreads();
     // inverse transform whose first stage computes the pre-process on load:
@@ -1514,6 +1639,12 @@ __global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restri
   }
 }
 
+template <bool OUT4>
+__global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
+                                                       const float2 *__restrict__ twg, float *__restrict__ out) {
+  c2r_rows_kernel_body<OUT4>(in, a, twg, out, (int)blockIdx.x);
+}
+
 // 2D isolated: F4 grid from the potential by the reference's zero-padded central
 // difference (scripts/scatter_field.py:551-555): a_x = -((phi[y][x+1] - phi[y][x-1]) / (2h)).
 __global__ void fd_grad2d_kernel(const float *__restrict__ phi, int G, float two_h, float4 *__restrict__ F4) {
@@ -1557,15 +1688,15 @@ struct GatherArgs {
 };
 
 template <int D, int MODE>
-__global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
+__device__ __forceinline__ void gather_kernel_body(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
                                                      float4 *__restrict__ vel4, int64_t n, GatherArgs a,
                                                      float *__restrict__ acc_out, float *__restrict__ phi_out,
                                                      float *__restrict__ vel_out, uint32_t *__restrict__ key,
                                                      uint32_t *__restrict__ slot, uint32_t *__restrict__ row_count,
-                                                     unsigned *__restrict__ err) {
+                                                     unsigned *__restrict__ err, const int bx) {
   const GridParams &g = a.g;
   const int G = g.G;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = (int64_t)bx * blockDim.x + threadIdx.x;
   const bool valid = i < n;
   float4 p = make_float4(0.f, 0.f, 0.f, 0.f), v = p;
   if (valid) {
@@ -1669,7 +1800,7 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
       if (threadIdx.x < 2) {
         double t = 0.0;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sred[threadIdx.x][q];
-        a.epart[(size_t)blockIdx.x * 2 + threadIdx.x] = t;
+        a.epart[(size_t)bx * 2 + threadIdx.x] = t;
       }
     }
     if (valid) {
@@ -1712,6 +1843,16 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
       }
     }
   }
+}
+
+template <int D, int MODE>
+__global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
+                                                     float4 *__restrict__ vel4, int64_t n, GatherArgs a,
+                                                     float *__restrict__ acc_out, float *__restrict__ phi_out,
+                                                     float *__restrict__ vel_out, uint32_t *__restrict__ key,
+                                                     uint32_t *__restrict__ slot, uint32_t *__restrict__ row_count,
+                                                     unsigned *__restrict__ err) {
+  gather_kernel_body<D, MODE>(F4, pos4, vel4, n, a, acc_out, phi_out, vel_out, key, slot, row_count, err, (int)blockIdx.x);
 }
 
 // Fixed-order sum of the gather's per-block energy partials: out[0] kinetic, out[1] potential.
@@ -1779,6 +1920,143 @@ __global__ void cell_index_kernel(const float *__restrict__ pos, int64_t n, Grid
     i0[i * D + d] = c;
     w[i * D + d] = f;
   }
+}
+
+// ---------------------------------------------------------------------------------
+// Multi-scene launches: one grid covers the blocks of every scene of a batch for one stage of
+// the run loop. Scene s owns blocks [boff[s], boff[s+1]) of the grid; its block runs the
+// single-scene kernel body with the scene's arguments (a pack in device memory) and its local
+// block index, so every scene computes exactly what its own launch would.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int scene_of(const int *__restrict__ boff, int ns, int b) {
+  int lo = 0, hi = ns;  // boff[lo] <= b < boff[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&boff[mid]) <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+struct ScanPack {
+  uint32_t *count, *start, *tile_sum, *tile_off;
+  int nrow, ntiles;
+};
+struct ScatterPack {
+  const float4 *pos_in, *vel_in;
+  int64_t n;
+  const uint32_t *key, *slot, *start, *tile_off;
+  float4 *pos_out, *vel_out;
+};
+struct DepPlanPack {
+  const uint32_t *start, *tile_off;
+  DepositArgs a;
+  uint32_t *nch, *item_off, *slot_off, *item_blk;
+  uint4 *seg_tab;
+  unsigned *err;
+};
+struct DepPack {
+  const float4 *pos4;
+  const unsigned *mmax;
+  DepositArgs a;
+  const float2 *tw;
+  float2 *spec;
+  unsigned *err;
+  const uint32_t *item_off, *slot_off, *item_blk;
+  const uint4 *seg_tab;
+  unsigned long long *scratch;
+  unsigned *counters;
+};
+struct RowsPack {
+  float2 *data;
+  int64_t nrows;
+  int RB, L, twmul, Lt, inverse;
+  FastDiv fdL;
+  const float2 *tw;
+};
+struct GreenPack {
+  const float2 *spec;
+  GreenArgs a;
+  const float2 *tw;
+  float2 *out;
+};
+struct C2RPack {
+  const float2 *in;
+  C2RArgs a;
+  const float2 *tw;
+  float *out;
+};
+struct GatherPack {
+  const float4 *F4;
+  float4 *pos4, *vel4;
+  int64_t n;
+  GatherArgs a;
+  uint32_t *key, *slot, *row_count;
+  unsigned *err;
+};
+
+__global__ void __launch_bounds__(1024) scan_local_multi(const ScanPack *__restrict__ pk, const int *__restrict__ boff,
+                                                         int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const ScanPack q = pk[s];
+  scan_local_kernel_body(q.count, q.start, q.tile_sum, q.nrow, (int)blockIdx.x - boff[s]);
+}
+// one block per scene
+__global__ void __launch_bounds__(1024) scan_tiles_multi(const ScanPack *__restrict__ pk) {
+  const ScanPack q = pk[blockIdx.x];
+  scan_tiles_kernel_body(q.tile_sum, q.tile_off, q.ntiles, 0);
+}
+__global__ void __launch_bounds__(256) scatter_sorted_multi(const ScatterPack *__restrict__ pk,
+                                                            const int *__restrict__ boff, int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const ScatterPack q = pk[s];
+  scatter_sorted_kernel_body(q.pos_in, q.vel_in, q.n, q.key, q.slot, q.start, q.tile_off, q.pos_out, q.vel_out,
+                             (int)blockIdx.x - boff[s]);
+}
+__global__ void __launch_bounds__(256) deposit_count_multi(const DepPlanPack *__restrict__ pk,
+                                                           const int *__restrict__ boff, int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const DepPlanPack &q = pk[s];
+  deposit_count_kernel_body<3>(q.start, q.tile_off, q.a, q.nch, q.seg_tab, q.err, (int)blockIdx.x - boff[s]);
+}
+// one block per scene
+__global__ void __launch_bounds__(1024) deposit_plan_multi(const DepPlanPack *__restrict__ pk) {
+  const DepPlanPack &q = pk[blockIdx.x];
+  deposit_plan_kernel_body<3>(q.start, q.tile_off, q.a, q.nch, q.item_off, q.slot_off, q.seg_tab, q.item_blk, q.err, 0);
+}
+template <bool AGG>
+__global__ void __launch_bounds__(256, 4) deposit_multi(const DepPack *__restrict__ pk, const int *__restrict__ boff,
+                                                        int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const DepPack &q = pk[s];
+  deposit_kernel_body<3, 1, AGG>(q.pos4, q.mmax, q.a, q.tw, nullptr, q.spec, q.err, q.item_off, q.slot_off, q.seg_tab,
+                                 q.item_blk, q.scratch, q.counters, (int)blockIdx.x - boff[s]);
+}
+__global__ void __launch_bounds__(256) fft_rows_multi(const RowsPack *__restrict__ pk, const int *__restrict__ boff,
+                                                      int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const RowsPack &q = pk[s];
+  fft_rows_kernel_body(q.data, q.nrows, q.RB, q.L, q.fdL, q.twmul, q.Lt, q.tw, q.inverse, (int)blockIdx.x - boff[s]);
+}
+template <int TY>
+__global__ void __launch_bounds__(512) green_multi(const GreenPack *__restrict__ pk, const int *__restrict__ boff,
+                                                   int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const GreenPack &q = pk[s];
+  fft_z_green_kernel_body<TY>(q.spec, q.a, q.tw, q.out, (int)blockIdx.x - boff[s]);
+}
+__global__ void __launch_bounds__(512, 2) c2r_multi(const C2RPack *__restrict__ pk, const int *__restrict__ boff,
+                                                    int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const C2RPack &q = pk[s];
+  c2r_rows_kernel_body<true>(q.in, q.a, q.tw, q.out, (int)blockIdx.x - boff[s]);
+}
+__global__ void __launch_bounds__(256) gather_multi(const GatherPack *__restrict__ pk, const int *__restrict__ boff,
+                                                    int ns) {
+  const int s = scene_of(boff, ns, blockIdx.x);
+  const GatherPack &q = pk[s];
+  gather_kernel_body<3, MODE_KD>(q.F4, q.pos4, q.vel4, q.n, q.a, nullptr, nullptr, nullptr, q.key, q.slot,
+                                 q.row_count, q.err, (int)blockIdx.x - boff[s]);
 }
 
 }  // namespace augur

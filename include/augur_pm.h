@@ -229,6 +229,27 @@ int augur_pm_run_begin(augur_pm_plan *plan, const float *pos, const float *vel,
                        const float *mass, const float *mask, int64_t n, float dt,
                        void *stream);
 int augur_pm_run_steps(augur_pm_plan *plan, int k, void *stream);
+
+/*
+ * Batch of scenes stepped together: every plan (periodic, after augur_pm_run_begin, each with
+ * its own body count and grid) keeps its state, and augur_pm_batch_run_steps advances all of
+ * them by k merged steps with one launch per stage for the whole batch (11 launches per step:
+ * re-sort scans and scatter, deposit planning and deposit + x transform, y transform, z
+ * transform with the Green's function, inverse y transforms, x C2R, gather + kick-drift); each
+ * launch's blocks are dealt to the scenes by a table of block offsets, and every scene computes
+ * exactly what its own augur_pm_run_steps would, bit for bit. Replaces the reference's padded
+ * (B, Nmax, D) batch with one grid per batch (to_tensors, scripts/scatter_field.py:779-794);
+ * scenes here keep uneven body counts and grids. The plans must share the z-transform tile
+ * (green_tile_y) and the deposit variant (deposit_aggregate); their tile shapes, force-grid
+ * bindings and body counts are read at creation, so a batch is created again after any of them
+ * changes. augur_pm_run_end (or run_unload) of each plan ends the run as usual. create allocates
+ * the block tables (device memory) and synchronises the device; run_steps does not.
+ */
+typedef struct augur_pm_batch augur_pm_batch;
+int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int nplans);
+int augur_pm_batch_run_steps(augur_pm_batch *batch, int k, void *stream);
+int augur_pm_batch_size(const augur_pm_batch *batch);
+int augur_pm_batch_destroy(augur_pm_batch *batch);
 int augur_pm_run_end(augur_pm_plan *plan, float *pos, float *vel, float *acc_out,
                      void *stream);
 

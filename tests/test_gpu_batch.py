@@ -107,6 +107,34 @@ def test_batched_graph_equals_per_scene_runs():
     sim.close()
 
 
+@pytest.mark.parametrize("tiles", [None, "mixed"])
+def test_fused_batch_equals_per_scene_runs(tiles):
+    """One launch per stage for all scenes (augur_pm_batch_run_steps) against each scene's own
+    run: positions and velocities bit-identical, with scenes of different body counts, grids and
+    (second case) tile shapes, including a one-body scene."""
+    batch = _small_batch(count=9, seed=9400)
+    pos1, vel1, mass1 = scenes.make_scene("plummer", 1, seed=5)
+    batch.append({"kind": "plummer", "n": 1, "seed": 5, "grid": 32, "pos": pos1, "vel": vel1, "mass": mass1})
+    tl = None
+    if tiles == "mixed":
+        tl = {32: {"deposit_rows_y": 8, "c2r_rows": 16, "fft_rows": 8, "deposit_chunk": 1024},
+              48: {"deposit_rows_y": 16, "deposit_rows_z": 2, "c2r_rows": 8},
+              64: {"deposit_rows_y": 4, "fft_rows": 32, "c2r_rows": 32, "deposit_chunk": 4096}}
+    dt, k = 5e-4, 6
+    sim = BatchedPM(batch, dt=dt, tiles=tl, fused=True)
+    sim.begin()
+    sim.steps(k - 2)
+    sim.steps(2)
+    out = sim.end()
+    for sc, (p, v) in zip(batch, out):
+        plan = PMPlan(3, sc["grid"], sc["n"], "periodic", 1.0, device=DEV)
+        if tl:
+            plan.set_tiles(tl[sc["grid"]])
+        pr, vr = _run(plan, sc["pos"], sc["vel"], sc["mass"], dt, k + 1)
+        assert torch.equal(p, pr) and torch.equal(v, vr), (sc["kind"], sc["n"], sc["grid"])
+    sim.close()
+
+
 def _net(seed=1, scale=0.05):
     net = GridCNN(DEV, seed=seed, phi_scale=0.1, out_scale=1.0)
     g = torch.Generator().manual_seed(seed + 1)
