@@ -544,9 +544,7 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem);
   uint32_t *acc_hi = acc_lo + (size_t)RR * G;
   float *rows = reinterpret_cast<float *>(smem + region);
-  // the fp32 rows, or (fused spectrum path) the transform's scratch rows
-  const size_t rows_bytes = (size_t)RR * max(RS * 4, PS * 8);
-  float2 *tw = reinterpret_cast<float2 *>(smem + region + rows_bytes);
+  float2 *tw = reinterpret_cast<float2 *>(smem + region + (size_t)RR * RS * 4);
 
   const uint4 *tab = seg_tab + (size_t)blk * (MAXSEGB + 1);
   if (tid <= MAXSEGB) {
@@ -703,39 +701,6 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
     if (!s_last) return;
     __threadfence();
     if (tid == 0) counters[blk] = 0u;
-  }
-
-  if constexpr (MODE == 1) {
-    // spectrum only, two-stage row transforms (G = 64 .. 512 except 3-smooth lengths of three
-    // stages): the fixed-point sums are converted on the transform's first load, so there is no
-    // separate conversion pass. Stage 0 reads the accumulators (or the split block's tile) and
-    // writes the scratch rows; stage 1 writes the transformed rows over the accumulator area.
-    const int M = G / 2, MS = M + 1;
-    if (fft_nstages(M) == 2) {
-      auto conv = [&](int c) -> float {
-        unsigned long long q;
-        if (gtile) {  // the split block's total, and the tile cleared for the next call
-          q = __ldcg(&gtile[c]);
-          gtile[c] = 0ull;
-        } else {
-          q = ((unsigned long long)acc_hi[c] << 13) + acc_lo[c];
-        }
-        const float fq = (q >> 32) ? __ull2float_rn(q) : __uint2float_rn((unsigned)q);
-        return __fmul_rn(fq, qs.outscale);
-      };
-      float2 *Zt = reinterpret_cast<float2 *>(smem);  // transformed rows, stride MS
-      float2 *Sb = reinterpret_cast<float2 *>(rows);  // stage-0 output, padded rows of PS
-      {
-        auto ld = [&](int b, int e) -> float2 {
-          const int c = b * G + 2 * e;
-          return make_float2(conv(c), conv(c + 1));
-        };
-        auto st = [&](int b, int e, float2 v) { Zt[b * MS + e] = v; };
-        AUGUR_FFT_IO(M, 0, RR, ld, st, Zt, Sb, PS, tw, a.twmul, false);
-      }
-      deposit_r2c_post<D>(Zt, MS, M, RR, G, RY, z0, y0, a, tw, spec_out);
-      return;
-    }
   }
 
   // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
