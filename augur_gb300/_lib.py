@@ -35,6 +35,7 @@ SIGNATURES = {
     "augur_pm_gather": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     "augur_pm_force": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
     "augur_pm_step": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp]),
+    "augur_pm_step_host": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp]),
     "augur_pm_run": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _i32, _vp, _vp]),
     "augur_pm_run_begin": (_i32, [_vp, _vp, _vp, _vp, _vp, _i64, _f32, _vp]),
     "augur_pm_run_steps": (_i32, [_vp, _i32, _vp]),

@@ -433,13 +433,17 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
 // ---------------------------------------------------------------------------------------
 // Input layer on tcgen05: x (B, G^3, 2) bf16 -> z0 (optional), h0 = gelu(z0), 32 channels.
 // K = 27 taps x 2 channels = 54, padded to 64 (four K = 16 MMAs per tile); the A operand is
-// built in shared memory by four producer warps (im2col: thread r gathers the 27 neighbours of
-// voxel x0 + r, two channels each, into 16-byte K blocks), published to the MMA warp through
+// built in shared memory by producer warps (im2col: thread r gathers the 27 neighbours of voxel
+// x0 + r, two channels each, into 16-byte K blocks), published to the MMA warp through
 // full/empty mbarriers; the epilogue is the forward layers' (eight warps, two per TMEM lane
-// quarter). Weights: augur_cnn_prep_weights(w_in, 32, 2, 2, 32, 0) into a zeroed 64 x 32 buffer.
+// quarter). The producers form IN_GROUPS groups of 128 threads that take the tile rows in turn,
+// so that as many rows' gathers are in flight at once (one group's loads are a few L2 round trips
+// per row, which alone would bound the layer). Weights: augur_cnn_prep_weights(w_in, 32, 2, 2, 32,
+// 0) into a zeroed 64 x 32 buffer.
 // ---------------------------------------------------------------------------------------
-constexpr int IN_PROD_WARPS = 8;                        // 256 producer threads: two per voxel row
-constexpr int IN_STAGES = 4;                            // A buffers in flight
+constexpr int IN_PROD_WARPS = 16;                       // producer warps: IN_GROUPS x 128 threads
+constexpr int IN_GROUPS = IN_PROD_WARPS / 4;            // rows gathered at once
+constexpr int IN_STAGES = 8;                            // A buffers in flight
 constexpr int IN_KB = 8;                                // 16-byte K blocks (64 K values)
 constexpr int IN_ABYTES = IN_KB * CONV_M * 16;          // 16 KB per A buffer
 constexpr int IN_THREADS = 32 * (EPI_WARPS + 1 + IN_PROD_WARPS);
@@ -464,13 +468,13 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
     const uint4 *src = reinterpret_cast<const uint4 *>(wB);
     uint4 *dst = reinterpret_cast<uint4 *>(sW);
     for (int e = tid; e < IN_KB * N; e += IN_THREADS) dst[e] = src[e];
-    // K blocks 6 (upper half) and 7 of every A buffer are padding: zero once
+    // K block 7 of every A buffer is padding: zero once
     uint4 *A = reinterpret_cast<uint4 *>(sA);
     for (int e = tid; e < IN_STAGES * IN_KB * CONV_M; e += IN_THREADS) A[e] = make_uint4(0u, 0u, 0u, 0u);
   }
   if (tid == 0) {
     for (int i = 0; i < IN_STAGES; ++i) {
-      mbar_init(&full[i], 32 * IN_PROD_WARPS);
+      mbar_init(&full[i], CONV_M);
       mbar_init(&empty[i], 1);
     }
     for (int i = 0; i < NACC; ++i) {
@@ -502,10 +506,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
   };
 
   if (warp > MMA_WARP) {
-    // ---- producers: threads r and r + 128 build row r of the tile's A operand (K blocks 0-3
-    // and 4-6 respectively) ---------------------------------------------------------------------
+    // ---- producers: thread r of group grp builds row r of the A operand of tiles t with
+    // t % IN_GROUPS == grp (K blocks 0-6; block 7 and tap 27 are padding) ---------------------
     const int pr = tid - 32 * (MMA_WARP + 1);
-    const int r = pr & (CONV_M - 1), kh = pr >> 7;
+    const int r = pr & (CONV_M - 1), grp = pr >> 7;
     const uint32_t *x32 = reinterpret_cast<const uint32_t *>(x);  // two bf16 channels per voxel
     uint32_t t = 0;
     bool go = true;
@@ -514,28 +518,26 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
       const size_t bbase = (size_t)u.b * G * G * G;
       const int xx = u.x0 + r;
       for (int i = 0; i < u.ny; ++i, ++t) {
+        if ((int)(t % IN_GROUPS) != grp) continue;
         const uint32_t st = t % IN_STAGES, n = t / IN_STAGES;
         if (n > 0 && !wait(&empty[st], (n - 1) & 1u)) {
           go = false;
           break;
         }
         const int y = u.ya + i;
-        const int t0 = kh * 16;  // taps t0 .. t0 + 15 (K blocks 4 kh .. 4 kh + 3; tap 27 is padding)
-        uint32_t v[16];
+        uint32_t v[28];
 #pragma unroll
-        for (int tt = 0; tt < 16; ++tt) {
-          const int tap = t0 + tt;
+        for (int tap = 0; tap < 28; ++tap) {
           const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
           const int zz = u.z + dz, yy = y + dy, xq = xx + dx;
           const bool in = tap < 27 && zz >= 0 && zz < G && yy >= 0 && yy < G && xq >= 0 && xq < G;
-          v[tt] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
+          v[tap] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
         }
         unsigned char *A = sA + (size_t)st * IN_ABYTES;
 #pragma unroll
-        for (int kb = 0; kb < 4; ++kb)
-          if (4 * kh + kb < 7)
-            *reinterpret_cast<uint4 *>(A + ((size_t)(4 * kh + kb) * CONV_M + r) * 16) =
-                make_uint4(v[4 * kb], v[4 * kb + 1], v[4 * kb + 2], v[4 * kb + 3]);
+        for (int kb = 0; kb < 7; ++kb)
+          *reinterpret_cast<uint4 *>(A + ((size_t)kb * CONV_M + r) * 16) =
+              make_uint4(v[4 * kb], v[4 * kb + 1], v[4 * kb + 2], v[4 * kb + 3]);
         fence_async_smem();  // generic-proxy stores -> visible to the tensor core
         mbar_arrive(&full[st]);
       }

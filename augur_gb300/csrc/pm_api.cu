@@ -18,6 +18,10 @@
 
 using namespace augur;
 
+// Chunks of caller bodies in the host-buffer step: the copies of one chunk overlap the kernels of
+// the chunks before it.
+constexpr int HS_CHUNKS = 8;
+
 struct augur_pm_plan {
   int dim, G, mode;
   double extent, eps, gnewton;
@@ -68,11 +72,19 @@ struct augur_pm_plan {
   unsigned epart_n;
   int64_t launches;
   size_t bytes;
+  // host-buffer step (augur_pm_step_host): device copies of the caller's pos, vel, acc, two copy
+  // streams, and the events that order chunks between them and the caller's stream
+  float *hs_buf;
+  cudaStream_t hs_in, hs_out;
+  cudaEvent_t hs_ev[3 * HS_CHUNKS + 2];
 };
 
 namespace {
 
 int cuda_status(cudaError_t e) { return e == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA; }
+
+// scratch buffers of the z transform in fft_z_green_kernel (two stages ping-pong through one)
+int green_nbuf(int G) { return fft_nstages(G) > 2 ? 2 : 1; }
 
 #define AUGUR_LAUNCH_CHECK(plan)                      \
   do {                                                \
@@ -146,37 +158,54 @@ cudaStream_t S(void *s) { return (cudaStream_t)s; }
 
 // ---- pipeline pieces ----------------------------------------------------------------
 
-int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *acc, const float *mass,
-                  const float *mask, int64_t n, bool drift, float dt, cudaStream_t st) {
+// Keys, slots and the row histogram of caller bodies off .. off + cnt - 1 (the arrays are the
+// caller's whole arrays; key/slot are indexed like them), with the optional velocity-Verlet drift.
+int keys_hist_range(augur_pm_plan *p, float *pos, const float *vel, const float *acc, const float *mass,
+                    const float *mask, int64_t off, int64_t cnt, bool drift, float dt, cudaStream_t st) {
+  if (cnt <= 0) return AUGUR_OK;
   const GridParams &g = p->gp;
+  const int D = p->dim;
+  const unsigned nb = blocks_for(cnt, 256);
+  const float hdt2 = (float)(0.5 * (double)dt * (double)dt);
+  float *ps = pos + off * D;
+  const float *vs = vel ? vel + off * D : nullptr, *as = acc ? acc + off * D : nullptr;
+  const float *ms = mass + off, *ks = mask + off;
+  uint32_t *key = p->key + off, *slot = p->slot + off;
+  if (D == 3) {
+    if (drift)
+      keys_hist_aos_kernel<3, true><<<nb, 256, 0, st>>>(ps, vs, as, ms, ks, cnt, g, dt, hdt2, key, slot, p->row_count,
+                                                       p->d_mmax, p->d_err);
+    else
+      keys_hist_aos_kernel<3, false><<<nb, 256, 0, st>>>(ps, vs, as, ms, ks, cnt, g, dt, hdt2, key, slot,
+                                                        p->row_count, p->d_mmax, p->d_err);
+  } else {
+    if (drift)
+      keys_hist_aos_kernel<2, true><<<nb, 256, 0, st>>>(ps, vs, as, ms, ks, cnt, g, dt, hdt2, key, slot, p->row_count,
+                                                       p->d_mmax, p->d_err);
+    else
+      keys_hist_aos_kernel<2, false><<<nb, 256, 0, st>>>(ps, vs, as, ms, ks, cnt, g, dt, hdt2, key, slot,
+                                                        p->row_count, p->d_mmax, p->d_err);
+  }
+  AUGUR_LAUNCH_CHECK(p);
+  return AUGUR_OK;
+}
+
+int sort_begin(augur_pm_plan *p, int64_t n, cudaStream_t st) {
   p->cur_n = n;
   if (cudaMemsetAsync(p->row_count, 0, sizeof(uint32_t) * p->nrow, st) != cudaSuccess) return AUGUR_ECUDA;
   if (cudaMemsetAsync(p->d_mmax, 0, sizeof(unsigned), st) != cudaSuccess) return AUGUR_ECUDA;
-  const unsigned nb = blocks_for(n, 256);
-  const float hdt2 = (float)(0.5 * (double)dt * (double)dt);
-  if (n > 0) {
-    if (p->dim == 3) {
-      if (drift)
-        keys_hist_aos_kernel<3, true><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key, p->slot,
-                                                         p->row_count, p->d_mmax, p->d_err);
-      else
-        keys_hist_aos_kernel<3, false><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key,
-                                                          p->slot, p->row_count, p->d_mmax, p->d_err);
-    } else {
-      if (drift)
-        keys_hist_aos_kernel<2, true><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key, p->slot,
-                                                         p->row_count, p->d_mmax, p->d_err);
-      else
-        keys_hist_aos_kernel<2, false><<<nb, 256, 0, st>>>(pos, vel, acc, mass, mask, n, g, dt, hdt2, p->key,
-                                                          p->slot, p->row_count, p->d_mmax, p->d_err);
-    }
-    AUGUR_LAUNCH_CHECK(p);
-  }
+  return AUGUR_OK;
+}
+
+// scan of the histogram and the scatter of the caller's bodies into sorted order
+int sort_finish(augur_pm_plan *p, const float *pos, const float *vel, const float *mass, const float *mask, int64_t n,
+                cudaStream_t st) {
   scan_local_kernel<<<p->ntiles, 1024, 0, st>>>(p->row_count, p->row_start, p->tile_sum, p->nrow);
   AUGUR_LAUNCH_CHECK(p);
   scan_tiles_kernel<<<1, 1024, 0, st>>>(p->tile_sum, p->tile_off, p->ntiles);
   AUGUR_LAUNCH_CHECK(p);
   if (n > 0) {
+    const unsigned nb = blocks_for(n, 256);
     if (p->dim == 3)
       scatter_aos_kernel<3><<<nb, 256, 0, st>>>(pos, vel, mass, mask, n, p->key, p->slot, p->row_start, p->tile_off,
                                                 p->pos4[p->cur], p->vel4[p->cur]);
@@ -186,6 +215,14 @@ int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *a
     AUGUR_LAUNCH_CHECK(p);
   }
   return AUGUR_OK;
+}
+
+int sort_from_aos(augur_pm_plan *p, float *pos, const float *vel, const float *acc, const float *mass,
+                  const float *mask, int64_t n, bool drift, float dt, cudaStream_t st) {
+  int rc = sort_begin(p, n, st);
+  if (!rc) rc = keys_hist_range(p, pos, vel, acc, mass, mask, 0, n, drift, dt, st);
+  if (!rc) rc = sort_finish(p, pos, vel, mass, mask, n, st);
+  return rc;
 }
 
 // re-sort the run state after a gather that produced keys + histogram
@@ -309,13 +346,14 @@ int launch_green(augur_pm_plan *p, int ncomp, cudaStream_t st) {
   ga.TY = p->green_TY;
   ga.ncomp = ncomp;
   ga.Lt = p->Lt;
+  ga.nbuf = green_nbuf(G);
   ga.fsh = p->sh_L;
   ga.kfund = (float)(2.0 * M_PI / p->extent);
   ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
   if (p->green_TY == 16)
-    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), green_threads<16>(), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
   else
-    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), 512, p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), green_threads<8>(), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -417,17 +455,52 @@ GatherArgs gather_args(const augur_pm_plan *p, float kick, float dt, int drift) 
   return a;
 }
 
-int gather_force(augur_pm_plan *p, const float4 *F4, int64_t n, float *acc, float *phi, cudaStream_t st) {
-  if (n == 0) return AUGUR_OK;
+// Gather at the sorted bodies (after sort_from_aos) into the caller's order: gather_sorted puts
+// the sorted accelerations (float4: a * mask, phi * mask) in the free half of the body double
+// buffer, then accel_to_caller writes acc / phi for caller bodies off .. off + cnt - 1 (vel == null)
+// or applies the velocity-Verlet kick to their vel and acc.
+float4 *gather_sorted(augur_pm_plan *p, const float4 *F4, int64_t n, cudaStream_t st) {
   GatherArgs a = gather_args(p, 0.f, 0.f, 0);
+  float4 *acc4s = p->pos4[p->cur ^ 1];
+  const unsigned nb = blocks_for(n, 256);
+  float *a4 = reinterpret_cast<float *>(acc4s);
   if (p->dim == 3)
-    gather_kernel<3, MODE_FORCE><<<blocks_for(n, 256), 256, 0, st>>>(
-        F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc, phi, nullptr, nullptr, nullptr, nullptr, p->d_err);
+    gather_kernel<3, MODE_FORCE><<<nb, 256, 0, st>>>(F4, p->pos4[p->cur], p->vel4[p->cur], n, a, a4, nullptr,
+                                                     nullptr, nullptr, nullptr, nullptr, p->d_err);
   else
-    gather_kernel<2, MODE_FORCE><<<blocks_for(n, 256), 256, 0, st>>>(
-        F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc, phi, nullptr, nullptr, nullptr, nullptr, p->d_err);
+    gather_kernel<2, MODE_FORCE><<<nb, 256, 0, st>>>(F4, p->pos4[p->cur], p->vel4[p->cur], n, a, a4, nullptr,
+                                                     nullptr, nullptr, nullptr, nullptr, p->d_err);
+  return acc4s;
+}
+
+int accel_to_caller(augur_pm_plan *p, const float4 *acc4s, int64_t off, int64_t cnt, float *acc, float *phi,
+                    float *vel, float kick, cudaStream_t st) {
+  if (cnt <= 0) return AUGUR_OK;
+  const int D = p->dim;
+  const unsigned nb = blocks_for(cnt, 256);
+  const uint32_t *k = p->key + off, *sl = p->slot + off, *rs = p->row_start, *to = p->tile_off;
+  float *ac = acc + off * D, *ph = phi ? phi + off : nullptr, *ve = vel ? vel + off * D : nullptr;
+  if (vel) {
+    if (D == 3)
+      accel_to_caller_kernel<3, true><<<nb, 256, 0, st>>>(acc4s, cnt, k, sl, rs, to, kick, ac, ph, ve);
+    else
+      accel_to_caller_kernel<2, true><<<nb, 256, 0, st>>>(acc4s, cnt, k, sl, rs, to, kick, ac, ph, ve);
+  } else {
+    if (D == 3)
+      accel_to_caller_kernel<3, false><<<nb, 256, 0, st>>>(acc4s, cnt, k, sl, rs, to, 0.f, ac, ph, nullptr);
+    else
+      accel_to_caller_kernel<2, false><<<nb, 256, 0, st>>>(acc4s, cnt, k, sl, rs, to, 0.f, ac, ph, nullptr);
+  }
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
+}
+
+int gather_force(augur_pm_plan *p, const float4 *F4, int64_t n, float *acc, float *phi, cudaStream_t st,
+                 float *vel = nullptr, float kick = 0.f) {
+  if (n == 0) return AUGUR_OK;
+  const float4 *acc4s = gather_sorted(p, F4, n, st);
+  AUGUR_LAUNCH_CHECK(p);
+  return accel_to_caller(p, acc4s, 0, n, acc, phi, vel, kick, st);
 }
 
 // ---- tile shapes ----------------------------------------------------------------------
@@ -467,8 +540,9 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   // shared memory of each kernel (layouts in pm_kernels.cuh; transform rows padded by fft_row_stride)
   const size_t PM = (size_t)fft_row_stride(M), PL = (size_t)fft_row_stride(L);
   const size_t s_dep = (size_t)RY * RZ * (2 * PM * 8 + (size_t)(G + 2) * 4) + (size_t)Lt * 8;
-  const size_t s_green = (size_t)3 * G * t->green_tile_y * 8 + (size_t)Lt * 8;
-  const size_t s_c2r = (size_t)2 * RB * PM * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 + (size_t)Lt * 8;
+  const size_t s_green = (size_t)(1 + green_nbuf(G)) * G * t->green_tile_y * 8 + (size_t)Lt * 8;
+  const size_t s_c2r = ((size_t)c2r_x_elems(M, RB) + (size_t)RB * PM) * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 +
+                       (size_t)Lt * 8;
   const size_t s_rows = (size_t)2 * t->fft_rows * PL * 8 + (size_t)Lt * 8;
   const size_t s_r2c = (size_t)16 * ((M + 1) + 2 * PM) * 8 + (size_t)Lt * 8;
   const size_t lim = p->smem_max;
@@ -610,6 +684,12 @@ int augur_pm_plan_destroy(augur_pm_plan *p) {
                   p->pair_sorted, p->pair_params, p->pair_nbj, p->pair_nbq};
   for (void *q : ptrs)
     if (q) cudaFree(q);
+  if (p->hs_buf) {
+    cudaFree(p->hs_buf);
+    cudaStreamDestroy(p->hs_in);
+    cudaStreamDestroy(p->hs_out);
+    for (cudaEvent_t e : p->hs_ev) cudaEventDestroy(e);
+  }
   delete p;
   return AUGUR_OK;
 }
@@ -832,16 +912,93 @@ int augur_pm_step(augur_pm_plan *p, float *pos, float *vel, float *acc, const fl
   if (rc) return rc;
   rc = grid_force(p, 3, st);
   if (rc) return rc;
-  if (n == 0) return AUGUR_OK;
-  GatherArgs a = gather_args(p, (float)(0.5 * (double)dt), dt, 0);
-  if (p->dim == 3)
-    gather_kernel<3, MODE_VV><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc,
-                                                                  nullptr, vel, nullptr, nullptr, nullptr, p->d_err);
-  else
-    gather_kernel<2, MODE_VV><<<blocks_for(n, 256), 256, 0, st>>>(p->F4, p->pos4[p->cur], p->vel4[p->cur], n, a, acc,
-                                                                  nullptr, vel, nullptr, nullptr, nullptr, p->d_err);
+  return gather_force(p, p->F4, n, acc, nullptr, st, vel, (float)(0.5 * (double)dt));
+}
+
+int augur_pm_step_host(augur_pm_plan *p, float *pos, float *vel, float *acc, const float *mass, const float *mask,
+                       int64_t n, float dt, int have_acc, void *stream) {
+  int rc = check_plan(p, n);
+  if (rc) return rc;
+  if (n > 0 && (!pos || !vel || !acc || !mass || !mask)) return AUGUR_EINVAL;
+  cudaStream_t st = S(stream);
+  const int D = p->dim;
+  if (!p->hs_buf) {
+    if (cudaMalloc(&p->hs_buf, sizeof(float) * 3 * (size_t)p->max_n * D) != cudaSuccess) {
+      p->hs_buf = nullptr;
+      return AUGUR_ENOMEM;
+    }
+    bool ok = cudaStreamCreateWithFlags(&p->hs_in, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&p->hs_out, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t &e : p->hs_ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) return AUGUR_ECUDA;
+    p->bytes += sizeof(float) * 3 * (size_t)p->max_n * D;
+  }
+  float *dpos = p->hs_buf, *dvel = dpos + (size_t)p->max_n * D, *dacc = dvel + (size_t)p->max_n * D;
+  const size_t rb = sizeof(float) * D;  // bytes per body of pos, vel, acc
+  auto h2d = [&](float *d, const float *h, int64_t off, int64_t cnt, cudaStream_t s) {
+    return cudaMemcpyAsync(d + off * D, h + off * D, (size_t)cnt * rb, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  };
+  auto d2h = [&](float *h, const float *d, int64_t off, int64_t cnt, cudaStream_t s) {
+    return cudaMemcpyAsync(h + off * D, d + off * D, (size_t)cnt * rb, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  };
+  if (!have_acc || n == 0) {
+    // first step (the force at the start positions comes first): whole arrays in, out
+    if (n > 0 && !(h2d(dpos, pos, 0, n, st) && h2d(dvel, vel, 0, n, st))) return AUGUR_ECUDA;
+    rc = augur_pm_step(p, dpos, dvel, dacc, mass, mask, n, dt, have_acc, stream);
+    if (rc) return rc;
+    if (n > 0 && !(d2h(pos, dpos, 0, n, st) && d2h(vel, dvel, 0, n, st) && d2h(acc, dacc, 0, n, st)))
+      return AUGUR_ECUDA;
+    return AUGUR_OK;
+  }
+  p->launches = 0;
+  p->run_active = 0;
+  const int nc = (int)std::min<int64_t>(HS_CHUNKS, n);
+  auto lo = [&](int c) { return n * c / nc; };
+  cudaEvent_t *ev_in = p->hs_ev, *ev_drift = p->hs_ev + HS_CHUNKS, *ev_kick = p->hs_ev + 2 * HS_CHUNKS;
+  cudaEvent_t ev_start = p->hs_ev[3 * HS_CHUNKS], ev_done = p->hs_ev[3 * HS_CHUNKS + 1];
+  bool ok = cudaEventRecord(ev_start, st) == cudaSuccess && cudaStreamWaitEvent(p->hs_in, ev_start, 0) == cudaSuccess &&
+            cudaStreamWaitEvent(p->hs_out, ev_start, 0) == cudaSuccess;
+  // inputs in by chunks; each chunk's drift, keys and histogram start as soon as it has landed
+  for (int c = 0; ok && c < nc; ++c) {
+    const int64_t a = lo(c), cnt = lo(c + 1) - a;
+    ok = h2d(dpos, pos, a, cnt, p->hs_in) && h2d(dvel, vel, a, cnt, p->hs_in) && h2d(dacc, acc, a, cnt, p->hs_in) &&
+         cudaEventRecord(ev_in[c], p->hs_in) == cudaSuccess;
+  }
+  if (!ok) return AUGUR_ECUDA;
+  rc = sort_begin(p, n, st);
+  for (int c = 0; !rc && c < nc; ++c) {
+    const int64_t a = lo(c), cnt = lo(c + 1) - a;
+    if (cudaStreamWaitEvent(st, ev_in[c], 0) != cudaSuccess) return AUGUR_ECUDA;
+    rc = keys_hist_range(p, dpos, dvel, dacc, mass, mask, a, cnt, true, dt, st);
+    if (!rc && cudaEventRecord(ev_drift[c], st) != cudaSuccess) rc = AUGUR_ECUDA;
+  }
+  if (rc) return rc;
+  // the drifted positions are final: out while the grid is solved
+  for (int c = 0; ok && c < nc; ++c) {
+    const int64_t a = lo(c), cnt = lo(c + 1) - a;
+    ok = cudaStreamWaitEvent(p->hs_out, ev_drift[c], 0) == cudaSuccess && d2h(pos, dpos, a, cnt, p->hs_out);
+  }
+  if (!ok) return AUGUR_ECUDA;
+  rc = sort_finish(p, dpos, dvel, mass, mask, n, st);
+  if (!rc) rc = grid_force(p, 3, st);
+  if (rc) return rc;
+  const float4 *acc4s = gather_sorted(p, p->F4, n, st);
   AUGUR_LAUNCH_CHECK(p);
-  return AUGUR_OK;
+  const float kick = (float)(0.5 * (double)dt);
+  for (int c = 0; !rc && c < nc; ++c) {
+    const int64_t a = lo(c), cnt = lo(c + 1) - a;
+    rc = accel_to_caller(p, acc4s, a, cnt, dacc, nullptr, dvel, kick, st);
+    if (!rc && cudaEventRecord(ev_kick[c], st) != cudaSuccess) rc = AUGUR_ECUDA;
+  }
+  if (rc) return rc;
+  for (int c = 0; ok && c < nc; ++c) {
+    const int64_t a = lo(c), cnt = lo(c + 1) - a;
+    ok = cudaStreamWaitEvent(p->hs_out, ev_kick[c], 0) == cudaSuccess && d2h(vel, dvel, a, cnt, p->hs_out) &&
+         d2h(acc, dacc, a, cnt, p->hs_out);
+  }
+  // the caller's stream completes only after every copy
+  ok = ok && cudaEventRecord(ev_done, p->hs_out) == cudaSuccess && cudaStreamWaitEvent(st, ev_done, 0) == cudaSuccess;
+  return ok ? AUGUR_OK : AUGUR_ECUDA;
 }
 
 static int run_gather(augur_pm_plan *p, float kick, int drift, float *acc_out, cudaStream_t st,
@@ -1350,6 +1507,7 @@ int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int
     ga.TY = p->green_TY;
     ga.ncomp = 3;
     ga.Lt = p->Lt;
+    ga.nbuf = green_nbuf(G);
     ga.fsh = p->sh_L;
     ga.kfund = (float)(2.0 * M_PI / p->extent);
     ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
@@ -1448,9 +1606,9 @@ int augur_pm_batch_run_steps(augur_pm_batch *b, int k, void *stream) {
       deposit_multi<false><<<b->tot_dep, DEP_THREADS, b->smem_dep, st>>>(b->dep + (size_t)par * ns, off(BS_DEP), ns);
     fft_rows_multi<<<b->tot_rows_f, 256, b->smem_rows, st>>>(b->rows_f, off(BS_ROWS_F), ns);
     if (b->green_ty == 16)
-      green_multi<16><<<b->tot_green, 512, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+      green_multi<16><<<b->tot_green, green_threads<16>(), b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
     else
-      green_multi<8><<<b->tot_green, 512, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+      green_multi<8><<<b->tot_green, green_threads<8>(), b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
     fft_rows_multi<<<b->tot_rows_i, 256, b->smem_rows, st>>>(b->rows_i, off(BS_ROWS_I), ns);
     c2r_multi<<<b->tot_c2r, 512, b->smem_c2r, st>>>(b->c2r, off(BS_C2R), ns);
     if (b->tot_gather)

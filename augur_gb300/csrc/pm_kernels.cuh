@@ -84,7 +84,10 @@ __device__ __forceinline__ uint32_t row_key(const GridParams &g, int ix, int iy,
   return on ? (uint32_t)(iy + 1) : (uint32_t)(g.G + 1);
 }
 
-// Warp-aggregated slot within a row: one atomicAdd per distinct key per warp.
+// Warp-aggregated slot within a row: one atomicAdd per distinct key per warp (in sorted order
+// the lanes of a warp share a few row keys even after a drift has moved some of them; adding per
+// run of equal adjacent keys instead measured 80 -> 128 us for the gather at 3M bodies, from the
+// extra adds on the same hot row counters).
 // All 32 lanes must call this together.
 __device__ __forceinline__ uint32_t warp_slot(uint32_t *row_count, uint32_t key, bool valid) {
   const int lane = threadIdx.x & 31;
@@ -1427,6 +1430,7 @@ __global__ void __launch_bounds__(PTC_M) pair_weight_tc_kernel(const float4 *__r
 // ---------------------------------------------------------------------------------
 struct GreenArgs {
   int G, TY, ncomp, Lt;
+  int nbuf;        // transform scratch buffers: 1 for two-stage lengths (the stages meet in one), else 2
   FftShape fsh;    // length G
   float kfund;     // 2 pi / box
   float gfac;      // -4 pi G_newton / G^3
@@ -1446,7 +1450,7 @@ __device__ __forceinline__ void fft_z_green_kernel_body(const float2 *__restrict
   const size_t cstride = (size_t)(M + 1) * plane;
   float2 *P = reinterpret_cast<float2 *>(smem);
   float2 *B = P + (size_t)G * TY;
-  float2 *C = B + (size_t)G * TY;
+  float2 *C = B + (size_t)(a.nbuf - 1) * G * TY;
   float2 *tw = C + (size_t)G * TY;
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
   __syncthreads();
@@ -1483,8 +1487,13 @@ __device__ __forceinline__ void fft_z_green_kernel_body(const float2 *__restrict
   }
 }
 
+// 16 TY threads: one per (column, butterfly) of a radix-16 stage of a 256-point column
+// transform, so no thread idles through the stages (measured 101 -> 92 us at 256^3 against 512)
 template <int TY>
-__global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
+constexpr int green_threads() { return 16 * TY; }
+
+template <int TY>
+__global__ void __launch_bounds__(green_threads<TY>(), 1024 / green_threads<TY>()) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
                                                           const float2 *__restrict__ twg,
                                                           float2 *__restrict__ out) {
   fft_z_green_kernel_body<TY>(spec, a, twg, out, (int)blockIdx.x);
@@ -1502,6 +1511,14 @@ __global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict_
 // Otherwise writes component 0 as real rows out[r][x] for r < nkeep, x < Lkeep (times scale).
 // ---------------------------------------------------------------------------------
 constexpr int C2R_LU = 5;  // C2R input loads per thread in flight
+// The C2R input block X is stored [kx][row] with RB + 2 float2 per kx (consecutive rows of one kx
+// land on consecutive banks for the loads, and the first stage's reads of X_k and X_{M-k} by
+// (row, butterfly) lanes spread over the banks); for transforms of three or more stages X is also
+// the second scratch buffer, rows of fft_row_stride(M).
+__host__ __device__ inline int c2r_x_elems(int M, int RB) {
+  const int a = (M + 1) * (RB + 2), b = RB * fft_row_stride(M);
+  return a > b ? a : b;
+}
 struct C2RArgs {
   int L, nrows, RB, ncomp, Lt;
   int nkeep, Lkeep;
@@ -1517,11 +1534,12 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
                                                        const float2 *__restrict__ twg, float *__restrict__ out, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int L = a.L, M = L / 2, RB = a.RB;
-  const int MS = fft_row_stride(M);  // X holds the loaded rows (M + 1 values), then serves as transform scratch
+  const int MS = fft_row_stride(M);  // scratch row stride
+  const int XP = RB + 2;             // X[kx * XP + row]
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = bx * RB;
   float2 *X = reinterpret_cast<float2 *>(smem);
-  float2 *Y = X + (size_t)RB * MS;
+  float2 *Y = X + c2r_x_elems(M, RB);
   float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [ncomp][RB][L]
   float2 *tw = reinterpret_cast<float2 *>(res + (size_t)(OUT4 ? 4 : 1) * RB * L);
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
@@ -1550,7 +1568,7 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
           const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
           float2 w = v[u];
           if (kx == 0 || kx == M) w.y = 0.f;  // imaginary part of DC and Nyquist is ignored
-          X[rr * MS + kx] = w;
+          X[kx * XP + rr] = w;
         }
       }
     }
@@ -1559,8 +1577,8 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
     // E_k = X_k + conj X_{M-k} ; O_k = (X_k - conj X_{M-k}) W^{-k} ; Z_k = E_k + i O_k
     float *dst = res + (size_t)c * RB * L;
     auto ld = [&](int b, int k) -> float2 {
-      float2 xk = X[b * MS + k];
-      float2 xc = cconj(X[b * MS + (M - k)]);
+      float2 xk = X[k * XP + b];
+      float2 xc = cconj(X[(M - k) * XP + b]);
       float2 E = cadd(xk, xc);
       float2 O = cmul(csub(xk, xc), cconj(tw[k * tstep]));
       return make_float2(E.x - O.y, E.y + O.x);
@@ -1636,13 +1654,12 @@ __global__ void kernel_lattice_kernel(float *__restrict__ K, int G2, float h, fl
 
 // ---------------------------------------------------------------------------------
 // K4: CIC gather of F4 at the sorted bodies, fused with the integrator.
-//   MODE_FORCE : acc[id] = a * mask, phi[id]
+//   MODE_FORCE : acc4s[i] = (a * mask, phi * mask) in sorted order (float4, coalesced); the
+//                caller's arrays are written by accel_to_caller_kernel
 //   MODE_KD    : v += kick * a ; if drift: x += dt * v, wrap, new row key + slot (run loop)
-//   MODE_VV    : velocity-Verlet kick on caller arrays: vel[id] += (dt/2)*(acc[id] + a);
-//                acc[id] = a (scripts/scatter_field.py:686-688)
 // Corner order and fp32 operation order follow ScatterField.gather (:252-261).
 // ---------------------------------------------------------------------------------
-enum { MODE_FORCE = 0, MODE_KD = 1, MODE_VV = 2 };
+enum { MODE_FORCE = 0, MODE_KD = 1 };
 
 struct GatherArgs {
   GridParams g;
@@ -1718,24 +1735,9 @@ __device__ __forceinline__ void gather_kernel_body(const float4 *__restrict__ F4
   const uint32_t id = idw & 0x7fffffffu;
   const float mk = (idw & 0x80000000u) ? 0.f : 1.f;
   if (MODE == MODE_FORCE) {
-    if (valid) {
-      acc_out[(size_t)id * D] = __fmul_rn(ax, mk);
-      acc_out[(size_t)id * D + 1] = __fmul_rn(ay, mk);
-      if (D == 3) acc_out[(size_t)id * D + 2] = __fmul_rn(az, mk);
-      if (phi_out) phi_out[id] = __fmul_rn(ph, mk);
-    }
-  } else if (MODE == MODE_VV) {
-    if (valid) {
-      float an[3] = {__fmul_rn(ax, mk), __fmul_rn(ay, mk), __fmul_rn(az, mk)};
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        float ao = acc_out[(size_t)id * D + d];
-        float dv = __fmul_rn(a.kick, __fadd_rn(ao, an[d]));
-        vel_out[(size_t)id * D + d] = __fadd_rn(vel_out[(size_t)id * D + d], dv);
-        acc_out[(size_t)id * D + d] = an[d];
-      }
-      if (phi_out) phi_out[id] = __fmul_rn(ph, mk);
-    }
+    if (valid)
+      reinterpret_cast<float4 *>(acc_out)[i] =
+          make_float4(__fmul_rn(ax, mk), __fmul_rn(ay, mk), __fmul_rn(az, mk), __fmul_rn(ph, mk));
   } else {  // MODE_KD on the sorted state
     uint32_t k = 0;
     if (valid) {
@@ -1818,6 +1820,36 @@ __global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ slot, uint32_t *__restrict__ row_count,
                                                      unsigned *__restrict__ err) {
   gather_kernel_body<D, MODE>(F4, pos4, vel4, n, a, acc_out, phi_out, vel_out, key, slot, row_count, err, (int)blockIdx.x);
+}
+
+// Caller-order pass after a MODE_FORCE gather. Body j of the caller's arrays sits at sorted slot
+// row_begin(key[j]) + slot[j] (where scatter_aos put it), so its acceleration is read there (the
+// sorted float4s and the row starts stay in L2) while the caller's arrays are read and written in
+// their own order, coalesced, instead of one scattered read-modify-write per body.
+//   VV = false: acc[j] = a ; phi[j] = phi (when given)
+//   VV = true : velocity-Verlet kick vel[j] += kick * (acc[j] + a) ; acc[j] = a
+//               (scripts/scatter_field.py:686-688)
+template <int D, bool VV>
+__global__ void __launch_bounds__(256) accel_to_caller_kernel(const float4 *__restrict__ acc4s, int64_t n,
+                                                              const uint32_t *__restrict__ key,
+                                                              const uint32_t *__restrict__ slot,
+                                                              const uint32_t *__restrict__ start,
+                                                              const uint32_t *__restrict__ tile_off, float kick,
+                                                              float *__restrict__ acc, float *__restrict__ phi,
+                                                              float *__restrict__ vel) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const float4 a = acc4s[row_begin(start, tile_off, key[j]) + slot[j]];
+  const float an[3] = {a.x, a.y, a.z};
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    if (VV) {
+      const float dv = __fmul_rn(kick, __fadd_rn(acc[(size_t)j * D + d], an[d]));
+      vel[(size_t)j * D + d] = __fadd_rn(vel[(size_t)j * D + d], dv);
+    }
+    acc[(size_t)j * D + d] = an[d];
+  }
+  if (phi) phi[j] = a.w;
 }
 
 // Fixed-order sum of the gather's per-block energy partials: out[0] kinetic, out[1] potential.
@@ -2004,7 +2036,7 @@ __global__ void __launch_bounds__(256) fft_rows_multi(const RowsPack *__restrict
   fft_rows_kernel_body(q.data, q.nrows, q.RB, q.L, q.fdL, q.twmul, q.Lt, q.tw, q.inverse, (int)blockIdx.x - boff[s]);
 }
 template <int TY>
-__global__ void __launch_bounds__(512) green_multi(const GreenPack *__restrict__ pk, const int *__restrict__ boff,
+__global__ void __launch_bounds__(green_threads<TY>(), 1024 / green_threads<TY>()) green_multi(const GreenPack *__restrict__ pk, const int *__restrict__ boff,
                                                    int ns) {
   const int s = scene_of(boff, ns, blockIdx.x);
   const GreenPack &q = pk[s];

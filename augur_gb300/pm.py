@@ -253,6 +253,22 @@ class PMPlan:
         self._call("augur_pm_step", pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), mass.data_ptr(),
                    mask.data_ptr(), n, float(dt), int(bool(have_acc)))
 
+    def step_host(self, pos, vel, acc, mass=None, mask=None, dt: float = 1e-3, have_acc: bool = True) -> None:
+        """``step`` on host tensors: pos, vel, acc are (N, D) float32 CPU tensors (pinned for the
+        copies to overlap the kernels), updated in place once the plan's stream has finished;
+        mass and mask are device tensors. Same results as ``step`` on device copies."""
+        for t, name in ((pos, "pos"), (vel, "vel"), (acc, "acc")):
+            if not isinstance(t, torch.Tensor) or t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous():
+                raise ValueError(f"{name} must be a contiguous float32 CPU tensor")
+            if t.dim() != 2 or t.shape[1] != self.dim or t.shape != pos.shape:
+                raise ValueError(f"{name} must be (N, {self.dim}) like pos, got {tuple(t.shape)}")
+        n = pos.shape[0]
+        if n > self.max_bodies:
+            raise ValueError(f"{n} bodies exceed the plan's max_bodies={self.max_bodies}")
+        mass, mask = self._mm(n, mass, mask)
+        self._call("augur_pm_step_host", pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), mass.data_ptr(),
+                   mask.data_ptr(), n, float(dt), int(bool(have_acc)))
+
     def run(self, pos, vel, mass=None, mask=None, dt: float = 1e-3, nsteps: int = 1, want_acc: bool = False):
         """nsteps merged kick-drift-kick steps in place on the sorted device state."""
         n = self._n(pos)

@@ -205,6 +205,23 @@ int augur_pm_step(augur_pm_plan *plan, float *pos, float *vel, float *acc,
                   int have_acc, void *stream);
 
 /*
+ * augur_pm_step on the caller's HOST arrays: pos, vel, acc (N, D) in host memory (page-locked,
+ * e.g. cudaHostAlloc, for the copies to run asynchronously and overlap; pageable memory works but
+ * each copy then blocks), updated in place when the stream reaches the end of the call; mass and
+ * mask (N,) are device pointers. Same results as copying the arrays to the device, calling
+ * augur_pm_step and copying them back. With have_acc set, the bodies move in chunks: a chunk's
+ * drift and row keys start as soon as its copy has landed, the drifted positions go back while
+ * the grid is solved, and the kicked velocities and new accelerations go back chunk by chunk
+ * (two internal copy streams ordered against `stream` by events; the call's work, copies
+ * included, is complete when `stream` reaches its end). The plan keeps 3 N D floats of device
+ * staging from the first call. Replaces the host round trip around ScatterField._step
+ * (scripts/scatter_field.py:677-688) with its arrays on the host.
+ */
+int augur_pm_step_host(augur_pm_plan *plan, float *pos, float *vel, float *acc,
+                       const float *mass, const float *mask, int64_t n, float dt,
+                       int have_acc, void *stream);
+
+/*
  * nsteps leapfrog steps (kick-drift-kick, merged between steps as in Sim.tick,
  * scripts/scatter_bh_1b.py:123-146) with the body state kept sorted by grid row on the
  * device between steps; one force evaluation per step plus one at the start. The
