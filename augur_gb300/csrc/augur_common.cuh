@@ -88,6 +88,23 @@ __device__ __forceinline__ bool cic_axis(float x, float half_ext, float h, int &
   return true;
 }
 
+// cic_axis with the division resolved at compile time: POW2 when h is a power of two (then
+// t * (1/h) == t / h exactly), for loops that take the branch once outside
+template <bool POW2>
+__device__ __forceinline__ bool cic_axis_t(float x, float half_ext, float h, float inv_h, int &i0, float &w) {
+  const float t = __fadd_rn(x, half_ext);
+  const float u = __fsub_rn(POW2 ? __fmul_rn(t, inv_h) : __fdiv_rn(t, h), 0.5f);
+  if (!(fabsf(u) < 1.0e9f)) {
+    i0 = 0;
+    w = 0.f;
+    return false;
+  }
+  const float f = floorf(u);
+  i0 = (int)f;
+  w = __fsub_rn(u, f);
+  return true;
+}
+
 __device__ __forceinline__ int wrap_idx(int i, int G) {
   int r = i % G;
   return r < 0 ? r + G : r;

@@ -10,6 +10,7 @@
 //   force grid         F4[cell] = (a_x, a_y, a_z, phi) float4, so the gather is one 128-bit
 //                      load per CIC corner
 #pragma once
+#include <type_traits>
 
 #include "augur_common.cuh"
 #include "tcgen05.cuh"
@@ -490,18 +491,29 @@ __device__ __forceinline__ void deposit_r2c_post(const float2 *Z, int MS, int M,
                                                  const DepositArgs &a, const float2 *tw, float2 *__restrict__ spec_out) {
   const int tstep = a.Lt / G;
   const size_t plane = (size_t)(D == 3 ? G : 1) * G;  // rows per kx plane
-  for (int e = threadIdx.x; e < (M + 1) * RR; e += blockDim.x) {
-    int kx = (int)fdiv(e, a.fdRR), rr = e - kx * RR;
+  auto post = [&](int kx, int rr) -> float2 {
     float2 zk = Z[rr * MS + (kx == M ? 0 : kx)];
     float2 zc = cconj(Z[rr * MS + (kx == 0 ? 0 : M - kx)]);
     float2 ev = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
     float2 od = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y - zc.y));
     float2 w = tw[kx * tstep];
     float2 t = cmul(w, od);
-    float2 X = make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
-    int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
-    size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
-    spec_out[(size_t)kx * plane + row] = X;
+    return make_float2(ev.x + t.y, ev.y - t.x);  // ev - i*t
+  };
+  auto row_of = [&](int rr) -> size_t {
+    const int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
+    return (size_t)(z0 + zz) * G + (y0 + yy);
+  };
+  const int nt = blockDim.x;
+  if (nt % RR == 0) {  // each thread keeps one row: kx = tid / RR, + nt / RR, ...
+    const int rr = threadIdx.x % RR;
+    float2 *dst = spec_out + row_of(rr);
+    for (int kx = threadIdx.x / RR; kx <= M; kx += nt / RR) dst[(size_t)kx * plane] = post(kx, rr);
+  } else {
+    for (int e = threadIdx.x; e < (M + 1) * RR; e += nt) {
+      const int kx = (int)fdiv(e, a.fdRR), rr = e - kx * RR;
+      spec_out[(size_t)kx * plane + row_of(rr)] = post(kx, rr);
+    }
   }
 }
 
@@ -574,6 +586,10 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
 
   // One segment at a time: a segment is one base z row (one key range of sorted bodies), so
   // which z corners of its bodies fall inside the block is the same for the whole segment.
+  // (the body loop is compiled twice, with the cell-index division resolved either way; the
+  // choice made per body inside the loop cost 5 us at 3M bodies, 32-bit indices another 2-3 us)
+  auto segments = [&](auto pow2) {
+  constexpr bool POW2 = decltype(pow2)::value;
   for (int sg = 0; sg < nseg; ++sg) {
     const long long s0 = max(f_lo, s_pre[sg]), s1 = min(f_hi, s_pre[sg + 1]);
     if (s0 >= s1) continue;
@@ -592,15 +608,19 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
         zin[oz] = lz < RZ;
       }
     }
-    for (long long f0 = s0 + (long long)warp * 32; f0 < s1; f0 += (long long)nwarp * 32) {
-      const long long f = f0 + lane;
-      const bool valid = f < s1;
+    // body indices are below 2^31 (32-bit loop arithmetic)
+    const int s1i = (int)s1;
+    const float4 *pb = pos4 + bias;
+    for (int f0 = (int)s0 + warp * 32; f0 < s1i; f0 += nwarp * 32) {
+      const int f = f0 + lane;
+      const bool valid = f < s1i;
       float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (valid) p = pos4[bias + f];
+      if (valid) p = pb[f];
       int ix = 0, iy = 0, iz = 0;
       float wx = 0.f, wy = 0.f, wz = 0.f;
-      bool ok = cic_axis(p.x, g.half_ext, g.h, ix, wx, g.inv_h) & cic_axis(p.y, g.half_ext, g.h, iy, wy, g.inv_h);
-      if (D == 3) ok &= cic_axis(p.z, g.half_ext, g.h, iz, wz, g.inv_h);
+      bool ok = cic_axis_t<POW2>(p.x, g.half_ext, g.h, g.inv_h, ix, wx) &
+                cic_axis_t<POW2>(p.y, g.half_ext, g.h, g.inv_h, iy, wy);
+      if (D == 3) ok &= cic_axis_t<POW2>(p.z, g.half_ext, g.h, g.inv_h, iz, wz);
       if (valid && !ok) set_err(err, AUGUR_ERRBIT_NONFINITE);
       const bool live = valid && ok && p.w > 0.f;
       // x corners: cells bx and bx1 of a row (periodic wrap or grid bounds)
@@ -687,6 +707,10 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
       }
     }
   }
+  };
+  if (g.inv_h != 0.f) segments(std::true_type{});
+  else segments(std::false_type{});
+
   __syncthreads();
 
   unsigned long long *gtile = nullptr;
