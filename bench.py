@@ -539,7 +539,7 @@ def run_batch(args, world, rank, local):
     branch_ms = timed(lambda: simb.steps(K)) / K
     simb.end()
     simb.close()
-    # plain PM, one launch per stage for all scenes (the headline form)
+    # plain PM, one launch per stage for all scenes
     sim = BatchedPM(batch, dt=args.dt, fused=True)
     sim.begin()
     launches_per_step = 11
