@@ -332,8 +332,10 @@ int launch_c2r(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   ca.fdRB = make_fastdiv(ca.RB);
   ca.fdM = make_fastdiv(ca.L / 2);
   ca.fdL = make_fastdiv(ca.L);
-  c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, p->smem_c2r, st>>>(p->spec3, ca, p->tw,
-                                                                                 reinterpret_cast<float *>(F4));
+  ca.nbx = c2r_smem_bytes(M, ca.RB, G, ncomp, 2, p->Lt) <= p->smem_c2r ? 2 : 1;
+  const size_t smem = c2r_smem_bytes(M, ca.RB, G, ncomp, ca.nbx, p->Lt);
+  c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, smem, st>>>(p->spec3, ca, p->tw,
+                                                                          reinterpret_cast<float *>(F4));
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -541,8 +543,11 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   const size_t PM = (size_t)fft_row_stride(M), PL = (size_t)fft_row_stride(L);
   const size_t s_dep = (size_t)RY * RZ * (2 * PM * 8 + (size_t)(G + 2) * 4) + (size_t)Lt * 8;
   const size_t s_green = (size_t)(1 + green_nbuf(G)) * G * t->green_tile_y * 8 + (size_t)Lt * 8;
-  const size_t s_c2r = ((size_t)c2r_x_elems(M, RB) + (size_t)RB * PM) * 8 + (size_t)(p->gp.periodic ? 4 : 1) * RB * L * 4 +
-                       (size_t)Lt * 8;
+  // periodic: four result planes with one input block (force + potential), and, where it fits,
+  // three with two (force only, the next component copied in during a transform)
+  size_t s_c2r = c2r_smem_bytes(M, RB, L, p->gp.periodic ? 4 : 1, 1, Lt);
+  if (p->gp.periodic && c2r_smem_bytes(M, RB, L, 3, 2, Lt) <= p->smem_max)
+    s_c2r = std::max(s_c2r, c2r_smem_bytes(M, RB, L, 3, 2, Lt));
   const size_t s_rows = (size_t)2 * t->fft_rows * PL * 8 + (size_t)Lt * 8;
   const size_t s_r2c = (size_t)16 * ((M + 1) + 2 * PM) * 8 + (size_t)Lt * 8;
   const size_t lim = p->smem_max;
@@ -1526,6 +1531,7 @@ int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int
     ca.fdRB = make_fastdiv(ca.RB);
     ca.fdM = make_fastdiv(ca.L / 2);
     ca.fdL = make_fastdiv(ca.L);
+    ca.nbx = c2r_smem_bytes(M, ca.RB, G, 3, 2, p->Lt) <= p->smem_c2r ? 2 : 1;
     c2r[i] = {p->spec3, ca, p->tw, reinterpret_cast<float *>(p->F4)};
     const GatherArgs ga2 = gather_args(p, p->run_dt, p->run_dt, 1);
     for (int par = 0; par < 2; ++par) {

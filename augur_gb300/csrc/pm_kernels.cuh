@@ -1534,14 +1534,18 @@ __global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict_
 // of every component. OUT4: writes F4[r][x] = (c0, c1, c2, c3 or 0) for x < L.
 // Otherwise writes component 0 as real rows out[r][x] for r < nkeep, x < Lkeep (times scale).
 // ---------------------------------------------------------------------------------
-constexpr int C2R_LU = 5;  // C2R input loads per thread in flight
 // The C2R input block X is stored [kx][row] with RB + 2 float2 per kx (consecutive rows of one kx
-// land on consecutive banks for the loads, and the first stage's reads of X_k and X_{M-k} by
+// land on consecutive banks for the copies, and the first stage's reads of X_k and X_{M-k} by
 // (row, butterfly) lanes spread over the banks); for transforms of three or more stages X is also
 // the second scratch buffer, rows of fft_row_stride(M).
 __host__ __device__ inline int c2r_x_elems(int M, int RB) {
   const int a = (M + 1) * (RB + 2), b = RB * fft_row_stride(M);
   return a > b ? a : b;
+}
+// Shared memory of c2r_rows_kernel: nbx input blocks, the scratch rows, nres result planes, twiddles.
+__host__ __device__ inline size_t c2r_smem_bytes(int M, int RB, int L, int nres, int nbx, int Lt) {
+  return ((size_t)nbx * c2r_x_elems(M, RB) + (size_t)RB * fft_row_stride(M)) * 8 + (size_t)nres * RB * L * 4 +
+         (size_t)Lt * 8;
 }
 struct C2RArgs {
   int L, nrows, RB, ncomp, Lt;
@@ -1551,6 +1555,7 @@ struct C2RArgs {
   int twmul;
   FastDiv fdRB, fdM, fdL;
   int ext;  // single component: keep rows/columns 0..Lkeep and L-1 into a (Lkeep+2)^2 array, index +1 (L-1 -> 0)
+  int nbx;  // input blocks: 2 = the next component is copied in while this one is transformed (0 or 1: one)
 };
 
 template <bool OUT4>
@@ -1560,49 +1565,53 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
   const int L = a.L, M = L / 2, RB = a.RB;
   const int MS = fft_row_stride(M);  // scratch row stride
   const int XP = RB + 2;             // X[kx * XP + row]
+  const int XE = c2r_x_elems(M, RB);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = bx * RB;
-  float2 *X = reinterpret_cast<float2 *>(smem);
-  float2 *Y = X + c2r_x_elems(M, RB);
-  float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [ncomp][RB][L]
-  float2 *tw = reinterpret_cast<float2 *>(res + (size_t)(OUT4 ? 4 : 1) * RB * L);
+  const int nc = OUT4 ? a.ncomp : 1;
+  const int nbx = (a.nbx == 2 && nc > 1) ? 2 : 1;
+  float2 *X0 = reinterpret_cast<float2 *>(smem);
+  float2 *Y = X0 + (size_t)nbx * XE;
+  float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [nc][RB][L]
+  float2 *tw = reinterpret_cast<float2 *>(res + (size_t)nc * RB * L);
   for (int e = tid; e < a.Lt; e += nt) tw[e] = twg[e];
   const size_t cstride = (size_t)(M + 1) * a.nrows;
   const int tstep = a.Lt / L;
-  const int nc = OUT4 ? a.ncomp : 1;
-  for (int c = 0; c < nc; ++c) {
+  auto xbuf = [&](int c) { return X0 + (size_t)(nbx == 2 ? (c & 1) : 0) * XE; };
+  // component c into its input block by asynchronous 8-byte copies (rows past nrows read as zero);
+  // the reads, 128-byte row pieces spread over M + 1 kx planes, are latency-bound, so with two
+  // blocks the next component's copies run during this one's transform
+  auto issue = [&](int c) {
     const float2 *src = in + c * cstride;
-    // C2R_LU loads per thread in flight before any is stored (the loads, 128-byte row pieces
-    // spread over M + 1 kx planes, are latency-bound one at a time)
-    for (int e0 = tid; e0 < (M + 1) * RB; e0 += nt * C2R_LU) {
-      float2 v[C2R_LU];
-#pragma unroll
-      for (int u = 0; u < C2R_LU; ++u) {
-        const int e = e0 + u * nt;
-        v[u] = make_float2(0.f, 0.f);
-        if (e < (M + 1) * RB) {
-          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
-          if (r0 + rr < a.nrows) v[u] = __ldcs(&src[(size_t)kx * a.nrows + r0 + rr]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < C2R_LU; ++u) {
-        const int e = e0 + u * nt;
-        if (e < (M + 1) * RB) {
-          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
-          float2 w = v[u];
-          if (kx == 0 || kx == M) w.y = 0.f;  // imaginary part of DC and Nyquist is ignored
-          X[kx * XP + rr] = w;
-        }
-      }
+    float2 *Xb = xbuf(c);
+    for (int e = tid; e < (M + 1) * RB; e += nt) {
+      const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
+      const bool inr = r0 + rr < a.nrows;
+      cp_async8(smem_u32(&Xb[kx * XP + rr]), inr ? &src[(size_t)kx * a.nrows + r0 + rr] : src, inr ? 8u : 0u);
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  for (int c = 0; c < nc; ++c) {
+    if (nbx == 2 && c + 1 < nc) {
+      issue(c + 1);  // its block was last read by the transform of component c - 1
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
+    const float2 *X = xbuf(c);
     // inverse transform whose first stage computes the pre-process on load:
     // E_k = X_k + conj X_{M-k} ; O_k = (X_k - conj X_{M-k}) W^{-k} ; Z_k = E_k + i O_k
+    // (the imaginary parts of X_0 and X_M, DC and Nyquist, are ignored)
     float *dst = res + (size_t)c * RB * L;
     auto ld = [&](int b, int k) -> float2 {
       float2 xk = X[k * XP + b];
       float2 xc = cconj(X[(M - k) * XP + b]);
+      if (k == 0) {
+        xk.y = 0.f;
+        xc.y = 0.f;
+      }
       float2 E = cadd(xk, xc);
       float2 O = cmul(csub(xk, xc), cconj(tw[k * tstep]));
       return make_float2(E.x - O.y, E.y + O.x);
@@ -1610,7 +1619,9 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
     auto st = [&](int b, int k, float2 v) {
       *reinterpret_cast<float2 *>(&dst[b * L + 2 * k]) = make_float2(v.x * a.scale, v.y * a.scale);
     };
-    AUGUR_FFT_IO(M, 0, RB, ld, st, X, Y, MS, tw, a.twmul, true);
+    // (three-stage lengths use the input block as their second scratch buffer)
+    AUGUR_FFT_IO(M, 0, RB, ld, st, const_cast<float2 *>(X), Y, MS, tw, a.twmul, true);
+    if (nbx == 1 && c + 1 < nc) issue(c + 1);
   }
   if (OUT4) {
     float4 *o4 = reinterpret_cast<float4 *>(out);

@@ -29,6 +29,14 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;
 }
 
+// ---- asynchronous global -> shared copies of 8 bytes (zero-filled past src_bytes) ------------
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // ---- instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both operands K-major ----
 // bits 4-5 D format (1 = F32); 7-9 A format (1 = BF16); 10-12 B format (1 = BF16);
 // 15/16 A/B major (0 = K); 17-22 N >> 3; 24-28 M >> 4.
