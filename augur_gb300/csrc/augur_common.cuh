@@ -105,6 +105,30 @@ __device__ __forceinline__ bool cic_axis_t(float x, float half_ext, float h, flo
   return true;
 }
 
+// GELU x Phi(x) with erfc from Abramowitz & Stegun, Handbook of Mathematical Functions, eq. 7.1.26
+// (|erf error| <= 1.5e-7): erfc(z) ~ t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-z^2),
+// t = 1 / (1 + p z), z = |x| / sqrt 2 >= 0, and 2 - erfc(z) for the other sign, so negative inputs
+// keep their relative accuracy. About half the instructions of the erff form.
+__device__ __forceinline__ float as_erfc_exp(float x, float &ez2) {
+  const float z = fabsf(x) * 0.70710678118654752440f;
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+  const float poly =
+      t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
+  ez2 = __expf(-z * z);  // exp(-x^2 / 2)
+  return poly * ez2;      // erfc(|x| / sqrt 2)
+}
+__device__ __forceinline__ float gelu_as(float x) {
+  float e;
+  const float ec = as_erfc_exp(x, e);
+  return 0.5f * x * (x >= 0.f ? 2.0f - ec : ec);
+}
+// d/dx [x Phi(x)] = Phi(x) + x phi(x), phi(x) = exp(-x^2/2) / sqrt(2 pi) (the same exponential)
+__device__ __forceinline__ float gelu_grad_as(float x) {
+  float e;
+  const float ec = as_erfc_exp(x, e);
+  return 0.5f * (x >= 0.f ? 2.0f - ec : ec) + x * (0.39894228040143267794f * e);
+}
+
 __device__ __forceinline__ int wrap_idx(int i, int G) {
   int r = i % G;
   return r < 0 ? r + G : r;

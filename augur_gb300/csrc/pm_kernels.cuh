@@ -1072,17 +1072,8 @@ __global__ void pair_scatter_kernel(const float *__restrict__ pos, const uint32_
 }
 
 // GELU for the pair MLP, evaluated 128 times per pair: 0.5 x erfc(-x / sqrt 2) with erfc from
-// Abramowitz & Stegun, Handbook of Mathematical Functions, eq. 7.1.26 (|erf error| <= 1.5e-7):
-// erfc(z) ~ t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-z^2), t = 1 / (1 + p z), z >= 0, and
-// 2 - erfc(z) for the other sign, so negative inputs keep their relative accuracy.
-__device__ __forceinline__ float pair_gelu_as(float x) {
-  const float z = fabsf(x) * 0.70710678118654752440f;
-  const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
-  const float poly =
-      t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f), 0.254829592f);
-  const float ec = poly * __expf(-z * z);  // erfc(|x| / sqrt 2)
-  return 0.5f * x * (x >= 0.f ? 2.0f - ec : ec);
-}
+// the pair MLP's GELU: gelu_as (erfc after Abramowitz & Stegun 7.1.26, |erf error| <= 1.5e-7)
+__device__ __forceinline__ float pair_gelu_as(float x) { return gelu_as(x); }
 
 // lower bound of the distance from coordinate x to cell c's extent along one axis (edge cells
 // extend to infinity: they hold the clamped bodies)
