@@ -74,9 +74,7 @@ __device__ __forceinline__ void tma_load5(uint32_t dst, const CUtensorMap *map, 
 struct ConvArgs {
   int B, G;
   int xseg;          // ceil(G / 128)
-  int yc;            // y rows per work unit
-  int nyc;           // ceil(G / yc)
-  int nunits;        // B * G * xseg * nyc
+  long long rows;    // B * G * xseg * G output rows (b, z, x segment, y), split evenly over the CTAs
   float out_scale;   // EPI_OUT: added field = out_scale * (acc + bias)
   uint32_t budget;   // tries of a pipeline wait before the CTA gives up (AUGUR_ERRBIT_TIMEOUT)
 };
@@ -84,20 +82,33 @@ struct ConvArgs {
 struct ConvUnit {
   int b, z, x0, ya, ny;
 };
-__device__ __forceinline__ ConvUnit conv_unit(const ConvArgs &a, int unit) {
-  ConvUnit u;
-  int t = unit;
-  const int yc = t % a.nyc;
-  t /= a.nyc;
+// Work of a CTA: one contiguous range of the flattened output rows (b, z, x segment, y), cut into
+// pieces at column ends (a piece is a ConvUnit: consecutive y rows of one (b, z, x segment)).
+// Equal ranges keep every SM busy to the end: dealing fixed 32-row units to 152 CTAs gave the
+// slowest ones 4 units (136 input rows with halos) against 115 on average at 128^3.
+__device__ __forceinline__ long long cta_rows_begin(const ConvArgs &a) {
+  return a.rows * (long long)blockIdx.x / gridDim.x;
+}
+__device__ __forceinline__ long long cta_rows_end(const ConvArgs &a) {
+  return a.rows * (long long)(blockIdx.x + 1) / gridDim.x;
+}
+__device__ __forceinline__ bool next_piece(const ConvArgs &a, long long &f, long long end, ConvUnit &u) {
+  if (f >= end) return false;
+  const long long col = f / a.G;
+  const int y = (int)(f - col * a.G);
+  const int ny = (int)min((long long)(a.G - y), end - f);
+  int t = (int)col;
   const int xs = t % a.xseg;
   t /= a.xseg;
   u.z = t % a.G;
   u.b = t / a.G;
   u.x0 = xs * CONV_M;
-  u.ya = yc * a.yc;
-  u.ny = min(a.G, u.ya + a.yc) - u.ya;
-  return u;
+  u.ya = y;
+  u.ny = ny;
+  f += ny;
+  return true;
 }
+
 
 // ---------------------------------------------------------------------------------------
 // tcgen05 implicit-GEMM 3x3x3 conv. CIN in {16, 32}, N (output channels) in {16, 32}.
@@ -116,8 +127,9 @@ __device__ __forceinline__ ConvUnit conv_unit(const ConvArgs &a, int unit) {
 // Accumulators start from zero and every MMA accumulates: the epilogue zeroes a slot after
 // reading it.
 //
-// Work unit = (batch, z, x segment, chunk of yc consecutive y rows); the CTA takes units
-// blockIdx.x, + gridDim.x, ... Warp-specialised pipeline, no block barrier per row:
+// Work: each CTA takes one contiguous range of the output rows (batch, z, x segment, y), in pieces
+// of consecutive y rows of one (batch, z, x segment). Warp-specialised pipeline, no block barrier
+// per row:
 //   TMA warp   loads input row y' of planes z-1, z, z+1 (one 8-channel x 130-voxel box per
 //              channel block; the tensor map zero-fills outside the grid) into a ring of RING
 //              slots, arming full[slot] with the byte count;
@@ -219,8 +231,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
     uint32_t k = 0;
     if (lane == 0) {
       bool go = true;
-      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-        const ConvUnit u = conv_unit(a, unit);
+      long long fpos = cta_rows_begin(a);
+      const long long fend = cta_rows_end(a);
+      ConvUnit u;
+      while (go && next_piece(a, fpos, fend, u)) {
         for (int j = 0; j < u.ny + 2; ++j, ++k) {
           const uint32_t slot = k % RING, n = k / RING;
           if (n > 0 && !wait(&empty[slot], (n - 1) & 1u)) {
@@ -249,8 +263,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
       const uint32_t w0 = smem_u32(sW);
       uint32_t k0 = 0, T0 = 0;
       bool go = true;
-      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-        const ConvUnit u = conv_unit(a, unit);
+      long long fpos = cta_rows_begin(a);
+      const long long fend = cta_rows_end(a);
+      ConvUnit u;
+      while (go && next_piece(a, fpos, fend, u)) {
         for (int j = 0; j < u.ny + 2 && go; ++j) {
           const uint32_t kr = k0 + j;
           if (!wait(&full[kr % RING], (kr / RING) & 1u)) {
@@ -304,8 +320,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
     const bool active = !(EPI == EPI_OUT && half == 1);  // three output channels: first half only
     uint32_t T = 0;
     bool go = true;
-    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-      const ConvUnit u = conv_unit(a, unit);
+    long long fpos = cta_rows_begin(a);
+    const long long fend = cta_rows_end(a);
+    ConvUnit u;
+    while (go && next_piece(a, fpos, fend, u)) {
       const size_t bbase = (size_t)u.b * G * G * G;
       for (int i = 0; i < u.ny; ++i, ++T) {
         const uint32_t sl = slot_of(T);
@@ -512,8 +530,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
     const uint32_t *x32 = reinterpret_cast<const uint32_t *>(x);  // two bf16 channels per voxel
     uint32_t t = 0;
     bool go = true;
-    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-      const ConvUnit u = conv_unit(a, unit);
+    long long fpos = cta_rows_begin(a);
+    const long long fend = cta_rows_end(a);
+    ConvUnit u;
+    while (go && next_piece(a, fpos, fend, u)) {
       const size_t bbase = (size_t)u.b * G * G * G;
       const int xx = u.x0 + r;
       for (int i = 0; i < u.ny; ++i, ++t) {
@@ -546,8 +566,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
       const uint64_t b_desc0 = smem_desc(smem_u32(sW), N * 16, 128);
       uint32_t t = 0;
       bool go = true;
-      for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-        const ConvUnit u = conv_unit(a, unit);
+      long long fpos = cta_rows_begin(a);
+      const long long fend = cta_rows_end(a);
+      ConvUnit u;
+      while (go && next_piece(a, fpos, fend, u)) {
         for (int i = 0; i < u.ny; ++i, ++t) {
           const uint32_t st = t % IN_STAGES, acc = t % NACC;
           if (!wait(&full[st], (t / IN_STAGES) & 1u)) go = false;
@@ -574,8 +596,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
     const int c0 = half * NC;
     uint32_t t = 0;
     bool go = true;
-    for (int unit = blockIdx.x; unit < a.nunits && go; unit += gridDim.x) {
-      const ConvUnit u = conv_unit(a, unit);
+    long long fpos = cta_rows_begin(a);
+    const long long fend = cta_rows_end(a);
+    ConvUnit u;
+    while (go && next_piece(a, fpos, fend, u)) {
       const size_t bbase = (size_t)u.b * G * G * G;
       for (int i = 0; i < u.ny; ++i, ++t) {
         const uint32_t acc = t % NACC;
@@ -1140,13 +1164,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   a.G = G;
   a.xseg = (G + CONV_M - 1) / CONV_M;
   const int nsm = current_sm_count();
-  // y chunk: long enough to amortise the two halo rows, short enough to fill every SM
-  const int columns = B * G * a.xseg;
-  int yc = G;
-  while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
-  a.yc = yc;
-  a.nyc = (G + yc - 1) / yc;
-  a.nunits = columns * a.nyc;
+  a.rows = (long long)B * G * a.xseg * G;
   a.out_scale = out_scale;
   a.budget = g_wait_budget.load();
   // input activations [B][G][G][G][CIN] bf16 as a 5D tensor (c, x, y, z, b); box = 8 channels x
@@ -1156,7 +1174,7 @@ int launch_conv_tc(const void *in, const void *wB, const float *bias, const void
   constexpr int WBYTES = 27 * CIN * N * 2;
   const size_t smem = ((WBYTES + 127) / 128) * 128 + (size_t)RING * 3 * (CIN / 8) * SLAB_ROWS * 16;
   if (raise_dyn_smem((const void *)conv_tc_kernel<CIN, N, EPI>, smem)) return AUGUR_ECUDA;
-  const int grid = std::min(a.nunits, nsm);
+  const int grid = (int)std::min<long long>(a.rows, nsm);
   conv_tc_kernel<CIN, N, EPI><<<grid, CONV_THREADS, smem, st>>>(map, (const bf16 *)wB, bias, resid,
                                                                 (const bf16 *)zprev, out0, (bf16 *)out1, a, err, stats);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;
@@ -1169,17 +1187,12 @@ int launch_conv_in_tc(const void *x, const void *wB, const float *bias, void *z0
   a.G = G;
   a.xseg = (G + CONV_M - 1) / CONV_M;
   const int nsm = current_sm_count();
-  const int columns = B * G * a.xseg;
-  int yc = G;
-  while (yc > 8 && (long long)columns * ((G + yc - 1) / yc) < 3LL * nsm) yc = (yc + 1) / 2;
-  a.yc = yc;
-  a.nyc = (G + yc - 1) / yc;
-  a.nunits = columns * a.nyc;
+  a.rows = (long long)B * G * a.xseg * G;
   a.out_scale = 1.f;
   a.budget = g_wait_budget.load();
   const size_t smem = (size_t)IN_KB * 32 * 16 + (size_t)IN_STAGES * IN_ABYTES;
   if (raise_dyn_smem((const void *)conv_in_tc_kernel, smem)) return AUGUR_ECUDA;
-  const int grid = std::min(a.nunits, nsm);
+  const int grid = (int)std::min<long long>(a.rows, nsm);
   conv_in_tc_kernel<<<grid, IN_THREADS, smem, st>>>((const bf16 *)x, (const bf16 *)wB, bias, (bf16 *)z0, (bf16 *)h0,
                                                     a, err);
   return cudaGetLastError() == cudaSuccess ? AUGUR_OK : AUGUR_ECUDA;

@@ -332,7 +332,7 @@ int launch_c2r(augur_pm_plan *p, int ncomp, float4 *F4, cudaStream_t st) {
   ca.fdRB = make_fastdiv(ca.RB);
   ca.fdM = make_fastdiv(ca.L / 2);
   ca.fdL = make_fastdiv(ca.L);
-  ca.nbx = c2r_smem_bytes(M, ca.RB, G, ncomp, 2, p->Lt) <= p->smem_c2r ? 2 : 1;
+  ca.nbx = (M <= 128 && c2r_smem_bytes(M, ca.RB, G, ncomp, 2, p->Lt) <= p->smem_c2r) ? 2 : 1;
   const size_t smem = c2r_smem_bytes(M, ca.RB, G, ncomp, ca.nbx, p->Lt);
   c2r_rows_kernel<true><<<(unsigned)(G * G / p->c2r_RB), 512, smem, st>>>(p->spec3, ca, p->tw,
                                                                           reinterpret_cast<float *>(F4));
@@ -353,9 +353,9 @@ int launch_green(augur_pm_plan *p, int ncomp, cudaStream_t st) {
   ga.kfund = (float)(2.0 * M_PI / p->extent);
   ga.gfac = (float)(-4.0 * M_PI * p->gnewton / ((double)G * G * G));
   if (p->green_TY == 16)
-    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), green_threads<16>(), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+    fft_z_green_kernel<16><<<(unsigned)((M + 1) * (G / 16)), green_threads(G, 16), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
   else
-    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), green_threads<8>(), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
+    fft_z_green_kernel<8><<<(unsigned)((M + 1) * (G / 8)), green_threads(G, 8), p->smem_green, st>>>(p->spec, ga, p->tw, p->spec3);
   AUGUR_LAUNCH_CHECK(p);
   return AUGUR_OK;
 }
@@ -546,7 +546,7 @@ int apply_tiles(augur_pm_plan *p, const augur_pm_tiles *t, bool check_only) {
   // periodic: four result planes with one input block (force + potential), and, where it fits,
   // three with two (force only, the next component copied in during a transform)
   size_t s_c2r = c2r_smem_bytes(M, RB, L, p->gp.periodic ? 4 : 1, 1, Lt);
-  if (p->gp.periodic && c2r_smem_bytes(M, RB, L, 3, 2, Lt) <= p->smem_max)
+  if (p->gp.periodic && M <= 128 && c2r_smem_bytes(M, RB, L, 3, 2, Lt) <= p->smem_max)
     s_c2r = std::max(s_c2r, c2r_smem_bytes(M, RB, L, 3, 2, Lt));
   const size_t s_rows = (size_t)2 * t->fft_rows * PL * 8 + (size_t)Lt * 8;
   const size_t s_r2c = (size_t)16 * ((M + 1) + 2 * PM) * 8 + (size_t)Lt * 8;
@@ -1398,6 +1398,7 @@ struct augur_pm_batch {
   std::vector<augur_pm_plan *> plans;
   int parity;  // steps taken mod 2: pack set in use
   int green_ty, agg;
+  int green_nt;  // threads of the z-transform launch (the largest any scene's grid wants)
   size_t smem_dep, smem_rows, smem_green, smem_c2r;
   int tot_scan, tot_scatter, tot_depcount, tot_dep, tot_rows_f, tot_rows_i, tot_green, tot_c2r, tot_gather;
   int *boff;  // device: 9 tables of ns + 1 block offsets, stage after stage
@@ -1460,6 +1461,7 @@ int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int
     }
     if (i == 0) {
       b->green_ty = p->green_TY;
+      b->green_nt = 0;
       b->agg = p->dep_agg;
     } else if (p->green_TY != b->green_ty || p->dep_agg != b->agg) {
       rc = AUGUR_EINVAL;  // one z-transform tile and one deposit variant per batch
@@ -1467,6 +1469,7 @@ int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int
     }
     const int G = p->G, M = p->M;
     const int64_t n = p->run_n;
+    b->green_nt = std::max(b->green_nt, green_threads(G, p->green_TY));
     int cnt[BS_N];
     cnt[BS_SCAN] = p->ntiles;
     cnt[BS_SCATTER] = (int)blocks_for(n, 256);
@@ -1531,7 +1534,7 @@ int augur_pm_batch_create(augur_pm_batch **out, augur_pm_plan *const *plans, int
     ca.fdRB = make_fastdiv(ca.RB);
     ca.fdM = make_fastdiv(ca.L / 2);
     ca.fdL = make_fastdiv(ca.L);
-    ca.nbx = c2r_smem_bytes(M, ca.RB, G, 3, 2, p->Lt) <= p->smem_c2r ? 2 : 1;
+    ca.nbx = (M <= 128 && c2r_smem_bytes(M, ca.RB, G, 3, 2, p->Lt) <= p->smem_c2r) ? 2 : 1;
     c2r[i] = {p->spec3, ca, p->tw, reinterpret_cast<float *>(p->F4)};
     const GatherArgs ga2 = gather_args(p, p->run_dt, p->run_dt, 1);
     for (int par = 0; par < 2; ++par) {
@@ -1612,9 +1615,9 @@ int augur_pm_batch_run_steps(augur_pm_batch *b, int k, void *stream) {
       deposit_multi<false><<<b->tot_dep, DEP_THREADS, b->smem_dep, st>>>(b->dep + (size_t)par * ns, off(BS_DEP), ns);
     fft_rows_multi<<<b->tot_rows_f, 256, b->smem_rows, st>>>(b->rows_f, off(BS_ROWS_F), ns);
     if (b->green_ty == 16)
-      green_multi<16><<<b->tot_green, green_threads<16>(), b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+      green_multi<16><<<b->tot_green, b->green_nt, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
     else
-      green_multi<8><<<b->tot_green, green_threads<8>(), b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
+      green_multi<8><<<b->tot_green, b->green_nt, b->smem_green, st>>>(b->green, off(BS_GREEN), ns);
     fft_rows_multi<<<b->tot_rows_i, 256, b->smem_rows, st>>>(b->rows_i, off(BS_ROWS_I), ns);
     c2r_multi<<<b->tot_c2r, 512, b->smem_c2r, st>>>(b->c2r, off(BS_C2R), ns);
     if (b->tot_gather)

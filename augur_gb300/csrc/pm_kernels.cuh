@@ -1502,13 +1502,16 @@ __device__ __forceinline__ void fft_z_green_kernel_body(const float2 *__restrict
   }
 }
 
-// 16 TY threads: one per (column, butterfly) of a radix-16 stage of a 256-point column
-// transform, so no thread idles through the stages (measured 101 -> 92 us at 256^3 against 512)
-template <int TY>
-constexpr int green_threads() { return 16 * TY; }
+// Threads of fft_z_green_kernel: one per (column, butterfly) of a radix-16 stage, at least 16 TY,
+// at most 512 (256 at G = 128 and 256: 101 -> 92 us at 256^3 against 512; 512 for longer columns,
+// whose stages have more butterflies: 8.0 ms at 1024^3 against 12.6 with 256)
+__host__ __device__ inline int green_threads(int G, int TY) {
+  const int t = TY * G / 16;
+  return t < 16 * TY ? 16 * TY : (t > 512 ? 512 : t);
+}
 
 template <int TY>
-__global__ void __launch_bounds__(green_threads<TY>(), 1024 / green_threads<TY>()) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
+__global__ void __launch_bounds__(512) fft_z_green_kernel(const float2 *__restrict__ spec, GreenArgs a,
                                                           const float2 *__restrict__ twg,
                                                           float2 *__restrict__ out) {
   fft_z_green_kernel_body<TY>(spec, a, twg, out, (int)blockIdx.x);
@@ -1525,10 +1528,13 @@ __global__ void kmul_kernel(float2 *__restrict__ spec, const float2 *__restrict_
 // of every component. OUT4: writes F4[r][x] = (c0, c1, c2, c3 or 0) for x < L.
 // Otherwise writes component 0 as real rows out[r][x] for r < nkeep, x < Lkeep (times scale).
 // ---------------------------------------------------------------------------------
-// The C2R input block X is stored [kx][row] with RB + 2 float2 per kx (consecutive rows of one kx
-// land on consecutive banks for the copies, and the first stage's reads of X_k and X_{M-k} by
-// (row, butterfly) lanes spread over the banks); for transforms of three or more stages X is also
-// the second scratch buffer, rows of fft_row_stride(M).
+// The C2R input block X: for M <= 128 (a warp's first-stage lanes span several rows) stored
+// [kx][row] with RB + 2 float2 per kx, so consecutive rows of one kx land on consecutive banks for
+// the copies and the first stage's reads of X_k and X_{M-k} spread over the banks; for longer rows
+// (a warp within one row) stored [row][kx] with rows of fft_row_stride(M), loaded through
+// registers (the kx-major form with cp.async measured 17.3 ms at 1024^3 against 15.4). For
+// transforms of three or more stages X is also the second scratch buffer, rows of
+// fft_row_stride(M).
 __host__ __device__ inline int c2r_x_elems(int M, int RB) {
   const int a = (M + 1) * (RB + 2), b = RB * fft_row_stride(M);
   return a > b ? a : b;
@@ -1549,18 +1555,23 @@ struct C2RArgs {
   int nbx;  // input blocks: 2 = the next component is copied in while this one is transformed (0 or 1: one)
 };
 
-template <bool OUT4>
+// KXM (M <= 128): input block [kx][row], the next component copied in with cp.async during this
+// one's transform (two blocks when a.nbx == 2). Otherwise: rows [row][kx] loaded through
+// registers, C2R_LU loads per thread in flight, one block.
+constexpr int C2R_LU = 5;
+template <bool OUT4, bool KXM>
 __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ in, C2RArgs a,
                                                        const float2 *__restrict__ twg, float *__restrict__ out, const int bx) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int L = a.L, M = L / 2, RB = a.RB;
   const int MS = fft_row_stride(M);  // scratch row stride
-  const int XP = RB + 2;             // X[kx * XP + row]
+  const int XP = RB + 2;             // X[kx * XP + row] (KXM) or X[row * MS + kx]
+  auto xi = [&](int kx, int rr) { return KXM ? kx * XP + rr : rr * MS + kx; };
   const int XE = c2r_x_elems(M, RB);
   const int tid = threadIdx.x, nt = blockDim.x;
   const int r0 = bx * RB;
   const int nc = OUT4 ? a.ncomp : 1;
-  const int nbx = (a.nbx == 2 && nc > 1) ? 2 : 1;
+  const int nbx = (KXM && a.nbx == 2 && nc > 1) ? 2 : 1;
   float2 *X0 = reinterpret_cast<float2 *>(smem);
   float2 *Y = X0 + (size_t)nbx * XE;
   float *res = reinterpret_cast<float *>(Y + (size_t)RB * MS);  // [nc][RB][L]
@@ -1578,17 +1589,45 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
     for (int e = tid; e < (M + 1) * RB; e += nt) {
       const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
       const bool inr = r0 + rr < a.nrows;
-      cp_async8(smem_u32(&Xb[kx * XP + rr]), inr ? &src[(size_t)kx * a.nrows + r0 + rr] : src, inr ? 8u : 0u);
+      cp_async8(smem_u32(&Xb[xi(kx, rr)]), inr ? &src[(size_t)kx * a.nrows + r0 + rr] : src, inr ? 8u : 0u);
     }
     cp_async_commit();
   };
-  issue(0);
+  // component c through registers (C2R_LU loads per thread in flight before any is stored)
+  auto load_regs = [&](int c) {
+    const float2 *src = in + c * cstride;
+    for (int e0 = tid; e0 < (M + 1) * RB; e0 += nt * C2R_LU) {
+      float2 v[C2R_LU];
+#pragma unroll
+      for (int u = 0; u < C2R_LU; ++u) {
+        const int e = e0 + u * nt;
+        v[u] = make_float2(0.f, 0.f);
+        if (e < (M + 1) * RB) {
+          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
+          if (r0 + rr < a.nrows) v[u] = __ldcs(&src[(size_t)kx * a.nrows + r0 + rr]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < C2R_LU; ++u) {
+        const int e = e0 + u * nt;
+        if (e < (M + 1) * RB) {
+          const int kx = (int)fdiv(e, a.fdRB), rr = e - kx * RB;
+          X0[xi(kx, rr)] = v[u];
+        }
+      }
+    }
+  };
+  if (KXM) issue(0);
   for (int c = 0; c < nc; ++c) {
-    if (nbx == 2 && c + 1 < nc) {
-      issue(c + 1);  // its block was last read by the transform of component c - 1
-      cp_async_wait<1>();
+    if (KXM) {
+      if (nbx == 2 && c + 1 < nc) {
+        issue(c + 1);  // its block was last read by the transform of component c - 1
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
     } else {
-      cp_async_wait<0>();
+      load_regs(c);
     }
     __syncthreads();
     const float2 *X = xbuf(c);
@@ -1597,8 +1636,8 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
     // (the imaginary parts of X_0 and X_M, DC and Nyquist, are ignored)
     float *dst = res + (size_t)c * RB * L;
     auto ld = [&](int b, int k) -> float2 {
-      float2 xk = X[k * XP + b];
-      float2 xc = cconj(X[(M - k) * XP + b]);
+      float2 xk = X[xi(k, b)];
+      float2 xc = cconj(X[xi(M - k, b)]);
       if (k == 0) {
         xk.y = 0.f;
         xc.y = 0.f;
@@ -1612,7 +1651,7 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
     };
     // (three-stage lengths use the input block as their second scratch buffer)
     AUGUR_FFT_IO(M, 0, RB, ld, st, const_cast<float2 *>(X), Y, MS, tw, a.twmul, true);
-    if (nbx == 1 && c + 1 < nc) issue(c + 1);
+    if (KXM && nbx == 1 && c + 1 < nc) issue(c + 1);
   }
   if (OUT4) {
     float4 *o4 = reinterpret_cast<float4 *>(out);
@@ -1651,7 +1690,10 @@ __device__ __forceinline__ void c2r_rows_kernel_body(const float2 *__restrict__ 
 template <bool OUT4>
 __global__ void __launch_bounds__(512, 2) c2r_rows_kernel(const float2 *__restrict__ in, C2RArgs a,
                                                        const float2 *__restrict__ twg, float *__restrict__ out) {
-  c2r_rows_kernel_body<OUT4>(in, a, twg, out, (int)blockIdx.x);
+  if (a.L <= 256)
+    c2r_rows_kernel_body<OUT4, true>(in, a, twg, out, (int)blockIdx.x);
+  else
+    c2r_rows_kernel_body<OUT4, false>(in, a, twg, out, (int)blockIdx.x);
 }
 
 // 2D isolated: F4 grid from the potential by the reference's zero-padded central
@@ -2062,7 +2104,7 @@ __global__ void __launch_bounds__(256) fft_rows_multi(const RowsPack *__restrict
   fft_rows_kernel_body(q.data, q.nrows, q.RB, q.L, q.fdL, q.twmul, q.Lt, q.tw, q.inverse, (int)blockIdx.x - boff[s]);
 }
 template <int TY>
-__global__ void __launch_bounds__(green_threads<TY>(), 1024 / green_threads<TY>()) green_multi(const GreenPack *__restrict__ pk, const int *__restrict__ boff,
+__global__ void __launch_bounds__(512) green_multi(const GreenPack *__restrict__ pk, const int *__restrict__ boff,
                                                    int ns) {
   const int s = scene_of(boff, ns, blockIdx.x);
   const GreenPack &q = pk[s];
@@ -2072,7 +2114,10 @@ __global__ void __launch_bounds__(512, 2) c2r_multi(const C2RPack *__restrict__ 
                                                     int ns) {
   const int s = scene_of(boff, ns, blockIdx.x);
   const C2RPack &q = pk[s];
-  c2r_rows_kernel_body<true>(q.in, q.a, q.tw, q.out, (int)blockIdx.x - boff[s]);
+  if (q.a.L <= 256)
+    c2r_rows_kernel_body<true, true>(q.in, q.a, q.tw, q.out, (int)blockIdx.x - boff[s]);
+  else
+    c2r_rows_kernel_body<true, false>(q.in, q.a, q.tw, q.out, (int)blockIdx.x - boff[s]);
 }
 __global__ void __launch_bounds__(256) gather_multi(const GatherPack *__restrict__ pk, const int *__restrict__ boff,
                                                     int ns) {
