@@ -1,4 +1,4 @@
-"""Plain PM is the fallback and the judge: the monitor's revert logic on synthetic series (CPU)."""
+"""Plain PM is the fallback and the yardstick: the monitor's revert logic on synthetic series (CPU)."""
 import math
 
 from augur_gb300.learned import FallbackMonitor
