@@ -536,6 +536,10 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
     while (go && next_piece(a, fpos, fend, u)) {
       const size_t bbase = (size_t)u.b * G * G * G;
       const int xx = u.x0 + r;
+      // the three x neighbours' validity is fixed for the piece; the nine (dz, dy) rows' per row
+      bool xin[3];
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) xin[dx] = xx + dx - 1 >= 0 && xx + dx - 1 < G;
       for (int i = 0; i < u.ny; ++i, ++t) {
         if ((int)(t % IN_GROUPS) != grp) continue;
         const uint32_t st = t % IN_STAGES, n = t / IN_STAGES;
@@ -546,12 +550,14 @@ __global__ void __launch_bounds__(IN_THREADS, 1) conv_in_tc_kernel(const bf16 *_
         const int y = u.ya + i;
         uint32_t v[28];
 #pragma unroll
-        for (int tap = 0; tap < 28; ++tap) {
-          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-          const int zz = u.z + dz, yy = y + dy, xq = xx + dx;
-          const bool in = tap < 27 && zz >= 0 && zz < G && yy >= 0 && yy < G && xq >= 0 && xq < G;
-          v[tap] = in ? __ldg(x32 + bbase + ((size_t)zz * G + yy) * G + xq) : 0u;
+        for (int r9 = 0; r9 < 9; ++r9) {
+          const int zz = u.z + r9 / 3 - 1, yy = y + r9 % 3 - 1;
+          const bool rin = zz >= 0 && zz < G && yy >= 0 && yy < G;
+          const uint32_t *row = x32 + bbase + ((size_t)(rin ? zz : 0) * G + (rin ? yy : 0)) * G + xx - 1;
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx) v[r9 * 3 + dx] = (rin && xin[dx]) ? __ldg(row + dx) : 0u;
         }
+        v[27] = 0u;
         unsigned char *A = sA + (size_t)st * IN_ABYTES;
 #pragma unroll
         for (int kb = 0; kb < 7; ++kb)

@@ -19,9 +19,9 @@
 using namespace augur;
 
 // Chunks of caller bodies in the host-buffer step: the copies of one chunk overlap the kernels of
-// the chunks before it (3M bodies on GB300: 1.76 ms per step with 4 chunks, 1.84 with 8, 1.94 with
-// 16; each chunk's copies and launches carry a fixed cost).
-constexpr int HS_CHUNKS = 4;
+// the chunks before it (3M bodies on GB300: 1.69 ms per step with 2 chunks, 1.76 with 1 and with
+// 4, 1.84 with 8, 1.94 with 16; each chunk's copies and launches carry a fixed cost).
+constexpr int HS_CHUNKS = 2;
 
 struct augur_pm_plan {
   int dim, G, mode;

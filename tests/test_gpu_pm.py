@@ -244,10 +244,10 @@ def test_step_matches_reference_verlet_formula():
     assert O.rel_rms(st1[1][0].cpu().numpy(), a1) < TOL
 
 
-@pytest.mark.parametrize("n", [3, 100_003])
+@pytest.mark.parametrize("n", [1, 100_003])
 def test_step_host_equals_device_step(n):
     """augur_pm_step_host on pinned host arrays (chunked copies overlapping the kernels) gives the
-    same bits as augur_pm_step on device copies, over a first step and two more; n = 3 has fewer
+    same bits as augur_pm_step on device copies, over a first step and two more; n = 1 has fewer
     bodies than copy chunks."""
     G, dt = 32, 1e-3
     pos, vel, mass = scenes.make_scene("plummer", n, seed=5)
