@@ -929,14 +929,29 @@ int augur_pm_step_host(augur_pm_plan *p, float *pos, float *vel, float *acc, con
   cudaStream_t st = S(stream);
   const int D = p->dim;
   if (!p->hs_buf) {
-    if (cudaMalloc(&p->hs_buf, sizeof(float) * 3 * (size_t)p->max_n * D) != cudaSuccess) {
-      p->hs_buf = nullptr;
-      return AUGUR_ENOMEM;
+    // staging, streams and events are created together; on any failure whatever was created is
+    // released again, so the next call starts from scratch
+    float *buf = nullptr;
+    cudaStream_t sin = nullptr, sout = nullptr;
+    cudaEvent_t ev[3 * HS_CHUNKS + 2] = {};
+    bool ok = cudaMalloc(&buf, sizeof(float) * 3 * (size_t)p->max_n * D) == cudaSuccess;
+    const bool oom = !ok;
+    ok = ok && cudaStreamCreateWithFlags(&sin, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&sout, cudaStreamNonBlocking) == cudaSuccess;
+    for (cudaEvent_t &e : ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+      if (sout) cudaStreamDestroy(sout);
+      if (sin) cudaStreamDestroy(sin);
+      if (buf) cudaFree(buf);
+      cudaGetLastError();
+      return oom ? AUGUR_ENOMEM : AUGUR_ECUDA;
     }
-    bool ok = cudaStreamCreateWithFlags(&p->hs_in, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&p->hs_out, cudaStreamNonBlocking) == cudaSuccess;
-    for (cudaEvent_t &e : p->hs_ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
-    if (!ok) return AUGUR_ECUDA;
+    p->hs_buf = buf;
+    p->hs_in = sin;
+    p->hs_out = sout;
+    for (int i = 0; i < 3 * HS_CHUNKS + 2; ++i) p->hs_ev[i] = ev[i];
     p->bytes += sizeof(float) * 3 * (size_t)p->max_n * D;
   }
   float *dpos = p->hs_buf, *dvel = dpos + (size_t)p->max_n * D, *dacc = dvel + (size_t)p->max_n * D;
