@@ -141,11 +141,12 @@ __device__ __forceinline__ bool next_piece(const ConvArgs &a, long long &f, long
 // Every wait is bounded: a stall sets the CTA's abort flag, the roles leave their loops,
 // and bit AUGUR_ERRBIT_TIMEOUT is raised in *err.
 // ---------------------------------------------------------------------------------------
-// output-row accumulator slots in TMEM: 16 x 32 columns fill the SM's 512 (the kernel runs one CTA
-// per SM). The deeper ring lets the MMAs run further ahead of the epilogue and halves the ring wraps
-// that split an input row's MMAs (32 -> 32 at 128^3: 193 us with 8 slots, 184.5 with 16; a probe
-// without the MMA warp's waits ran 169).
-constexpr int RACC = 16;
+// output-row accumulator slots in TMEM: 512 / N, which fills the SM's 512 columns (the kernel runs
+// one CTA per SM). The deeper ring lets the MMAs run further ahead of the epilogue and halves the
+// ring wraps that split an input row's MMAs (32 -> 32 at 128^3: 193 us with 8 slots, 184.5 with
+// 16; a probe without the MMA warp's waits ran 169).
+template <int N>
+constexpr int racc_slots() { return 512 / N; }
 
 template <int CIN, int N, int EPI>
 __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_constant__ CUtensorMap tmap,
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) conv_tc_kernel(const __grid_c
   constexpr int SLOT_BYTES = 3 * CB * CBLK;
   constexpr uint32_t ROW_TX = 3u * CB * SLAB * 16;  // bytes the boxes of one ring slot bring
   constexpr int NC = N / 2;
+  constexpr int RACC = racc_slots<N>();
   constexpr int TMEM_COLS = RACC * N;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sW = smem;
