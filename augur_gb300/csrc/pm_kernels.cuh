@@ -1880,8 +1880,10 @@ __device__ __forceinline__ void gather_kernel_body(const float4 *__restrict__ F4
   }
 }
 
+// six CTAs per SM (40 registers): the corner loads are latency-bound, and more resident warps hide
+// them (80 -> 74 us at 3M bodies against five CTAs at 48 registers; eight spilled and ran 86 us)
 template <int D, int MODE>
-__global__ void __launch_bounds__(256) gather_kernel(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
+__global__ void __launch_bounds__(256, 6) gather_kernel(const float4 *__restrict__ F4, float4 *__restrict__ pos4,
                                                      float4 *__restrict__ vel4, int64_t n, GatherArgs a,
                                                      float *__restrict__ acc_out, float *__restrict__ phi_out,
                                                      float *__restrict__ vel_out, uint32_t *__restrict__ key,
