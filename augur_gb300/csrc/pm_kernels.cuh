@@ -730,26 +730,41 @@ __device__ __forceinline__ void deposit_kernel_body(const float4 *__restrict__ p
     if (tid == 0) counters[blk] = 0u;
   }
 
-  // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both)
-  for (int e = tid; e < RR * G; e += nt) {
-    int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
-    // u64 -> f32 rounds correctly either way; the 32-bit conversion is a fast FP32-pipe
-    // instruction, the 64-bit one is not on this part and is only needed for sums >= 2^32
-    unsigned long long q;
-    if (gtile) {  // the split block's total, and the tile cleared for the next call
-      q = __ldcg(&gtile[e]);
-      gtile[e] = 0ull;
-    } else {
-      q = ((unsigned long long)acc_hi[e] << 13) + acc_lo[e];
-    }
+  // fixed point -> float32 density rows (MODE 0: to HBM, 1: to shared memory, 2: both), two
+  // adjacent cells per thread and iteration (G is even: 64-bit shared loads and stores)
+  // u64 -> f32 rounds correctly either way; the 32-bit conversion is a fast FP32-pipe instruction,
+  // the 64-bit one is not on this part and is only needed for sums >= 2^32
+  auto to_f32 = [&](unsigned long long q) {
     const float fq = (q >> 32) ? __ull2float_rn(q) : __uint2float_rn((unsigned)q);
-    float v = __fmul_rn(fq, qs.outscale);
+    return __fmul_rn(fq, qs.outscale);
+  };
+  for (int e = 2 * tid; e < RR * G; e += 2 * nt) {
+    int rr = (int)fdiv(e, a.fdG), x = e - rr * G;
+    unsigned long long q0, q1;
+    if (gtile) {  // the split block's total, and the tile cleared for the next call
+      q0 = __ldcg(&gtile[e]);
+      q1 = __ldcg(&gtile[e + 1]);
+      gtile[e] = 0ull;
+      gtile[e + 1] = 0ull;
+    } else {
+      const uint2 lo = *reinterpret_cast<const uint2 *>(&acc_lo[e]);
+      const uint2 hi = *reinterpret_cast<const uint2 *>(&acc_hi[e]);
+      q0 = ((unsigned long long)hi.x << 13) + lo.x;
+      q1 = ((unsigned long long)hi.y << 13) + lo.y;
+    }
+    const float2 v = make_float2(to_f32(q0), to_f32(q1));
     if (MODE != 1) {
       int zz = (int)fdiv(rr, a.fdRY), yy = rr - zz * RY;
       size_t row = (size_t)(z0 + zz) * G + (y0 + yy);
-      rho_out[row * G + x] = v;
+      float *dst = &rho_out[row * G + x];
+      if ((reinterpret_cast<uintptr_t>(rho_out) & 7) == 0) {  // a caller's array may be 4-byte aligned
+        *reinterpret_cast<float2 *>(dst) = v;
+      } else {
+        dst[0] = v.x;
+        dst[1] = v.y;
+      }
     }
-    if (MODE != 0) rows[rr * RS + x] = v;
+    if (MODE != 0) *reinterpret_cast<float2 *>(&rows[rr * RS + x]) = v;
   }
   if (MODE == 0) return;
   __syncthreads();
